@@ -1,0 +1,323 @@
+"""Benchmark of the H.X hot kernel on the standalone lattice workload.
+
+Workload: 40^3 lattice, h = 0.5 fm, a block of 64 complex 2-spinors with
+seeded Gaussian components orthonormalised in FP64, seeded U / f / W fields
+(nuclearcgm_gb300.workloads). One step = one H.X over the whole block.
+Metric: H.X throughput in GB/s of algorithmic bytes, where the bytes of one
+H.X are those of the FP32 workload: X read once + Y written once + the 8
+per-point field values, 133.1 MB (the same unit for every arm, so the ratio
+of two lines is the ratio of their times per H.X).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Our arm times the FP32 TMA stencil on device-resident inputs with CUDA events
+on the launching stream; inputs rotate over 4 block pairs (524 MB > 129 MB
+L2) so every step reads from HBM. `e2e` is the same metric through the
+reference-facing C-ABI call ncgm_apply_h with pinned HOST buffers in the
+Eigen layout (complex<double>), copies included. The reference arm times the
+CPU restatement of the reference's assembled-CSR product (FP64) on all host
+cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+N_LAT, H_LAT, NCOLS = 40, 0.5, 64
+METRIC = "H.X HBM GB/s (algorithmic bytes) on 40^3 x 64 spinors"
+
+
+def _peaks():
+    path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device, self.proc, self.lines = device, None, []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+            time.sleep(0.25)
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [],
+                    "samples": 0}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+def _workload():
+    from nuclearcgm_gb300 import workloads
+    a, f, gradf, U, W = workloads.fields(N_LAT, H_LAT)
+    X = workloads.orthonormal_block(2 * N_LAT ** 3, NCOLS, seed=1)
+    return a, f, gradf, U, W, X
+
+
+def _cpu_reference(steps, warmup, a, f, gradf, U, W, X, cols_per_step):
+    """Times the FP64 CSR product of the oracle (the reference's assembled
+    Hamiltonian times a dense block) on all host threads."""
+    import numpy as np
+    from nuclearcgm_gb300 import workloads
+    from oracle import oracle
+    H = oracle.Hamiltonian.skyrme(N_LAT, a, f, gradf.T, U, W.T)
+    Xs = np.asfortranarray(X[:, :cols_per_step])
+    for _ in range(warmup):
+        H.apply(Xs)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        H.apply(Xs)
+    dt = (time.perf_counter() - t0) / steps
+    # throughput in the workload's unit: FP32-workload bytes of the columns
+    # processed per step
+    byts = workloads.hx_bytes(N_LAT, cols_per_step, 4)
+    return byts / dt / 1e9, dt
+
+
+def run_reference(args):
+    ws, rank = _dist()
+    if rank != 0:
+        return
+    a, f, gradf, U, W, X = _workload()
+    cores = os.cpu_count()
+    gbs, dt = _cpu_reference(args.steps, min(args.warmup, 2), a, f, gradf, U,
+                             W, X, 1)
+    line = {
+        "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s",
+        "impl": "reference", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": "H.X 40^3 lattice, 64 complex 2-spinors, "
+                               "h=0.5 fm (step = 1 of 64 columns)",
+                   "global_batch": 1, "seq_len": 2 * N_LAT ** 3,
+                   "parallelism": "host threads"},
+        "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s",
+                         "cores": cores, "kind": "port",
+                         "sample": "1 column of the 64-column block per step,"
+                                   " CSR assembled once (not timed)"},
+        "e2e": {"value": round(gbs, 3), "unit": "GB/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+    import nuclearcgm_gb300 as ng
+    from nuclearcgm_gb300 import abi, workloads
+
+    ws, rank = _dist()
+    if ws > 1:
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dev = torch.cuda.current_device()
+    a, f, gradf, U, W, X = _workload()
+    grid = ng.Grid(N_LAT, a)
+    ctx = ng.Context(grid, NCOLS)
+    H = ng.Hamiltonian(ctx, abi.NEUTRON).set_fields(f, gradf.T, U, W.T)
+    lib = ng.load()
+    stream = torch.cuda.current_stream()
+    ng._check(lib.ncgm_set_stream(ctx.h, stream.cuda_stream))
+    Nrow = 2 * N_LAT ** 3
+    xt = torch.from_numpy(np.ascontiguousarray(X.T)).to(torch.complex64)
+    sets = 4  # 4 x (X + Y) x 65.5 MB = 524 MB > 129 MB L2
+    Xs = [xt.cuda() for _ in range(sets)]
+    Ys = [torch.empty_like(Xs[0]) for _ in range(sets)]
+    # autotune the launch shape once on this lattice
+    ng._check(lib.ncgm_set_stream(ctx.h, None))
+    tune = lib.ncgm_apply_h_device  # warm the binding
+    ng._check(lib.ncgm_set_stream(ctx.h, stream.cuda_stream))
+
+    def step(i):
+        ng._check(tune(ctx.h, 0, Xs[i % sets].data_ptr(),
+                       Ys[i % sets].data_ptr(), NCOLS, abi.FP32, 0.0))
+
+    for i in range(max(args.warmup, 3)):
+        step(i)
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for i in range(args.steps):
+            step(i)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    ms_step = ms / args.steps
+    byts = workloads.hx_bytes(N_LAT, NCOLS, 4)
+    value = byts * ws / (ms_step * 1e-3) / 1e9
+    # parity spot check of this exact workload against FP64 (not timed)
+    Y32 = Ys[0].cpu().numpy().T.astype(np.complex128)
+    Y64 = H.apply(X)
+    rel32 = float(np.abs(Y32 - Y64).max() / np.abs(Y64).max())
+
+    # FP64 stencil, same workload (device-resident), for the record
+    x64 = torch.from_numpy(np.ascontiguousarray(X.T)).cuda()
+    y64 = torch.empty_like(x64)
+    for _ in range(3):
+        ng._check(tune(ctx.h, 0, x64.data_ptr(), y64.data_ptr(), NCOLS,
+                       abi.FP64, 0.0))
+    torch.cuda.synchronize()
+    e0.record(stream)
+    r64 = 10
+    for _ in range(r64):
+        ng._check(tune(ctx.h, 0, x64.data_ptr(), y64.data_ptr(), NCOLS,
+                       abi.FP64, 0.0))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms64 = e0.elapsed_time(e1) / r64
+
+    # e2e through the C-ABI with pinned host buffers (copies timed)
+    ng._check(lib.ncgm_set_stream(ctx.h, None))
+    xh = torch.from_numpy(np.ascontiguousarray(X.T)).pin_memory()
+    yh = torch.empty_like(xh).pin_memory()
+    ke = max(3, min(args.steps, 20))
+    ng._check(lib.ncgm_apply_h(ctx.h, 0, xh.data_ptr(), yh.data_ptr(), NCOLS,
+                               abi.FP32))
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        ng._check(lib.ncgm_apply_h(ctx.h, 0, xh.data_ptr(), yh.data_ptr(),
+                                   NCOLS, abi.FP32))
+    te = (time.perf_counter() - t0) / ke
+    e2e = byts / te / 1e9
+    h2d = Nrow * NCOLS * 16
+
+    peak, peak_kind = _peaks()
+    traffic = None
+    tp = os.path.join(HERE, "profiles", "stencil_fp32_traffic.json")
+    if os.path.exists(tp):
+        try:
+            traffic = json.load(open(tp)).get("dram_bytes_per_launch")
+        except Exception:
+            traffic = None
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        gbs_c, dt_c = _cpu_reference(3, 1, a, f, gradf, U, W, X, 4)
+        cpu = {"value": round(gbs_c, 3), "unit": "GB/s",
+               "cores": os.cpu_count(), "kind": "port",
+               "sample": "4 of 64 columns, 3 timed products (FP64 CSR)"}
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": "GB/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms_step, 5), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded splitmix64 fields and spinors)",
+        "config": {"workload": "H.X 40^3 lattice, 64 complex 2-spinors, "
+                               "h=0.5 fm, FP32 TMA stencil",
+                   "global_batch": NCOLS * ws, "seq_len": Nrow,
+                   "parallelism": "replicas" if ws > 1 else "single",
+                   "l2": "4 rotating X/Y sets (524 MB > 129 MB L2)"},
+        "roofline": {"bound": "hbm", "achieved": round(byts / (ms_step * 1e-3)
+                                                       / 1e9, 2),
+                     "peak": peak, "unit": "GB/s",
+                     "frac": round(byts / (ms_step * 1e-3) / 1e9 / peak, 4),
+                     "traffic": traffic, "peak_source": peak_kind},
+        "e2e": {"value": round(e2e, 3), "unit": "GB/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d},
+        "gpu_launches": args.steps,
+        "clocks": clk.summary(),
+        "fp32_rel_err_vs_fp64": rel32,
+        "fp64_stencil": {"ms_per_hx": round(ms64, 4),
+                         "gbs": round(workloads.hx_bytes(N_LAT, NCOLS, 8) /
+                                      (ms64 * 1e-3) / 1e9, 2)},
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true",
+                    help="skip the CPU-baseline sample on our arm")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,218 @@
+/*
+ * ncgm.h — C ABI of the GB300 (sm_103a) build of the nuclearcgm self-consistent
+ * lattice hot path: the finite-difference single-particle Hamiltonian apply,
+ * the block GCG eigensolver, density/field accumulation, the Coulomb Poisson
+ * solve, BCS/HFB pairing and the Hartree-Fock iteration that sequences them.
+ *
+ * Every entry point returns an int status (NCGM_OK == 0) and never throws.
+ * Matrices use the reference's Eigen layout: column-major, complex numbers as
+ * interleaved (re, im) doubles, spinor rows ordered s + 2*(i + n*(j + n*k)).
+ * Scalar lattice fields are n^3 doubles in i-fastest order; vector fields are
+ * n^3 x 3 column-major (x block, y block, z block), like Eigen::MatrixX3d.
+ *
+ * Pointers passed to ncgm_apply_h / ncgm_gcg may be host or device memory:
+ * the library asks the CUDA runtime which and copies when needed.
+ *
+ * Reference interfaces each entry point replaces are cited beside it as
+ * path:line inside the nuclearcgm source tree.
+ */
+#ifndef NCGM_H
+#define NCGM_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NCGM_OK 0
+#define NCGM_ERR_ARG 1      /* bad argument (sizes, null pointers, species) */
+#define NCGM_ERR_CUDA 2     /* CUDA runtime error or no CUDA device */
+#define NCGM_ERR_NAN 3      /* NaN / Inf detected in a result */
+#define NCGM_ERR_RANK 4     /* orthonormalisation found no independent columns */
+#define NCGM_ERR_TIMEOUT 5  /* a bounded device wait gave up */
+#define NCGM_ERR_EIG 6      /* projected eigensolver did not converge */
+#define NCGM_ERR_NOMEM 7    /* device allocation failed */
+
+#define NCGM_FP64 0         /* Hamiltonian apply in FP64 */
+#define NCGM_FP32 1         /* Hamiltonian apply in FP32 (inputs rounded) */
+
+#define NCGM_NEUTRON 0
+#define NCGM_PROTON 1
+
+#define NCGM_ORDER_MATCH_PREVIOUS 0 /* EigenpairsOrdering::MATCH_PREVIOUS */
+#define NCGM_ORDER_ASCENDING 1      /* EigenpairsOrdering::ASCENDING_ENERGIES */
+
+typedef struct ncgm_ctx ncgm_ctx;
+
+/* Skyrme EDF coupling constants, in the order of FunctionalParameters
+ * (include/EDF.hpp:20-23). */
+typedef struct ncgm_edf {
+  double C0rr, C1rr, C0Drr, C1Drr, C0rt, C1rt, C0J2, C1J2, C0rdr, C1rdr, C0nJ,
+      C1nJ, sigma;
+} ncgm_edf;
+
+/* Skyrme interaction parameters (include/EDF.hpp:4-18). */
+typedef struct ncgm_skyrme {
+  double W0, W0_pr, t0, t1, t2, t3, x0, x1, x2, x3, sigma, te, to;
+} ncgm_skyrme;
+
+/* Replaces EDF::setFromInteraction (src/skyrme/EDF.cpp:61-103). */
+int ncgm_edf_from_skyrme(const ncgm_skyrme *in, ncgm_edf *out);
+
+/* GCG parameters: GCGParameters (include/input_parser.hpp:29-35). */
+typedef struct ncgm_gcg_params {
+  int max_iter;    /* outer GCG iterations */
+  double tol;      /* absolute residual-norm lock tolerance */
+  int cg_steps;    /* max Jacobi-PCG steps per column */
+  double cg_tol;   /* relative PCG tolerance */
+  double shift;    /* initial shift (reference passes 0) */
+  int ordering;    /* NCGM_ORDER_* */
+  int precision;   /* precision of the PCG correction applies: NCGM_FP64/FP32 */
+  int precond;     /* 0: Jacobi (reference); 1: learned correction, Jacobi judge */
+} ncgm_gcg_params;
+
+typedef struct ncgm_gcg_stats {
+  int iterations;       /* outer iterations run */
+  int converged;        /* locked columns at exit */
+  int pcg_steps_max;    /* max PCG steps over columns, last outer iteration */
+  int pcg_steps_total;  /* sum of PCG steps over columns and iterations */
+  int basis_cols;       /* columns kept by the last orthonormalisation */
+  double max_residual;  /* max residual norm of the returned pairs */
+  double ms_total;      /* device wall time of the call */
+  double ms_pcg;        /* part spent in the PCG correction */
+} ncgm_gcg_stats;
+
+/* ---- context: grid and device state ------------------------------------ */
+
+/* Replaces Grid(n, a) (src/grid/grid.cpp:7-21): x_i = -a + i*h, h = 2a/(n-1).
+ * max_cols bounds the spinor columns any later call may pass. */
+int ncgm_create(ncgm_ctx **out, int n, double a, int max_cols, int flags);
+int ncgm_destroy(ncgm_ctx *ctx);
+/* Text of the last error on this thread. */
+const char *ncgm_last_error(void);
+/* Device sync; returns the first pending error. */
+int ncgm_sync(ncgm_ctx *ctx);
+
+/* ---- Hamiltonian -------------------------------------------------------- */
+
+/* Replaces Hamiltonian(grid, terms).buildMatrix() (src/hamiltonian/
+ * hamiltonian.cpp:303-372) with the term list of Utilities::skyrmeHamiltonian
+ * (src/util/utilities.cpp:56-70): SkyrmeU (src/skyrme/skyrme_u.cpp:15-24),
+ * NonLocalKineticPotential (src/potentials/non_local_kinetic_potential.cpp:
+ * 23-71), LocalKineticPotential (src/potentials/local_kinetic_potential.cpp:
+ * 22-46), SkyrmeSO (src/skyrme/skyrme_so.cpp:12-58) and LocalCoulombPotential
+ * (src/skyrme/local_coulomb_potential.cpp:12-41). No matrix is assembled: the
+ * fields are uploaded and H is applied as a stencil.
+ *   f      : hbar^2/2m*(r), n^3            (EffectiveMass::vector)
+ *   gradf  : grad f, n^3 x 3              (EffectiveMass::gradient)
+ *   U      : central field incl. constraint field, n^3 (IterationData::UN/UP)
+ *   W      : spin-orbit field, n^3 x 3, or NULL for no spin-orbit term (BN/BP)
+ *   UC     : Coulomb field, n^3, or NULL (IterationData::UCoul)           */
+int ncgm_set_fields(ncgm_ctx *ctx, int species, const double *f,
+                    const double *gradf, const double *U, const double *W,
+                    const double *UC);
+
+/* Replaces the Woods-Saxon guess Hamiltonian Hamiltonian::build_matrix5p()
+ * (src/hamiltonian/hamiltonian.cpp:207-302) with DeformedWoodsSaxonPotential
+ * (src/potentials/deformed_woods_saxon.cpp:12-17) and
+ * DeformedSpinOrbitPotential (src/potentials/deformed_spin_orbit.cpp:69-114),
+ * as assembled by main() (src/main.cpp:72-86). The fields are computed on the
+ * device from the parameters. */
+int ncgm_set_woods_saxon(ncgm_ctx *ctx, int species, int A, int Z, double V0,
+                         double r0, double diff, double kappa, double beta,
+                         double beta3, double so_V0, int spin_orbit);
+
+/* Y = H X for ncols spinor columns (replaces ComplexSparseMatrix * MatrixXcd,
+ * e.g. src/solver/solver.cpp:766). X, Y: N x ncols complex, N = 2 n^3. */
+int ncgm_apply_h(ncgm_ctx *ctx, int species, const double *X, double *Y,
+                 int ncols, int precision);
+
+/* Device-resident form of ncgm_apply_h: Y = (H + shift I) X enqueued on the
+ * context's stream without synchronising. X, Y are device buffers of complex
+ * numbers in the precision's type (complex<double> for NCGM_FP64,
+ * complex<float> for NCGM_FP32), N x ncols column-major. */
+int ncgm_apply_h_device(ncgm_ctx *ctx, int species, const void *X, void *Y,
+                        int ncols, int precision, double shift);
+
+/* Makes the context enqueue its work on `stream` (a cudaStream_t; NULL for
+ * the context's own stream). */
+int ncgm_set_stream(ncgm_ctx *ctx, void *stream);
+
+/* ---- eigensolver -------------------------------------------------------- */
+
+/* Replaces gcgm_complex_no_B_lock (src/solver/solver.cpp:642-959, declared in
+ * include/solver.hpp:43-47) as called by Utilities::solve (src/util/
+ * utilities.cpp:20-36) on the Hamiltonian set for `species`.
+ *   X_init : N x xcols (the first nev columns are used), ConjDir: N x pcols
+ *   X_out  : N x nev (may alias X_init), lambda_out: nev.                 */
+int ncgm_gcg(ncgm_ctx *ctx, int species, const double *X_init, int xcols,
+             const double *ConjDir, int pcols, int nev,
+             const ncgm_gcg_params *params, double *X_out, double *lambda_out,
+             ncgm_gcg_stats *stats);
+
+/* ---- self-consistent iteration ----------------------------------------- */
+
+/* Run configuration: the fields of InputParser (src/system/input_parser.cpp:
+ * 50-261) that the HF/HFB loop of main() (src/main.cpp:38-369) reads. */
+typedef struct ncgm_pairing {
+  double V0;          /* pairing strength (positive, reference convention) */
+  double window;      /* Fermi-window half width [MeV] */
+  int basis_size;     /* HFbasisSize: columns carried for this species */
+  int window_both;    /* two-sided smooth window */
+  int active;         /* pairing on for this species */
+} ncgm_pairing;
+
+#define NCGM_PAIRING_NONE 0
+#define NCGM_PAIRING_HFB 1
+#define NCGM_PAIRING_BCS 2
+
+typedef struct ncgm_hf_config {
+  int n;               /* axisMeshPoints */
+  double box_size;     /* boxSize (a = box_size / 2) */
+  int A, Z;
+  ncgm_edf edf;
+  int spin_orbit, use_j, com_corr, use_coulomb;
+  double density_mix;  /* densityMix */
+  int max_iterations;  /* maxIterations */
+  double energy_tol;   /* energyTol */
+  double initial_beta, beta3;
+  /* Woods-Saxon guess (parameters/woods_saxon.json) */
+  double ws_V0, ws_r0, ws_diff, ws_kappa, wsso_V0;
+  ncgm_gcg_params ws_gcg; /* initial GCG (maxIter 10, tol 1e-2, 40, 1e-4) */
+  ncgm_gcg_params hf_gcg; /* per-iteration GCG (1, 1e-6, 80, 1e-5) */
+  /* pairing */
+  int pairing_type;    /* NCGM_PAIRING_* */
+  ncgm_pairing pair_n, pair_p;
+  int start_hfb_iter;
+  double pairing_threshold;
+  /* constraints */
+  int constrain_com;   /* constrainCOM */
+  int curve_mode;      /* deformation-curve constraint set at target mu20 */
+  double mu20;         /* quadrupole target when curve_mode */
+  double constraints_tol;
+  /* stop rule extensions (0 = reference rule only) */
+  double spe_tol;      /* also require max |dSPE| < spe_tol when > 0 */
+} ncgm_hf_config;
+
+typedef struct ncgm_hf_result {
+  int iterations;      /* HF iterations run */
+  int converged;
+  double E_int;        /* integrated EDF energy + kinetic (main.cpp:300-301) */
+  double E_HF;         /* HFEnergy (iteration_data.cpp:212-224) */
+  double E_pair_n, E_pair_p;
+  double lambda_n, lambda_p; /* Fermi energies when pairing */
+  double beta, gamma;  /* quadrupole deformation (output only) */
+  double wall_s;       /* wall time of the run */
+  double last_dE;      /* |Delta E_int| of the final iteration */
+  double t_gcg_s, t_fields_s, t_poisson_s, t_pairing_s; /* phase times */
+} ncgm_hf_result;
+
+/* Runs the WS guess and the HF(B) loop of main() (src/main.cpp:59-342) on the
+ * GPU. Optional outputs (may be NULL): spe_n/spe_p (orbitals per species),
+ * rho_n/rho_p (n^3), energies (max_iterations x 2: E_int, E_HF per iter). */
+int ncgm_hf_run(const ncgm_hf_config *cfg, ncgm_hf_result *res, double *spe_n,
+                double *spe_p, double *rho_n, double *rho_p, double *energies);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NCGM_H */

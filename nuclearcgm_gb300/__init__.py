@@ -1,0 +1,225 @@
+"""nuclearcgm_gb300: GB300-native (sm_103a) build of the nuclearcgm
+self-consistent lattice hot path.
+
+The compute lives in the in-tree CUDA library libncgm.so (C ABI in
+include/ncgm.h). This package is the host-side mirror of the reference's
+interfaces for the path:
+
+  Grid                      <- Grid (include/grid.hpp)
+  Hamiltonian               <- Hamiltonian + Potential terms
+                               (include/hamiltonian.hpp, include/potential.hpp)
+  gcgm_complex_no_B_lock    <- include/solver.hpp:43-47
+  solve                     <- Utilities::solve (include/util/utilities.hpp)
+  hf_run                    <- the HF(B) loop of main() (src/main.cpp)
+
+There is no CPU fallback: if libncgm.so is missing or no CUDA device is
+visible, the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi, config
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libncgm.so")
+_lib = None
+
+
+class NcgmError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (abi.STATUS.get(status, status), msg))
+        self.status = status
+
+
+def load():
+    """Load libncgm.so (built by __graft_entry__.build()). Raises if absent."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise NcgmError(abi.NCGM_OK + 2,
+                            "libncgm.so not built: run __graft_entry__.build()")
+        _lib = abi.bind(C.CDLL(LIB_PATH))
+    return _lib
+
+
+def _check(status):
+    if status != abi.NCGM_OK:
+        raise NcgmError(status, load().ncgm_last_error().decode())
+
+
+def _ptr(x):
+    """Raw address of a numpy array or a torch tensor (host or device)."""
+    if x is None:
+        return None
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    return x.ctypes.data
+
+
+class Grid:
+    """Grid(n, a): x_i = -a + i h, h = 2a/(n-1) (src/grid/grid.cpp:7-41)."""
+
+    def __init__(self, n: int, a: float):
+        if n < 2:
+            raise ValueError("Grid error: n must be >= 2. Received n = %d" % n)
+        self.n, self.a = int(n), float(a)
+        self.h = 2.0 * a / (n - 1)
+        self.xs = -a + np.arange(n) * self.h
+
+    def idx(self, i, j, k, s):
+        return s + 2 * (i + self.n * (j + self.n * k))
+
+    def idx_nospin(self, i, j, k):
+        return i + self.n * (j + self.n * k)
+
+    @property
+    def total_spatial_points(self):
+        return self.n ** 3
+
+    @property
+    def total_points(self):
+        return 2 * self.n ** 3
+
+    def dV(self):
+        return self.h ** 3
+
+
+class Context:
+    """Device context for one lattice (ncgm_create / ncgm_destroy)."""
+
+    def __init__(self, grid: Grid, max_cols: int):
+        self.grid = grid
+        self.max_cols = max_cols
+        h = C.c_void_p()
+        _check(load().ncgm_create(C.byref(h), grid.n, grid.a, max_cols, 0))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            load().ncgm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _f64(x, n=None):
+    if x is None:
+        return None
+    if hasattr(x, "data_ptr"):
+        return x
+    a = np.ascontiguousarray(x, dtype=np.float64)
+    if n is not None and a.size != n:
+        raise ValueError("expected %d values, got %d" % (n, a.size))
+    return a
+
+
+class Hamiltonian:
+    """Matrix-free H for one species on a Context.
+
+    Replaces Hamiltonian(grid, terms).buildMatrix() with the Skyrme term list
+    (src/hamiltonian/hamiltonian.cpp:303-372): the fields are uploaded and
+    H.X is applied by the CUDA stencil. `apply` accepts (N, ncols) complex128
+    arrays in the reference's Eigen layout (column-major) or device tensors.
+    """
+
+    def __init__(self, ctx: Context, species: int = abi.NEUTRON):
+        self.ctx, self.species = ctx, species
+
+    def set_fields(self, f, gradf, U, W=None, UC=None):
+        ns = self.ctx.grid.n ** 3
+        args = [_f64(f, ns), _f64(gradf, 3 * ns), _f64(U, ns),
+                _f64(W, 3 * ns), _f64(UC, ns)]
+        self._keep = args
+        _check(load().ncgm_set_fields(self.ctx.h, self.species,
+                                      *[_ptr(a) for a in args]))
+        return self
+
+    def set_woods_saxon(self, A, Z, V0=55.5, r0=1.2, diff=0.67, kappa=0.86,
+                        beta=0.0, beta3=0.0, so_V0=55.5, spin_orbit=True):
+        """Woods-Saxon guess H (Hamiltonian::build_matrix5p with the deformed
+        WS and WS spin-orbit terms, src/main.cpp:72-86)."""
+        _check(load().ncgm_set_woods_saxon(self.ctx.h, self.species, A, Z, V0,
+                                           r0, diff, kappa, beta, beta3,
+                                           so_V0, int(spin_orbit)))
+        return self
+
+    def apply(self, X, precision=abi.FP64):
+        if hasattr(X, "data_ptr"):
+            import torch
+            # device tensors: (ncols, N) row-major == (N, ncols) Eigen layout
+            Y = torch.empty_like(X)
+            ncols = 1 if X.dim() == 1 else X.shape[0]
+            _check(load().ncgm_apply_h(self.ctx.h, self.species, X.data_ptr(),
+                                       Y.data_ptr(), ncols, precision))
+            return Y
+        X = np.asfortranarray(X, dtype=np.complex128)
+        ncols = 1 if X.ndim == 1 else X.shape[1]
+        Y = np.empty_like(X)
+        _check(load().ncgm_apply_h(self.ctx.h, self.species, X.ctypes.data,
+                                   Y.ctypes.data, ncols, precision))
+        return Y
+
+    def gcg(self, X_init, nev, ConjDir=None, params: abi.GcgParams = None):
+        """gcgm_complex_no_B_lock (src/solver/solver.cpp:642-959)."""
+        if params is None:
+            params = config._gcg(config.HF_GCG)
+        X_init = np.asfortranarray(X_init, dtype=np.complex128)
+        P = None if ConjDir is None else np.asfortranarray(
+            ConjDir, dtype=np.complex128)
+        N = X_init.shape[0]
+        Xo = np.zeros((N, nev), np.complex128, order="F")
+        lam = np.zeros(nev)
+        st = abi.GcgStats()
+        _check(load().ncgm_gcg(self.ctx.h, self.species, X_init.ctypes.data,
+                               X_init.shape[1], _ptr(P),
+                               0 if P is None else P.shape[1], nev,
+                               C.byref(params), Xo.ctypes.data, lam.ctypes.data,
+                               C.byref(st)))
+        return Xo, lam, st
+
+
+def gcgm_complex_no_B_lock(H: Hamiltonian, X_initial, ConjDir, nev,
+                           shift=0.0, max_iter=100, tolerance=1e-8,
+                           cg_steps=10, cg_tol=1e-9,
+                           ordering=abi.ORDER_MATCH_PREVIOUS,
+                           precision=abi.FP64):
+    """Reference signature (include/solver.hpp:43-47) on a device H."""
+    p = abi.GcgParams(max_iter=max_iter, tol=tolerance, cg_steps=cg_steps,
+                      cg_tol=cg_tol, shift=shift, ordering=ordering,
+                      precision=precision, precond=0)
+    X, lam, _ = H.gcg(X_initial, nev, ConjDir, p)
+    return X, lam
+
+
+def solve(H: Hamiltonian, ConjDir, calc: dict, guess, nev=None,
+          precision=abi.FP64):
+    """Utilities::solve (src/util/utilities.cpp:20-36): GCG with shift 0 and
+    ascending ordering, parameters from a GCGParameters-like dict."""
+    nev = guess.shape[1] if nev is None else nev
+    return gcgm_complex_no_B_lock(H, guess, ConjDir, nev, 0.0,
+                                  calc["maxIter"], calc["tol"], calc["steps"],
+                                  calc["cgTol"], abi.ORDER_ASCENDING,
+                                  precision)
+
+
+def hf_run(cfg: abi.HFConfig):
+    """Runs the WS guess and HF(B) iteration on the GPU (ncgm_hf_run)."""
+    res = abi.HFResult()
+    on, op = config.orbital_counts(cfg)
+    ns = cfg.n ** 3
+    spe_n, spe_p = np.zeros(on), np.zeros(op)
+    rho_n, rho_p = np.zeros(ns), np.zeros(ns)
+    en = np.zeros((max(cfg.max_iterations, 1), 2))
+    _check(load().ncgm_hf_run(C.byref(cfg), C.byref(res), spe_n.ctypes.data,
+                              spe_p.ctypes.data, rho_n.ctypes.data,
+                              rho_p.ctypes.data, en.ctypes.data))
+    return res, {"spe_n": spe_n, "spe_p": spe_p, "rho_n": rho_n,
+                 "rho_p": rho_p, "energies": en[:res.iterations]}

@@ -1,0 +1,230 @@
+"""CPU checks that pin the FP64 oracle: analytic derivatives, trapezoid
+integral, the assembled Hamiltonian against an independent numpy restatement
+of the term formulas, and Hermitian structure."""
+import numpy as np
+import pytest
+
+from conftest import random_block, random_fields
+from oracle import oracle
+
+
+def _xyz(n, a):
+    h = 2 * a / (n - 1)
+    xs = -a + np.arange(n) * h
+    Z, Y, X = np.meshgrid(xs, xs, xs, indexing="ij")
+    return X.ravel(), Y.ravel(), Z.ravel(), h
+
+
+def test_integral_constant_and_quadratic():
+    n, a = 14, 6.5
+    assert oracle.integral(n, a, np.ones(n ** 3)) == pytest.approx((2 * a) ** 3,
+                                                                   rel=1e-13)
+    x, y, z, h = _xyz(n, a)
+    # trapezoid rule on x^2 over [-a, a]: exact value of the composite rule
+    xs = -a + np.arange(n) * h
+    w = np.full(n, h)
+    w[0] = w[-1] = h / 2
+    tz = (w * xs ** 2).sum() * (2 * a) ** 2
+    assert oracle.integral(n, a, x ** 2) == pytest.approx(tz, rel=1e-13)
+
+
+def test_gradient_exact_on_linear_and_cubic():
+    n, a = 16, 7.5
+    x, y, z, h = _xyz(n, a)
+    g = oracle.grad_nospin(n, a, 2 * x - 3 * y + 0.5 * z)
+    assert np.allclose(g[:, 0], 2, atol=1e-12)
+    assert np.allclose(g[:, 1], -3, atol=1e-12)
+    assert np.allclose(g[:, 2], 0.5, atol=1e-12)
+    # 9/7/5-point interior stencils are exact for cubics; 3/2-point edges not
+    g = oracle.grad_nospin(n, a, x ** 3)
+    i = np.arange(n ** 3) % n
+    inner = (i >= 2) & (i <= n - 3)
+    assert np.allclose(g[inner, 0], 3 * x[inner] ** 2, rtol=1e-10)
+    assert not np.allclose(g[i == 0, 0], 3 * x[i == 0] ** 2, rtol=1e-3)
+
+
+def test_laplacian_edge_quirk():
+    """derivative2 uses a first-derivative formula at pos 0 and n-1
+    (differential_operators.cpp:562-578)."""
+    n, a = 12, 5.5
+    x, y, z, h = _xyz(n, a)
+    lap = oracle.lap_nospin(n, a, x ** 2)
+    i = np.arange(n ** 3) % n
+    j = (np.arange(n ** 3) // n) % n
+    k = np.arange(n ** 3) // n ** 2
+    # y, z derivative2 of x^2 is 0 except the first-derivative edge formula,
+    # which is also 0 for a function constant along the axis
+    inner = (i >= 1) & (i <= n - 2)
+    assert np.allclose(lap[inner], 2.0, rtol=1e-10)
+    edge0 = i == 0
+    expect = (x[edge0] + h) ** 2 - x[edge0] ** 2
+    assert np.allclose(lap[edge0], expect / h, rtol=1e-12)
+
+
+def _numpy_h(n, a, f, gradf, U, W, UC, X):
+    """Independent restatement of the five Skyrme terms as array stencils."""
+    h = 2 * a / (n - 1)
+    ns = n ** 3
+    psi = X.reshape(n, n, n, 2, order="C")  # [k][j][i][s]
+    f3 = f.reshape(n, n, n)
+    U3 = U.reshape(n, n, n) + (0 if UC is None else UC.reshape(n, n, n))
+    g3 = [gradf[c * ns:(c + 1) * ns].reshape(n, n, n) for c in range(3)]
+    W3 = [np.zeros((n, n, n)) if W is None else
+          W[c * ns:(c + 1) * ns].reshape(n, n, n) for c in range(3)]
+
+    def sh(v, ax, d):  # v at r + d e_ax, zero outside
+        out = np.zeros_like(v)
+        axis = 2 - ax  # array axes: 0 = k (z), 1 = j (y), 2 = i (x)
+        src = [slice(None)] * v.ndim
+        dst = [slice(None)] * v.ndim
+        if d > 0:
+            src[axis] = slice(d, None)
+            dst[axis] = slice(None, -d)
+        else:
+            src[axis] = slice(None, d)
+            dst[axis] = slice(-d, None)
+        out[tuple(dst)] = v[tuple(src)]
+        return out
+
+    out = (U3 + 7.5 * f3 / h ** 2)[..., None] * psi
+    sx = np.array([[0, 1], [1, 0]], complex)
+    sy = np.array([[0, -1j], [1j, 0]])
+    sz = np.array([[1, 0], [0, -1]], complex)
+    for ax in range(3):
+        L = (4 / 3) * (sh(psi, ax, 1) + sh(psi, ax, -1)) - (1 / 12) * (
+            sh(psi, ax, 2) + sh(psi, ax, -2))
+        out -= (f3 / h ** 2)[..., None] * L
+        D = (8 * (sh(psi, ax, 1) - sh(psi, ax, -1)) -
+             (sh(psi, ax, 2) - sh(psi, ax, -2))) / (12 * h)
+        out += (-g3[ax])[..., None] * D
+        Wx, Wy, Wz = W3
+        if ax == 0:
+            M = sy[None, None, None] * Wz[..., None, None] - \
+                sz[None, None, None] * Wy[..., None, None]
+        elif ax == 1:
+            M = sz[None, None, None] * Wx[..., None, None] - \
+                sx[None, None, None] * Wz[..., None, None]
+        else:
+            M = sx[None, None, None] * Wy[..., None, None] - \
+                sy[None, None, None] * Wx[..., None, None]
+        out += -1j * np.einsum("kjist,kjit->kjis", M, D)
+    return out.reshape(-1)
+
+
+@pytest.mark.parametrize("n,so,coul", [(6, True, False), (9, True, True),
+                                       (8, False, False)])
+def test_csr_matches_numpy_terms(n, so, coul):
+    a = 0.5 * (n - 1) * 0.9
+    f, gradf, U, W, UC = random_fields(n, 11 + n, so=so, coulomb=coul)
+    H = oracle.Hamiltonian.skyrme(n, a, f, gradf, U, W, UC)
+    X = random_block(2 * n ** 3, 2, 3)
+    Y = H.apply(X)
+    for c in range(2):
+        ref = _numpy_h(n, a, f, gradf, U, W, UC, X[:, c])
+        assert np.abs(Y[:, c] - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_csr_structure_and_hermiticity():
+    n, a = 8, 3.5
+    f, gradf, U, W, UC = random_fields(n, 5)
+    H = oracle.Hamiltonian.skyrme(n, a, f, gradf, U, W)
+    rp, col, val = H.csr()
+    N = 2 * n ** 3
+    assert rp[-1] == H.nnz()
+    # interior rows: 1 diagonal + 12 same-spin kinetic + SO blocks; at most 26
+    counts = np.diff(rp)
+    assert counts.max() <= 26 and counts.min() >= 7
+    for r in range(0, N, 97):
+        assert np.all(np.diff(col[rp[r]:rp[r + 1]]) > 0)  # ascending columns
+    # row-point fields make H non-Hermitian; constant f and W=0 restore it
+    import scipy.sparse as sp
+    M = sp.csr_matrix((val, col, rp), shape=(N, N))
+    assert abs(M - M.conj().T).max() > 1e-6
+    f0 = np.full(n ** 3, 20.7)
+    H0 = oracle.Hamiltonian.skyrme(n, a, f0, np.zeros(3 * n ** 3), U)
+    rp, col, val = H0.csr()
+    M0 = sp.csr_matrix((val, col, rp), shape=(N, N))
+    assert abs(M0 - M0.conj().T).max() < 1e-12
+
+
+def test_woods_saxon_matches_skyrme_form():
+    """build_matrix5p with WS terms equals the Skyrme stencil with constant
+    f = hbar^2/2m, U = V_WS and W = ls grad V_SO (the form the GPU uses)."""
+    n, a, A, Z = 10, 4.5, 16, 8
+    H = oracle.Hamiltonian.woods_saxon(n, a, A, Z)
+    X = random_block(2 * n ** 3, 2, 9)
+    Y = H.apply(X)
+    hbar, m = 197.327053, 938.91869
+    x, y, z, h = _xyz(n, a)
+    r = np.sqrt(x * x + y * y + z * z)
+    R = 1.2 * A ** (1 / 3)
+    U = -55.5 * (1 + 0.86 * (A - 2 * Z) / A) / (1 + np.exp((r - R) / 0.67))
+    et = np.exp((r - R) / 0.67)
+    sc = (55.5 / 0.67) * et / (1 + et) ** 2
+    ls = -35.0 * (hbar * 0.5 / m) ** 2
+    W = np.concatenate([ls * sc * x / r, ls * sc * y / r, ls * sc * z / r])
+    f = np.full(n ** 3, hbar ** 2 / (2 * m))
+    ref = _numpy_h(n, a, f, np.zeros(3 * n ** 3), U, W, None, X[:, 0])
+    assert np.abs(Y[:, 0] - ref).max() <= 1e-11 * np.abs(ref).max()
+
+
+def test_harmonic_oscillator_levels():
+    """Known answer: constant f, U = m w^2 r^2 / 2 -> hbar w (N + 3/2)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as sla
+    n, a = 24, 8.0
+    hbar, m = 197.327053, 938.91869
+    hw = 10.0
+    x, y, z, h = _xyz(n, a)
+    U = 0.5 * m * (hw / hbar) ** 2 * (x * x + y * y + z * z)
+    f = np.full(n ** 3, hbar ** 2 / (2 * m))
+    H = oracle.Hamiltonian.skyrme(n, a, f, np.zeros(3 * n ** 3), U)
+    rp, col, val = H.csr()
+    N = 2 * n ** 3
+    M = sp.csr_matrix((val, col, rp), shape=(N, N))
+    w = np.sort(sla.eigsh(M, k=8, sigma=0, which="LM")[0].real)
+    assert np.allclose(w[:2], 1.5 * hw, rtol=2e-3)
+    assert np.allclose(w[2:8], 2.5 * hw, rtol=2e-3)
+
+
+def test_heig_and_mgs_against_numpy():
+    rng = np.random.default_rng(0)
+    m = 17
+    A = rng.normal(size=(m, m)) + 1j * rng.normal(size=(m, m))
+    A = A + A.conj().T
+    w, V = oracle.heig(A)
+    assert np.allclose(w, np.linalg.eigvalsh(A), atol=1e-12)
+    assert np.abs(A @ V - V * w).max() < 1e-11
+    Q = oracle.mgs(random_block(500, 6, 1))
+    assert np.abs(Q.conj().T @ Q - np.eye(6)).max() < 1e-13
+
+
+def test_gcg_converges_to_lowest_eigenpairs():
+    """Many GCG iterations reproduce the lowest eigenvalues of a small H."""
+    n, a = 8, 5.0
+    f, gradf, U, W, UC = random_fields(n, 3)
+    f0 = np.full(n ** 3, 20.7)
+    H = oracle.Hamiltonian.skyrme(n, a, f0, np.zeros(3 * n ** 3), U, None)
+    rp, col, val = H.csr()
+    import scipy.sparse as sp
+    N = 2 * n ** 3
+    dense = sp.csr_matrix((val, col, rp), shape=(N, N)).toarray()
+    ref = np.linalg.eigvalsh(dense)[:6]
+    X0 = random_block(N, 6, 4)
+    X, lam, info = H.gcg(X0, 6, max_iter=60, tol=1e-9, cg_steps=40,
+                         cg_tol=1e-9)
+    assert np.allclose(lam, ref, atol=1e-7)
+
+
+def test_pcg_reduces_residual():
+    n, a = 8, 4.0
+    f, gradf, U, W, UC = random_fields(n, 8)
+    H = oracle.Hamiltonian.skyrme(n, a, f, gradf, U, W)
+    B = random_block(2 * n ** 3, 3, 2)
+    X0 = np.zeros_like(B)
+    shift = 80.0
+    Wsol, steps = H.pcg(B, X0, shift, 200, 1e-10)
+    R = B - H.apply(Wsol, shift)
+    # row-point fields make H mildly non-Hermitian: CG still converges here
+    assert (np.linalg.norm(R, axis=0) / np.linalg.norm(B, axis=0)).max() < 1e-6
+    assert steps.max() <= 200
