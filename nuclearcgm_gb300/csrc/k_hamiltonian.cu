@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(256) stencilPlanes32(PlaneArgs A) {
   }
   // phase of each slot flips every time it is refilled
   bool ok = true;
-  const uint32_t kLimit = 1u << 26;
+  const uint32_t kLimit = 1u << 22;
   int waitedUpTo = zlo - 1; // highest plane confirmed resident
   const int bandPts = (y1 - y0) * n;
   for (int k = k0; k < k1; ++k) {
