@@ -182,17 +182,16 @@ def run_ours(args):
     ctx = ng.Context(grid, NCOLS)
     H = ng.Hamiltonian(ctx, abi.NEUTRON).set_fields(f, gradf.T, U, W.T)
     lib = ng.load()
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream: kernels and CUDA events share it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ng._check(lib.ncgm_set_stream(ctx.h, stream.cuda_stream))
     Nrow = 2 * N_LAT ** 3
     xt = torch.from_numpy(np.ascontiguousarray(X.T)).to(torch.complex64)
     sets = 4  # 4 x (X + Y) x 65.5 MB = 524 MB > 129 MB L2
     Xs = [xt.cuda() for _ in range(sets)]
     Ys = [torch.empty_like(Xs[0]) for _ in range(sets)]
-    # autotune the launch shape once on this lattice
-    ng._check(lib.ncgm_set_stream(ctx.h, None))
-    tune = lib.ncgm_apply_h_device  # warm the binding
-    ng._check(lib.ncgm_set_stream(ctx.h, stream.cuda_stream))
+    tune = lib.ncgm_apply_h_device
 
     def step(i):
         ng._check(tune(ctx.h, 0, Xs[i % sets].data_ptr(),

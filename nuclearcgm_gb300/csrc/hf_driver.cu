@@ -2,12 +2,6 @@
 // entry points; filled in by the GCG / HF implementation.
 #include "ncgm_internal.cuh"
 
-extern "C" int ncgm_gcg(ncgm_ctx *, int, const double *, int, const double *,
-                        int, int, const ncgm_gcg_params *, double *, double *,
-                        ncgm_gcg_stats *) {
-  ncgm::setError("ncgm_gcg: not available in this build");
-  return NCGM_ERR_ARG;
-}
 extern "C" int ncgm_hf_run(const ncgm_hf_config *, ncgm_hf_result *, double *,
                            double *, double *, double *, double *) {
   ncgm::setError("ncgm_hf_run: not available in this build");

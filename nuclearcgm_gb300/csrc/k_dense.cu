@@ -1,0 +1,389 @@
+// Tall-skinny and small dense FP64 complex linear algebra for the block GCG
+// eigensolver (gcgm_complex_no_B_lock, src/solver/solver.cpp:642-959):
+//  * gram:      C = A^H B for N x p, N x q blocks (row chunks, deterministic
+//               two-pass reduction, no atomics);
+//  * gemmVC:    Y = V C for N x m times m x k;
+//  * cholDrop:  one-CTA Cholesky of a Gram matrix with the modified
+//               Gram-Schmidt column-drop rule (|v_j| after projection below
+//               1e-12 -> column dropped, solver.cpp:404-407), returning the
+//               inverse factor so that Q = V R^{-1};
+//  * heig:      one-CTA cyclic Jacobi Hermitian eigensolver reading the lower
+//               triangle (as SelfAdjointEigenSolver does), ascending order.
+#include "k_dense.cuh"
+
+#include <algorithm>
+#include <cmath>
+
+namespace ncgm {
+
+namespace {
+
+constexpr int kTile = 16;  // gram output tile
+constexpr int kRows = 32;  // rows staged per smem pass
+
+__global__ void gramKernel(const double2 *__restrict__ A, size_t lda, int p,
+                           const double2 *__restrict__ B, size_t ldb, int q,
+                           size_t N, size_t rowsPerChunk, double2 *partials) {
+  __shared__ double2 As[kRows][kTile + 1];
+  __shared__ double2 Bs[kRows][kTile + 1];
+  const int ti = threadIdx.x % kTile, tj = threadIdx.x / kTile;
+  const int i0 = blockIdx.x * kTile, j0 = blockIdx.y * kTile;
+  const size_t r0 = blockIdx.z * rowsPerChunk;
+  const size_t r1 = min(N, r0 + rowsPerChunk);
+  double2 acc = make_double2(0.0, 0.0);
+  for (size_t rb = r0; rb < r1; rb += kRows) {
+    // load kRows x kTile of A and B (column-major: consecutive rows)
+    for (int e = threadIdx.x; e < kRows * kTile; e += blockDim.x) {
+      int rr = e % kRows, cc = e / kRows;
+      size_t r = rb + rr;
+      int ia = i0 + cc, jb = j0 + cc;
+      As[rr][cc] = (r < r1 && ia < p) ? A[ia * lda + r] : make_double2(0, 0);
+      Bs[rr][cc] = (r < r1 && jb < q) ? B[jb * ldb + r] : make_double2(0, 0);
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int rr = 0; rr < kRows; ++rr) {
+      double2 a = As[rr][ti], b = Bs[rr][tj];
+      // conj(a) * b
+      acc.x += a.x * b.x + a.y * b.y;
+      acc.y += a.x * b.y - a.y * b.x;
+    }
+    __syncthreads();
+  }
+  const int i = i0 + ti, j = j0 + tj;
+  if (i < p && j < q)
+    partials[(size_t)blockIdx.z * p * q + (size_t)j * p + i] = acc;
+}
+
+__global__ void reducePartials(const double2 *partials, int chunks, int count,
+                               double2 *out, int ldo, int p) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= count) return;
+  double2 s = make_double2(0, 0);
+  for (int c = 0; c < chunks; ++c) {
+    double2 v = partials[(size_t)c * count + e];
+    s.x += v.x;
+    s.y += v.y;
+  }
+  int i = e % p, j = e / p;
+  out[(size_t)j * ldo + i] = s;
+}
+
+// Y(:, j) = sum_l V(:, l) C(l, j) (+ beta Y) ; C in shared memory
+__global__ void gemmVCKernel(const double2 *__restrict__ V, size_t ldv, int m,
+                             const double2 *__restrict__ Cm, int ldc, int k,
+                             double2 *Y, size_t ldy, size_t N, double beta) {
+  extern __shared__ double2 Cs[];
+  for (int e = threadIdx.x; e < m * k; e += blockDim.x) {
+    int l = e % m, j = e / m;
+    Cs[e] = Cm[(size_t)j * ldc + l];
+  }
+  __syncthreads();
+  const size_t r = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (r >= N) return;
+  const int j0 = blockIdx.y * 8;
+  const int j1 = min(k, j0 + 8);
+  double2 acc[8];
+#pragma unroll
+  for (int t = 0; t < 8; ++t) acc[t] = make_double2(0, 0);
+  for (int l = 0; l < m; ++l) {
+    double2 v = V[l * ldv + r];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      if (j0 + t < j1) {
+        double2 c = Cs[(size_t)(j0 + t) * m + l];
+        acc[t].x += v.x * c.x - v.y * c.y;
+        acc[t].y += v.x * c.y + v.y * c.x;
+      }
+    }
+  }
+  for (int t = 0; t < 8; ++t)
+    if (j0 + t < j1) {
+      double2 *y = Y + (size_t)(j0 + t) * ldy + r;
+      if (beta != 0.0) {
+        double2 o = *y;
+        acc[t].x += beta * o.x;
+        acc[t].y += beta * o.y;
+      }
+      *y = acc[t];
+    }
+}
+
+__device__ inline double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ inline double2 cconjmul(double2 a, double2 b) { // conj(a) b
+  return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+
+// One CTA. G (m x m, col-major, Hermitian, upper triangle used) ->
+// R upper with G = R^H R, columns whose pivot <= dropTol are dropped (their
+// row/column of R zero). Writes T = R^{-1} (m x m, zero rows/cols for dropped
+// columns) and keep[j] (1 kept, 0 dropped). Work arrays in global memory.
+__global__ void cholDropKernel(const double2 *G, int ldg, int m,
+                               double dropTol, double2 *R, double2 *T,
+                               int *keep) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < m * m; e += nt) {
+    R[e] = make_double2(0, 0);
+    T[e] = make_double2(0, 0);
+  }
+  __syncthreads();
+  __shared__ double piv;
+  for (int j = 0; j < m; ++j) {
+    // pivot: d = G_jj - sum_{k<j} |R_kj|^2
+    if (tid == 0) {
+      double d = G[(size_t)j * ldg + j].x;
+      for (int k = 0; k < j; ++k) {
+        double2 r = R[(size_t)j * m + k];
+        d -= r.x * r.x + r.y * r.y;
+      }
+      piv = d;
+      keep[j] = (d > dropTol) ? 1 : 0;
+      if (d > dropTol) R[(size_t)j * m + j] = make_double2(sqrt(d), 0.0);
+    }
+    __syncthreads();
+    if (piv > dropTol) {
+      const double rjj = sqrt(piv);
+      // R_ji = (G_ji - sum_{k<j} conj(R_kj) R_ki) / R_jj, i > j
+      for (int i = j + 1 + tid; i < m; i += nt) {
+        double2 s = G[(size_t)i * ldg + j];
+        for (int k = 0; k < j; ++k) {
+          double2 t = cconjmul(R[(size_t)j * m + k], R[(size_t)i * m + k]);
+          s.x -= t.x;
+          s.y -= t.y;
+        }
+        R[(size_t)i * m + j] = make_double2(s.x / rjj, s.y / rjj);
+      }
+    }
+    __syncthreads();
+  }
+  // T = R^{-1} restricted to kept columns: solve R T = I column by column
+  // (upper triangular back substitution), one thread per column of T.
+  for (int c = tid; c < m; c += nt) {
+    if (!keep[c]) continue;
+    for (int i = c; i >= 0; --i) {
+      if (!keep[i]) continue;
+      double2 s = make_double2(i == c ? 1.0 : 0.0, 0.0);
+      for (int k = i + 1; k <= c; ++k) {
+        if (!keep[k]) continue;
+        double2 t = cmul(R[(size_t)k * m + i], T[(size_t)c * m + k]);
+        s.x -= t.x;
+        s.y -= t.y;
+      }
+      double rii = R[(size_t)i * m + i].x;
+      T[(size_t)c * m + i] = make_double2(s.x / rii, s.y / rii);
+    }
+  }
+}
+
+// One CTA parallel-order Jacobi (round-robin pairing: every round rotates
+// m/2 disjoint (p,q) pairs at once, m-1 rounds per sweep) on a Hermitian
+// m x m matrix whose lower triangle is read. A, Vm: m x m workspaces;
+// w: eigenvalues ascending; Vm: eigenvectors in the same order.
+__global__ void heigKernel(const double2 *Ain, int lda, int m, double2 *A,
+                           double2 *Vm, double *w, int *perm, int *status) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < m * m; e += nt) {
+    int i = e % m, j = e / m;
+    double2 v;
+    if (i > j) v = Ain[(size_t)j * lda + i];
+    else if (i < j) {
+      double2 l = Ain[(size_t)i * lda + j];
+      v = make_double2(l.x, -l.y);
+    } else v = make_double2(Ain[(size_t)j * lda + i].x, 0.0);
+    A[e] = v;
+    Vm[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+  }
+  const int mp = (m % 2) ? m + 1 : m; // players incl. a dummy for odd m
+  const int npairs = mp / 2;
+  __shared__ int P[256], Q[256];
+  __shared__ double C[256], S[256];
+  __shared__ double2 E[256];
+  __shared__ double red[256];
+  __syncthreads();
+  double fro = 0;
+  {
+    double loc = 0;
+    for (int e = tid; e < m * m; e += nt) loc += A[e].x * A[e].x + A[e].y * A[e].y;
+    red[tid] = loc;
+    __syncthreads();
+    for (int st = nt / 2; st > 0; st >>= 1) {
+      if (tid < st) red[tid] += red[tid + st];
+      __syncthreads();
+    }
+    fro = red[0];
+    __syncthreads();
+  }
+  int converged = 0;
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double loc = 0;
+    for (int e = tid; e < m * m; e += nt) {
+      int i = e % m, j = e / m;
+      if (i > j) loc += A[e].x * A[e].x + A[e].y * A[e].y;
+    }
+    red[tid] = loc;
+    __syncthreads();
+    for (int st = nt / 2; st > 0; st >>= 1) {
+      if (tid < st) red[tid] += red[tid + st];
+      __syncthreads();
+    }
+    double off = red[0];
+    __syncthreads();
+    if (off <= 1e-32 * fro || off == 0.0) {
+      converged = 1;
+      break;
+    }
+    for (int r = 0; r < mp - 1; ++r) {
+      // pairing of this round and rotation parameters, one thread per pair
+      for (int k = tid; k < npairs; k += nt) {
+        int a, b;
+        if (k == 0) {
+          a = mp - 1;
+          b = r;
+        } else {
+          a = (r + k) % (mp - 1);
+          b = (r - k + (mp - 1)) % (mp - 1);
+        }
+        int p = min(a, b), q = max(a, b);
+        P[k] = p;
+        Q[k] = q;
+        C[k] = 1.0;
+        S[k] = 0.0;
+        E[k] = make_double2(1.0, 0.0);
+        if (q < m) {
+          double2 apq = A[(size_t)q * m + p];
+          double mag = sqrt(apq.x * apq.x + apq.y * apq.y);
+          double app = A[(size_t)p * m + p].x, aqq = A[(size_t)q * m + q].x;
+          if (mag != 0.0 &&
+              !(sweep > 3 && mag < 1e-18 * sqrt(fabs(app * aqq)) + 1e-300)) {
+            double tau = (aqq - app) / (2.0 * mag);
+            double t = (tau >= 0 ? 1.0 : -1.0) /
+                       (fabs(tau) + sqrt(1.0 + tau * tau));
+            C[k] = 1.0 / sqrt(1.0 + t * t);
+            S[k] = t * C[k];
+            E[k] = make_double2(apq.x / mag, apq.y / mag);
+          }
+        }
+      }
+      __syncthreads();
+      // A <- A U and V <- V U: thread per (row, pair)
+      for (int e = tid; e < m * npairs; e += nt) {
+        int row = e % m, k = e / m;
+        int p = P[k], q = Q[k];
+        if (q >= m || S[k] == 0.0) continue;
+        double c = C[k], s = S[k];
+        double2 ec = make_double2(E[k].x, -E[k].y);
+        double2 arp = A[(size_t)p * m + row], arq = A[(size_t)q * m + row];
+        double2 t1 = cmul(ec, arq);
+        A[(size_t)p * m + row] = make_double2(c * arp.x - s * t1.x, c * arp.y - s * t1.y);
+        A[(size_t)q * m + row] = make_double2(s * arp.x + c * t1.x, s * arp.y + c * t1.y);
+        double2 vrp = Vm[(size_t)p * m + row], vrq = Vm[(size_t)q * m + row];
+        double2 t2 = cmul(ec, vrq);
+        Vm[(size_t)p * m + row] = make_double2(c * vrp.x - s * t2.x, c * vrp.y - s * t2.y);
+        Vm[(size_t)q * m + row] = make_double2(s * vrp.x + c * t2.x, s * vrp.y + c * t2.y);
+      }
+      __syncthreads();
+      // A <- U^H A: thread per (pair, column)
+      for (int e = tid; e < m * npairs; e += nt) {
+        int col = e % m, k = e / m;
+        int p = P[k], q = Q[k];
+        if (q >= m || S[k] == 0.0) continue;
+        double c = C[k], s = S[k];
+        double2 ee = E[k];
+        double2 apr = A[(size_t)col * m + p], aqr = A[(size_t)col * m + q];
+        double2 t1 = cmul(ee, aqr);
+        A[(size_t)col * m + p] = make_double2(c * apr.x - s * t1.x, c * apr.y - s * t1.y);
+        A[(size_t)col * m + q] = make_double2(s * apr.x + c * t1.x, s * apr.y + c * t1.y);
+      }
+      __syncthreads();
+      for (int k = tid; k < npairs; k += nt) {
+        int p = P[k], q = Q[k];
+        if (q >= m || S[k] == 0.0) continue;
+        A[(size_t)q * m + p] = make_double2(0, 0);
+        A[(size_t)p * m + q] = make_double2(0, 0);
+        A[(size_t)p * m + p].y = 0.0;
+        A[(size_t)q * m + q].y = 0.0;
+      }
+      __syncthreads();
+    }
+  }
+  // sort ascending (stable insertion sort by thread 0), permute eigenvectors
+  if (tid == 0) {
+    for (int i = 0; i < m; ++i) perm[i] = i;
+    for (int i = 1; i < m; ++i) {
+      int pi = perm[i];
+      double key = A[(size_t)pi * m + pi].x;
+      int k = i - 1;
+      while (k >= 0 && A[(size_t)perm[k] * m + perm[k]].x > key) {
+        perm[k + 1] = perm[k];
+        --k;
+      }
+      perm[k + 1] = pi;
+    }
+    for (int i = 0; i < m; ++i) w[i] = A[(size_t)perm[i] * m + perm[i]].x;
+    *status = converged ? 0 : 1;
+  }
+  __syncthreads();
+  for (int e = tid; e < m * m; e += nt) {
+    int r = e % m, c = e / m;
+    A[e] = Vm[(size_t)perm[c] * m + r];
+  }
+  __syncthreads();
+  for (int e = tid; e < m * m; e += nt) Vm[e] = A[e];
+}
+
+} // namespace
+
+void gram(const double2 *A, size_t lda, int p, const double2 *B, size_t ldb,
+          int q, size_t N, double2 *C, int ldc, double2 *partials,
+          int maxChunks, cudaStream_t s) {
+  if (p == 0 || q == 0) return;
+  int chunks = (int)std::min<size_t>(maxChunks, std::max<size_t>(1, N / 256));
+  size_t rows = (N + chunks - 1) / chunks;
+  rows = ((rows + kRows - 1) / kRows) * kRows;
+  chunks = (int)((N + rows - 1) / rows);
+  dim3 grid((p + kTile - 1) / kTile, (q + kTile - 1) / kTile, chunks);
+  gramKernel<<<grid, kTile * kTile, 0, s>>>(A, lda, p, B, ldb, q, N, rows,
+                                            partials);
+  int count = p * q;
+  reducePartials<<<(count + 127) / 128, 128, 0, s>>>(partials, chunks, count,
+                                                     C, ldc, p);
+}
+
+int gramMaxChunks() { return 256; }
+
+void gemmVC(const double2 *V, size_t ldv, int m, const double2 *Cm, int ldc,
+            int k, double2 *Y, size_t ldy, size_t N, double beta,
+            cudaStream_t s) {
+  if (k == 0) return;
+  if (m == 0) {
+    // Y = beta Y; only used with beta = 0 -> zero
+    for (int j = 0; j < k; ++j)
+      cudaMemsetAsync(Y + (size_t)j * ldy, 0, N * sizeof(double2), s);
+    return;
+  }
+  size_t smem = (size_t)m * k * sizeof(double2);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(gemmVCKernel,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         200 * 1024);
+    attr = true;
+  }
+  dim3 grid((unsigned)((N + 127) / 128), (k + 7) / 8);
+  gemmVCKernel<<<grid, 128, smem, s>>>(V, ldv, m, Cm, ldc, k, Y, ldy, N, beta);
+}
+
+void cholDrop(const double2 *G, int ldg, int m, double dropTol, double2 *R,
+              double2 *T, int *keep, cudaStream_t s) {
+  cholDropKernel<<<1, 256, 0, s>>>(G, ldg, m, dropTol, R, T, keep);
+}
+
+void heig(const double2 *A, int lda, int m, double2 *work, double2 *V,
+          double *w, int *perm, int *status, cudaStream_t s) {
+  // the round-robin tables hold up to 256 pairs (m <= 512)
+  heigKernel<<<1, 256, 0, s>>>(A, lda, m, work, V, w, perm, status);
+}
+
+} // namespace ncgm

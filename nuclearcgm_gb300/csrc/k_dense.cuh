@@ -1,0 +1,25 @@
+// Dense FP64 complex helpers for the GCG eigensolver (see k_dense.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+namespace ncgm {
+
+// C (p x q, ld ldc) = A^H B; partials: >= maxChunks * p * q double2.
+void gram(const double2 *A, size_t lda, int p, const double2 *B, size_t ldb,
+          int q, size_t N, double2 *C, int ldc, double2 *partials,
+          int maxChunks, cudaStream_t s);
+int gramMaxChunks();
+// Y = V C + beta Y (V: N x m, C: m x k with m*k*16 bytes <= 200 KB).
+void gemmVC(const double2 *V, size_t ldv, int m, const double2 *C, int ldc,
+            int k, double2 *Y, size_t ldy, size_t N, double beta,
+            cudaStream_t s);
+// Cholesky of Gram G with MGS-equivalent drop; T = R^{-1}; keep flags.
+void cholDrop(const double2 *G, int ldg, int m, double dropTol, double2 *R,
+              double2 *T, int *keep, cudaStream_t s);
+// Hermitian eigensolver (lower triangle): w ascending, V eigenvectors (m x m).
+void heig(const double2 *A, int lda, int m, double2 *work, double2 *V,
+          double *w, int *perm, int *status, cudaStream_t s);
+
+} // namespace ncgm

@@ -23,7 +23,11 @@
 //    Outputs stream back with coalesced 16-byte stores.
 #include "ncgm_internal.cuh"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <algorithm>
+#include <vector>
 #include <cmath>
 #include <cstdio>
 
@@ -35,7 +39,7 @@ constexpr double kHbar = 197.327053;
 constexpr double kMass = 938.91869;
 
 template <class T> struct V4;
-template <> struct V4<double> { using type = double4; };
+template <> struct V4<double> { using type = double4_32a; };
 template <> struct V4<float> { using type = float4; };
 
 template <class T> struct Spinor {
@@ -152,14 +156,6 @@ __device__ __forceinline__ void mbarExpectTx(uint64_t *bar, uint32_t bytes) {
       "r"(bytes)
       : "memory");
 }
-__device__ __forceinline__ void tmaBulkLoad(void *dst, const void *src,
-                                            uint32_t bytes, uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
-      "[%0], [%1], %2, [%3];" ::"r"(smemAddr(dst)),
-      "l"(src), "r"(bytes), "r"(smemAddr(bar))
-      : "memory");
-}
 // Bounded wait on an mbarrier phase. Returns false after `limit` polls.
 __device__ __forceinline__ bool mbarWait(uint64_t *bar, uint32_t phase,
                                          uint32_t limit) {
@@ -177,113 +173,129 @@ __device__ __forceinline__ bool mbarWait(uint64_t *bar, uint32_t phase,
   return false;
 }
 
-struct PlaneArgs {
-  const float4 *X;
+// Tensor-map TMA (cp.async.bulk.tensor.5d) into a shared-memory ring.
+// The 5-D map views X as [col][k][j][i][4 floats]; one box is a padded
+// (TY+4) x (n+4) sub-plane that starts at i = -2, j = y0 - 2. Out-of-box
+// coordinates are zero-filled by the TMA unit, which is exactly the
+// reference's Dirichlet truncation, so the compute loop has no bounds checks.
+__device__ __forceinline__ void tmaTileLoad5(void *dst, const CUtensorMap *map,
+                                             int c0, int c1, int c2, int c3,
+                                             int c4, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::"
+      "complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(
+          smemAddr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2),
+      "r"(c3), "r"(c4), "r"(smemAddr(bar))
+      : "memory");
+}
+
+struct TileArgs {
   float4 *Y;
   const float4 *coef;
   int n;
   size_t ns;
   float shift;
-  int TY;      // rows per band
-  int kchunk;  // output planes per CTA
-  int ring;    // ring slots
-  int nbands;
-  int *err;    // device error word (timeout)
+  int TY;     // rows per band
+  int kchunk; // output planes per CTA
+  int ring;   // ring slots (>= 6)
+  int *err;   // device error word (timeout)
 };
 
+constexpr int kMaxPts = 8; // owned points per thread (bandPts <= 8*threads)
+
 // grid: x = band * nchunks + chunk, y = column
-__global__ void __launch_bounds__(256) stencilPlanes32(PlaneArgs A) {
+__global__ void __launch_bounds__(256)
+    stencilTiles32(const __grid_constant__ CUtensorMap map, TileArgs A) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  const int n = A.n;
+  const int n = A.n, W = n + 4;
   const int nchunks = (n + A.kchunk - 1) / A.kchunk;
   const int band = blockIdx.x / nchunks, chunk = blockIdx.x % nchunks;
   const int col = blockIdx.y;
   const int y0 = band * A.TY;
-  const int y1 = min(n, y0 + A.TY);
-  const int ylo = max(0, y0 - 2), yhi = min(n, y1 + 2);
-  const int rows = yhi - ylo;             // rows held per slot
-  const int slotElems = rows * n;         // float4 per slot
-  const uint32_t slotBytes = slotElems * 16u;
+  const int ty = min(A.TY, n - y0);
+  // a slot holds one box; slots start on 128-byte boundaries (TMA dst rule)
+  const int boxElems = (A.TY + 4) * W;
+  const int slotElems = (boxElems + 7) & ~7;
+  const uint32_t boxBytes = boxElems * 16u;
   float4 *ring = reinterpret_cast<float4 *>(smem_raw);
-  uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + (size_t)A.ring * slotBytes);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(
+      smem_raw + (size_t)A.ring * slotElems * 16u);
   const int k0 = chunk * A.kchunk, k1 = min(n, k0 + A.kchunk);
-  const int zlo = max(0, k0 - 2), zhi = min(n, k1 + 2); // planes to load
-  const float4 *Xc = A.X + (size_t)col * A.ns;
-  const size_t plane = (size_t)n * n;
+  const int zlo = k0 - 2, zhi = k1 + 2; // planes loaded (OOB -> zeros)
 
+  // owned points of the band (same for every plane)
+  int lr[kMaxPts], gq[kMaxPts];
+  const int bandPts = ty * n;
+  int np = 0;
+#pragma unroll
+  for (int t = 0; t < kMaxPts; ++t) {
+    int q = threadIdx.x + t * blockDim.x;
+    lr[t] = 0;
+    gq[t] = 0;
+    if (q < bandPts) {
+      int jj = q / n, i = q - jj * n;
+      lr[t] = (jj + 2) * W + (i + 2);
+      gq[t] = (y0 + jj) * n + i;
+      np = t + 1;
+    }
+  }
   if (threadIdx.x == 0) {
     for (int s = 0; s < A.ring; ++s) mbarInit(&bars[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  // issue the first loads (ring slots are reused modulo A.ring)
   auto issue = [&](int z) {
     int s = (z - zlo) % A.ring;
-    mbarExpectTx(&bars[s], slotBytes);
-    tmaBulkLoad(ring + (size_t)s * slotElems, Xc + z * plane + (size_t)ylo * n,
-                slotBytes, &bars[s]);
+    mbarExpectTx(&bars[s], boxBytes);
+    tmaTileLoad5(ring + (size_t)s * slotElems, &map, 0, -2, y0 - 2, z, col,
+                 &bars[s]);
   };
   int nextLoad = zlo;
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == 0)
     for (; nextLoad < zhi && nextLoad - zlo < A.ring; ++nextLoad) issue(nextLoad);
-  }
-  // phase of each slot flips every time it is refilled
   bool ok = true;
   const uint32_t kLimit = 1u << 22;
-  int waitedUpTo = zlo - 1; // highest plane confirmed resident
-  const int bandPts = (y1 - y0) * n;
+  int waitedUpTo = zlo - 1;
+  const size_t plane = (size_t)n * n;
+  float4 *Yc = A.Y + (size_t)col * A.ns;
   for (int k = k0; k < k1; ++k) {
-    const int need = min(zhi - 1, k + 2);
-    while (ok && waitedUpTo < need) {
+    while (ok && waitedUpTo < k + 2) {
       int z = waitedUpTo + 1;
       int s = (z - zlo) % A.ring;
       uint32_t phase = ((z - zlo) / A.ring) & 1u;
       if (!mbarWait(&bars[s], phase, kLimit)) ok = false;
       else waitedUpTo = z;
     }
-    // every thread takes the same branch: a timeout anywhere stops the CTA
-    ok = __syncthreads_and(ok);
+    ok = __syncthreads_and(ok); // block-uniform decision
     if (!ok) break;
-    const float4 *pl[5];
-    for (int dz = -2; dz <= 2; ++dz) {
-      int z = k + dz;
-      pl[dz + 2] = (z >= zlo && z < zhi)
-                       ? ring + (size_t)((z - zlo) % A.ring) * slotElems
-                       : nullptr;
-    }
-    for (int q = threadIdx.x; q < bandPts; q += blockDim.x) {
-      const int i = q % n, j = y0 + q / n;
-      const int lr = (j - ylo) * n + i; // local index in a slot
-      const size_t gp = (size_t)k * plane + (size_t)j * n + i;
-      const float4 *c2 = A.coef + 2 * gp;
-      float4 ca = __ldg(c2), cb = __ldg(c2 + 1);
-      float c[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
-      const float4 *cp = pl[2];
-      auto ld = [&](const float4 *base, int off, bool valid) -> Spinor<float> {
-        if (!valid || base == nullptr) return {0.f, 0.f, 0.f, 0.f};
-        float4 v = base[lr + off];
-        return {v.x, v.y, v.z, v.w};
-      };
-      Spinor<float> o = pointH<float>(
-          c, A.shift, ld(cp, 0, true), ld(cp, 1, i + 1 < n), ld(cp, -1, i >= 1),
-          ld(cp, 2, i + 2 < n), ld(cp, -2, i >= 2), ld(cp, n, j + 1 < n),
-          ld(cp, -n, j >= 1), ld(cp, 2 * n, j + 2 < n), ld(cp, -2 * n, j >= 2),
-          ld(pl[3], 0, k + 1 < n), ld(pl[1], 0, k >= 1),
-          ld(pl[4], 0, k + 2 < n), ld(pl[0], 0, k >= 2));
-      A.Y[(size_t)col * A.ns + gp] = make_float4(o.r0, o.i0, o.r1, o.i1);
-    }
-    __syncthreads(); // everyone done reading plane k-2 before it is refilled
-    if (threadIdx.x == 0) {
-      // plane k-2 is no longer needed: refill its slot with the next plane
-      while (nextLoad < zhi && nextLoad - zlo < (k - 1 - zlo) + A.ring) {
-        issue(nextLoad);
-        ++nextLoad;
+    const float4 *pm2 = ring + (size_t)((k - 2 - zlo) % A.ring) * slotElems;
+    const float4 *pm1 = ring + (size_t)((k - 1 - zlo) % A.ring) * slotElems;
+    const float4 *pc = ring + (size_t)((k - zlo) % A.ring) * slotElems;
+    const float4 *pp1 = ring + (size_t)((k + 1 - zlo) % A.ring) * slotElems;
+    const float4 *pp2 = ring + (size_t)((k + 2 - zlo) % A.ring) * slotElems;
+#pragma unroll
+    for (int t = 0; t < kMaxPts; ++t) {
+      if (t < np) {
+        const int l = lr[t];
+        const size_t gp = (size_t)k * plane + gq[t];
+        const float4 *c2 = A.coef + 2 * gp;
+        float4 ca = __ldg(c2), cb = __ldg(c2 + 1);
+        float c[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
+        auto S = [](float4 v) { return Spinor<float>{v.x, v.y, v.z, v.w}; };
+        Spinor<float> o = pointH<float>(
+            c, A.shift, S(pc[l]), S(pc[l + 1]), S(pc[l - 1]), S(pc[l + 2]),
+            S(pc[l - 2]), S(pc[l + W]), S(pc[l - W]), S(pc[l + 2 * W]),
+            S(pc[l - 2 * W]), S(pp1[l]), S(pm1[l]), S(pp2[l]), S(pm2[l]));
+        Yc[gp] = make_float4(o.r0, o.i0, o.r1, o.i1);
       }
     }
+    __syncthreads(); // plane k-2 is free after this
+    if (threadIdx.x == 0)
+      while (nextLoad < zhi && nextLoad < k - 1 + A.ring) issue(nextLoad++);
   }
   if (!ok) {
     if (threadIdx.x == 0) atomicExch(A.err, 1);
-    // drain: wait (bounded) for every copy this CTA issued
     for (int z = waitedUpTo + 1; z < nextLoad; ++z) {
       int s = (z - zlo) % A.ring;
       mbarWait(&bars[s], ((z - zlo) / A.ring) & 1u, kLimit);
@@ -381,9 +393,61 @@ struct ShapeCache {
 };
 ShapeCache g_shape[8];
 
-size_t planeSmem(int n, int TY, int ring) {
-  int rows = std::min(n, TY + 4);
-  return (size_t)ring * rows * n * 16 + (size_t)ring * 8;
+size_t tileSmem(int n, int TY, int ring) {
+  size_t slot = (((size_t)(TY + 4) * (n + 4) + 7) & ~size_t(7)) * 16;
+  return (size_t)ring * slot + (size_t)ring * 8;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no
+// direct libcuda link).
+PFN_cuTensorMapEncodeTiled_v12000 encodeFn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void *p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                         cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+struct MapKey {
+  const void *ptr;
+  int n, ncols, TY;
+};
+struct MapEntry {
+  MapKey k;
+  CUtensorMap map;
+};
+std::vector<MapEntry> g_maps;
+
+// 5-D map of X: dims (4 floats, i, j, k, col), box (4, n+4, TY+4, 1, 1).
+bool tensorMapFor(const void *X, int n, int ncols, int TY, CUtensorMap *out) {
+  for (auto &e : g_maps)
+    if (e.k.ptr == X && e.k.n == n && e.k.ncols == ncols && e.k.TY == TY) {
+      *out = e.map;
+      return true;
+    }
+  auto fn = encodeFn();
+  if (!fn) return false;
+  cuuint64_t dims[5] = {4, (cuuint64_t)n, (cuuint64_t)n, (cuuint64_t)n,
+                        (cuuint64_t)ncols};
+  cuuint64_t strides[4] = {16, (cuuint64_t)16 * n, (cuuint64_t)16 * n * n,
+                           (cuuint64_t)16 * n * n * n};
+  cuuint32_t box[5] = {4, (cuuint32_t)(n + 4), (cuuint32_t)(TY + 4), 1, 1};
+  cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  CUtensorMap m;
+  CUresult r = fn(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, const_cast<void *>(X),
+                  dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return false;
+  if (g_maps.size() > 64) g_maps.erase(g_maps.begin());
+  g_maps.push_back({{X, n, ncols, TY}, m});
+  *out = m;
+  return true;
 }
 
 } // namespace
@@ -444,17 +508,28 @@ void applyH64(ncgm_ctx *ctx, int species, const double2 *X, double2 *Y,
               int ncols, double shift, cudaStream_t s) {
   dim3 grid((unsigned)((ctx->ns + 255) / 256), ncols);
   stencilPoint<double><<<grid, 256, 0, s>>>(
-      reinterpret_cast<const double4 *>(X), reinterpret_cast<double4 *>(Y),
-      reinterpret_cast<const double4 *>(ctx->sp[species].coef64), ctx->n,
+      reinterpret_cast<const double4_32a *>(X), reinterpret_cast<double4_32a *>(Y),
+      reinterpret_cast<const double4_32a *>(ctx->sp[species].coef64), ctx->n,
       ctx->ns, shift);
 }
 
-static void launchPlanes(ncgm_ctx *ctx, int species, const float2 *X,
-                         float2 *Y, int ncols, float shift, cudaStream_t s,
-                         const StencilShape &sh, int TY, int ring) {
+// Rows per band: a candidate list for the autotuner; the ring holds the 5
+// planes of the stencil plus prefetch.
+static int bandRowsDefault(int n) {
+  int TY = n;
+  while (TY > 4 && tileSmem(n, TY, 6) > 110 * 1024) TY = (TY + 1) / 2;
+  return TY;
+}
+
+static bool launchTiles(ncgm_ctx *ctx, int species, const float2 *X,
+                        float2 *Y, int ncols, float shift, cudaStream_t s,
+                        const StencilShape &sh) {
   const int n = ctx->n;
-  PlaneArgs A;
-  A.X = reinterpret_cast<const float4 *>(X);
+  const int TY = sh.rows > 0 ? std::min(sh.rows, n) : bandRowsDefault(n);
+  if ((size_t)TY * n > (size_t)kMaxPts * sh.threads) return false;
+  CUtensorMap map;
+  if (!tensorMapFor(X, n, ncols, TY, &map)) return false;
+  TileArgs A;
   A.Y = reinterpret_cast<float4 *>(Y);
   A.coef = reinterpret_cast<const float4 *>(ctx->sp[species].coef32);
   A.n = n;
@@ -462,26 +537,24 @@ static void launchPlanes(ncgm_ctx *ctx, int species, const float2 *X,
   A.shift = shift;
   A.TY = TY;
   A.kchunk = sh.kchunk;
-  A.ring = ring;
-  A.nbands = (n + TY - 1) / TY;
+  A.ring = sh.ring;
   A.err = errWord();
+  const int nbands = (n + TY - 1) / TY;
   const int nchunks = (n + sh.kchunk - 1) / sh.kchunk;
-  dim3 grid(A.nbands * nchunks, ncols);
-  size_t smem = planeSmem(n, TY, ring);
-  stencilPlanes32<<<grid, sh.threads, smem, s>>>(A);
-}
-
-// Rows per band and ring depth for a given lattice: whole planes when they
-// fit twice per SM, otherwise bands of rows with a +-2 halo.
-static void bandShape(int n, int &TY, int &ring) {
-  ring = 6;
-  TY = n;
-  const size_t budget = 110 * 1024; // two CTAs per SM
-  while (TY > 4 && planeSmem(n, TY, ring) > budget) TY = (TY + 1) / 2;
+  dim3 grid(nbands * nchunks, ncols);
+  stencilTiles32<<<grid, sh.threads, tileSmem(n, TY, sh.ring), s>>>(map, A);
+  return true;
 }
 
 void applyH32(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
               int ncols, float shift, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(stencilTiles32,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         220 * 1024);
+    attr = true;
+  }
   StencilShape &sh0 = stencilShape32(ctx);
   if (!sh0.tuned && !sh0.tuning) {
     // first FP32 apply on this context: pick the launch shape by timing
@@ -490,17 +563,16 @@ void applyH32(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
     sh0.tuning = false;
     sh0.tuned = true;
   }
-  const StencilShape &sh = sh0;
-  int TY, ring;
-  bandShape(ctx->n, TY, ring);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(stencilPlanes32,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         200 * 1024);
-    attr = true;
+  if (!launchTiles(ctx, species, X, Y, ncols, shift, s, sh0)) {
+    // shape not launchable on this lattice: default shape
+    StencilShape d;
+    d.threads = 256;
+    d.rows = bandRowsDefault(ctx->n);
+    while ((size_t)d.rows * ctx->n > (size_t)kMaxPts * d.threads && d.rows > 1)
+      d.rows = (d.rows + 1) / 2;
+    if (!launchTiles(ctx, species, X, Y, ncols, shift, s, d))
+      setError("FP32 stencil: tensor map encoding failed");
   }
-  launchPlanes(ctx, species, X, Y, ncols, shift, s, sh, TY, ring);
 }
 
 // Project autotuner for the FP32 stencil launch shape: times each candidate
@@ -514,29 +586,51 @@ int autotuneStencil32(ncgm_ctx *ctx, int species, int ncols) {
   float2 *Y = static_cast<float2 *>(ctx->buf(2, bytes));
   if (!X || !Y) return NCGM_ERR_NOMEM;
   NCGM_CUDA(cudaMemsetAsync(X, 0, bytes, ctx->stream));
-  const int chunks[] = {4, 6, 8, 12, 16};
+  const int n = ctx->n;
+  std::vector<int> rowsC;
+  for (int r = n; r >= 4; r = (r + 1) / 2) {
+    rowsC.push_back(r);
+    if (r == 4) break;
+  }
+  const int chunks[] = {4, 8, 16};
   const int threads[] = {128, 256};
+  const int rings[] = {6, 8};
   float bestMs = 1e30f;
   StencilShape keep = best;
-  for (int kc : chunks)
-    for (int th : threads) {
-      StencilShape cand = best;
-      cand.kchunk = kc;
-      cand.threads = th;
-      best.kchunk = kc;
-      best.threads = th;
-      applyH32(ctx, species, X, Y, ncols, 0.f, ctx->stream); // warm
-      cudaEventRecord(ctx->ev0, ctx->stream);
-      for (int r = 0; r < 3; ++r) applyH32(ctx, species, X, Y, ncols, 0.f, ctx->stream);
-      cudaEventRecord(ctx->ev1, ctx->stream);
-      NCGM_CUDA(cudaEventSynchronize(ctx->ev1));
-      float ms = 0;
-      cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-      if (ms < bestMs) {
-        bestMs = ms;
-        keep = cand;
-      }
-    }
+  bool any = false;
+  for (int rw : rowsC)
+    for (int kc : chunks)
+      for (int th : threads)
+        for (int rg : rings) {
+          if (tileSmem(n, rw, rg) > 200 * 1024) continue;
+          if ((size_t)rw * n > (size_t)kMaxPts * th) continue;
+          StencilShape cand = best;
+          cand.kchunk = kc;
+          cand.threads = th;
+          cand.rows = rw;
+          cand.ring = rg;
+          best.kchunk = kc;
+          best.threads = th;
+          best.rows = rw;
+          best.ring = rg;
+          if (!launchTiles(ctx, species, X, Y, ncols, 0.f, ctx->stream, best))
+            continue; // warm
+          cudaEventRecord(ctx->ev0, ctx->stream);
+          for (int r = 0; r < 3; ++r)
+            launchTiles(ctx, species, X, Y, ncols, 0.f, ctx->stream, best);
+          cudaEventRecord(ctx->ev1, ctx->stream);
+          NCGM_CUDA(cudaEventSynchronize(ctx->ev1));
+          float ms = 0;
+          cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+          if (ms < bestMs) {
+            bestMs = ms;
+            keep = cand;
+            any = true;
+          }
+        }
+  if (!any) keep = StencilShape();
+  best.rows = keep.rows;
+  best.ring = keep.ring;
   best.kchunk = keep.kchunk;
   best.threads = keep.threads;
   NCGM_CUDA(cudaGetLastError());

@@ -1,0 +1,285 @@
+// Batched Jacobi-preconditioned conjugate gradients: the GCG correction step
+// of gcgm_complex_no_B_lock (src/solver/solver.cpp:723-745), one independent
+// system (A + shift I) w_k = x_k (lambda_k + shift) per active column with
+// initial guess x_k. The iteration and stopping rule are those of Eigen's
+// ConjugateGradient with DiagonalPreconditioner (textbook PCG, Saad Alg. 9.1):
+// stop when |r|^2 < max(tol^2 |b|^2, DBL_MIN) or after cg_steps iterations.
+// All columns advance together; a converged column is frozen by its flag.
+// Reductions are deterministic (per-block partials summed in a fixed order).
+// Vectors are FP64 (plain form) or FP32 (mixed form, dots in FP64).
+#include "k_pcg.cuh"
+
+#include <cfloat>
+
+namespace ncgm {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+template <class T> struct C2;
+template <> struct C2<double> { using type = double2; };
+template <> struct C2<float> { using type = float2; };
+
+__device__ double blockSum(double v, double *sh) {
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  double r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+// inverse Jacobi diagonal from the FP64 coefficient table: diag = c0 + shift
+__device__ inline double invDiag(const double *coef, size_t p, double shift) {
+  double d = coef[8 * p] + shift;
+  return d != 0.0 ? 1.0 / d : 1.0;
+}
+
+// r = b - T, b = x (lam+shift), z = Minv r, p = z, w = x; partials |b|^2,
+// |r|^2, Re(r^H z).
+template <class T>
+__global__ void pcgInitKernel(const typename C2<T>::type *X, size_t ldx,
+                              const typename C2<T>::type *Tx,
+                              typename C2<T>::type *Wv,
+                              typename C2<T>::type *R, typename C2<T>::type *Z,
+                              typename C2<T>::type *P, size_t N,
+                              const double *lamShift, const double *coef,
+                              double shift, double *partials, int nblk) {
+  __shared__ double sh[kThreads];
+  const int col = blockIdx.y;
+  const double ls = lamShift[col];
+  double bb = 0, rr = 0, rz = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x) {
+    size_t o = (size_t)col * N + i;
+    auto x = X[(size_t)col * ldx + i];
+    auto t = Tx[o];
+    double bx = (double)x.x * ls, by = (double)x.y * ls;
+    double rx = bx - (double)t.x, ry = by - (double)t.y;
+    double m = invDiag(coef, i / 2, shift);
+    double zx = m * rx, zy = m * ry;
+    bb += bx * bx + by * by;
+    rr += rx * rx + ry * ry;
+    rz += rx * zx + ry * zy;
+    Wv[o] = x;
+    R[o] = {(T)rx, (T)ry};
+    Z[o] = {(T)zx, (T)zy};
+    P[o] = {(T)zx, (T)zy};
+  }
+  double s0 = blockSum(bb, sh), s1 = blockSum(rr, sh), s2 = blockSum(rz, sh);
+  if (threadIdx.x == 0) {
+    double *pp = partials + (size_t)col * nblk * 3;
+    pp[blockIdx.x] = s0;
+    pp[nblk + blockIdx.x] = s1;
+    pp[2 * nblk + blockIdx.x] = s2;
+  }
+}
+
+__global__ void pcgInitFinish(PcgCol *st, const double *partials, int nblk,
+                              double tol) {
+  const int col = blockIdx.x;
+  if (threadIdx.x != 0) return;
+  const double *pp = partials + (size_t)col * nblk * 3;
+  double bb = 0, rr = 0, rz = 0;
+  for (int b = 0; b < nblk; ++b) {
+    bb += pp[b];
+    rr += pp[nblk + b];
+    rz += pp[2 * nblk + b];
+  }
+  PcgCol c;
+  c.rhsNorm2 = bb;
+  c.thr = fmax(tol * tol * bb, DBL_MIN);
+  c.absNew = rz;
+  c.absOld = rz;
+  c.beta = 0;
+  c.iters = 0;
+  c.zero = (bb == 0.0);
+  c.done = (bb == 0.0) || (rr < c.thr);
+  st[col] = c;
+}
+
+// partial p^H Ap (complex)
+template <class T>
+__global__ void pcgDotKernel(const typename C2<T>::type *P,
+                             const typename C2<T>::type *AP, size_t N,
+                             const PcgCol *st, double *partials, int nblk) {
+  __shared__ double sh[kThreads];
+  const int col = blockIdx.y;
+  if (st[col].done) return;
+  double re = 0, im = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x) {
+    size_t o = (size_t)col * N + i;
+    auto p = P[o];
+    auto a = AP[o];
+    re += (double)p.x * a.x + (double)p.y * a.y;
+    im += (double)p.x * a.y - (double)p.y * a.x;
+  }
+  double s0 = blockSum(re, sh), s1 = blockSum(im, sh);
+  if (threadIdx.x == 0) {
+    double *pp = partials + (size_t)col * nblk * 3;
+    pp[blockIdx.x] = s0;
+    pp[nblk + blockIdx.x] = s1;
+  }
+}
+
+// alpha = absNew / (p^H Ap); w += alpha p; r -= alpha Ap; z = Minv r;
+// partials |r|^2 and Re(r^H z) (stored after the p^H Ap partials).
+template <class T>
+__global__ void pcgUpdateKernel(typename C2<T>::type *Wv,
+                                typename C2<T>::type *R,
+                                typename C2<T>::type *Z,
+                                const typename C2<T>::type *P,
+                                const typename C2<T>::type *AP, size_t N,
+                                const PcgCol *st, const double *coef,
+                                double shift, double *partials,
+                                double *partials2, int nblk) {
+  __shared__ double sh[kThreads];
+  __shared__ double ar, ai;
+  const int col = blockIdx.y;
+  if (st[col].done) return;
+  if (threadIdx.x == 0) {
+    const double *pp = partials + (size_t)col * nblk * 3;
+    double re = 0, im = 0;
+    for (int b = 0; b < nblk; ++b) {
+      re += pp[b];
+      im += pp[nblk + b];
+    }
+    // alpha = absNew / (re + i im)
+    double den = re * re + im * im;
+    double a = st[col].absNew;
+    ar = a * re / den;
+    ai = -a * im / den;
+  }
+  __syncthreads();
+  const double alr = ar, ali = ai;
+  double rr = 0, rz = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x) {
+    size_t o = (size_t)col * N + i;
+    auto p = P[o];
+    auto a = AP[o];
+    auto w = Wv[o];
+    auto r = R[o];
+    double px = p.x, py = p.y, ax = a.x, ay = a.y;
+    double wx = (double)w.x + (alr * px - ali * py);
+    double wy = (double)w.y + (alr * py + ali * px);
+    double rx = (double)r.x - (alr * ax - ali * ay);
+    double ry = (double)r.y - (alr * ay + ali * ax);
+    double m = invDiag(coef, i / 2, shift);
+    double zx = m * rx, zy = m * ry;
+    Wv[o] = {(T)wx, (T)wy};
+    R[o] = {(T)rx, (T)ry};
+    Z[o] = {(T)zx, (T)zy};
+    rr += rx * rx + ry * ry;
+    rz += rx * zx + ry * zy;
+  }
+  double s0 = blockSum(rr, sh), s1 = blockSum(rz, sh);
+  if (threadIdx.x == 0) {
+    double *pp = partials2 + (size_t)col * nblk * 2;
+    pp[blockIdx.x] = s0;
+    pp[nblk + blockIdx.x] = s1;
+  }
+}
+
+__global__ void pcgFinishKernel(PcgCol *st, const double *partials2, int nblk,
+                                int *live) {
+  const int col = blockIdx.x;
+  if (threadIdx.x != 0) return;
+  PcgCol c = st[col];
+  if (c.done) return;
+  const double *pp = partials2 + (size_t)col * nblk * 2;
+  double rr = 0, rz = 0;
+  for (int b = 0; b < nblk; ++b) {
+    rr += pp[b];
+    rz += pp[nblk + b];
+  }
+  if (rr < c.thr) {
+    c.done = 1;
+  } else {
+    c.absOld = c.absNew;
+    c.absNew = rz;
+    c.beta = c.absNew / c.absOld;
+    c.iters += 1;
+    atomicAdd(live, 1);
+  }
+  st[col] = c;
+}
+
+template <class T>
+__global__ void pcgPKernel(typename C2<T>::type *P,
+                           const typename C2<T>::type *Z, size_t N,
+                           const PcgCol *st) {
+  const int col = blockIdx.y;
+  if (st[col].done) return;
+  const double b = st[col].beta;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x) {
+    size_t o = (size_t)col * N + i;
+    auto z = Z[o];
+    auto p = P[o];
+    P[o] = {(T)((double)z.x + b * p.x), (T)((double)z.y + b * p.y)};
+  }
+}
+
+template <class T>
+__global__ void pcgZeroKernel(typename C2<T>::type *Wv, size_t N,
+                              const PcgCol *st) {
+  const int col = blockIdx.y;
+  if (!st[col].zero) return;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x)
+    Wv[(size_t)col * N + i] = {(T)0, (T)0};
+}
+
+} // namespace
+
+int pcgBlocks(size_t N) {
+  size_t b = (N + kThreads * 4 - 1) / (kThreads * 4);
+  if (b > 128) b = 128;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+template <class T>
+void pcgRun(const PcgPlan<T> &pl, cudaStream_t s) {
+  const int nblk = pcgBlocks(pl.N);
+  dim3 grid(nblk, pl.ncols);
+  using V = typename C2<T>::type;
+  // T = (A + shift) X
+  pl.apply(pl.X, pl.ldx, pl.AP, pl.ncols, pl.shift, s);
+  pcgInitKernel<T><<<grid, kThreads, 0, s>>>(
+      reinterpret_cast<const V *>(pl.X), pl.ldx,
+      reinterpret_cast<const V *>(pl.AP), reinterpret_cast<V *>(pl.W),
+      reinterpret_cast<V *>(pl.R), reinterpret_cast<V *>(pl.Z),
+      reinterpret_cast<V *>(pl.P), pl.N, pl.lamShift, pl.coef, pl.shift,
+      pl.partials, nblk);
+  pcgInitFinish<<<pl.ncols, 32, 0, s>>>(pl.st, pl.partials, nblk, pl.tol);
+  for (int it = 0; it < pl.maxSteps; ++it) {
+    pl.apply(pl.P, pl.N, pl.AP, pl.ncols, pl.shift, s);
+    pcgDotKernel<T><<<grid, kThreads, 0, s>>>(
+        reinterpret_cast<const V *>(pl.P), reinterpret_cast<const V *>(pl.AP),
+        pl.N, pl.st, pl.partials, nblk);
+    pcgUpdateKernel<T><<<grid, kThreads, 0, s>>>(
+        reinterpret_cast<V *>(pl.W), reinterpret_cast<V *>(pl.R),
+        reinterpret_cast<V *>(pl.Z), reinterpret_cast<const V *>(pl.P),
+        reinterpret_cast<const V *>(pl.AP), pl.N, pl.st, pl.coef, pl.shift,
+        pl.partials, pl.partials2, nblk);
+    pcgFinishKernel<<<pl.ncols, 32, 0, s>>>(pl.st, pl.partials2, nblk,
+                                            pl.live);
+    pcgPKernel<T><<<grid, kThreads, 0, s>>>(
+        reinterpret_cast<V *>(pl.P), reinterpret_cast<const V *>(pl.Z), pl.N,
+        pl.st);
+  }
+  pcgZeroKernel<T><<<grid, kThreads, 0, s>>>(reinterpret_cast<V *>(pl.W),
+                                             pl.N, pl.st);
+}
+
+template void pcgRun<double>(const PcgPlan<double> &, cudaStream_t);
+template void pcgRun<float>(const PcgPlan<float> &, cudaStream_t);
+
+} // namespace ncgm

@@ -1,0 +1,38 @@
+// Batched Jacobi-PCG (see k_pcg.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <functional>
+
+namespace ncgm {
+
+struct PcgCol {
+  double absNew, absOld, beta, thr, rhsNorm2;
+  int iters, done, zero, pad;
+};
+
+// Buffers are device pointers to complex numbers of type T (interleaved),
+// N rows per column, ncols columns, column stride N except X (ldx).
+template <class T> struct PcgPlan {
+  size_t N = 0;
+  int ncols = 0;
+  const void *X = nullptr; // initial guess and right-hand-side direction
+  size_t ldx = 0;
+  void *W = nullptr, *R = nullptr, *Z = nullptr, *P = nullptr, *AP = nullptr;
+  const double *lamShift = nullptr; // lambda_k + shift per column (device)
+  const double *coef = nullptr;     // FP64 coefficient table (diagonal)
+  double shift = 0, tol = 0;
+  int maxSteps = 0;
+  PcgCol *st = nullptr;
+  double *partials = nullptr, *partials2 = nullptr; // ncols*128*3, ncols*128*2
+  int *live = nullptr; // count of column-iterations (stats)
+  // Y = (A + shift) X on device buffers (ld of X given, Y stride N)
+  std::function<void(const void *, size_t, void *, int, double, cudaStream_t)>
+      apply;
+};
+
+int pcgBlocks(size_t N);
+template <class T> void pcgRun(const PcgPlan<T> &plan, cudaStream_t s);
+
+} // namespace ncgm

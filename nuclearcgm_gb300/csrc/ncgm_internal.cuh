@@ -84,6 +84,8 @@ void applyH32(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
 struct StencilShape {
   int kchunk = 8;
   int threads = 256;
+  int rows = 0; // lattice rows per CTA band (0: default)
+  int ring = 6; // shared-memory ring slots
   bool tuned = false, tuning = false;
 };
 StencilShape &stencilShape32(ncgm_ctx *ctx);
