@@ -149,6 +149,23 @@ int ncgm_gcg(ncgm_ctx *ctx, int species, const double *X_init, int xcols,
              const ncgm_gcg_params *params, double *X_out, double *lambda_out,
              ncgm_gcg_stats *stats);
 
+/* ---- lattice densities and Coulomb field -------------------------------- */
+
+/* Densities of a block of (occupation-weighted) spinor columns Phi (N x
+ * ncols): rho, tau (n^3), J_{mu nu} (n^3 x 9, column mu*3+nu) and div J (n^3).
+ * Replaces Wavefunction::density / kineticDensity / soDensity / divJ
+ * (src/util/wavefunction.cpp:21-44, 348-360, 421-464, 466-517). */
+int ncgm_densities(ncgm_ctx *ctx, const double *Phi, int ncols, double *rho,
+                   double *tau, double *J9, double *divJ);
+
+/* Coulomb direct potential of a proton density by the Poisson equation with
+ * the multipole boundary halo, and UC = direct + Slater exchange. U_guess may
+ * be NULL (cold start). Replaces Wavefunction::coulombFieldPoisson and
+ * exchangeCoulombField (src/util/wavefunction.cpp:45-229). */
+int ncgm_poisson(ncgm_ctx *ctx, const double *rhoP, int Z,
+                 const double *U_guess, double *U_out, double *UC_out,
+                 int *iterations);
+
 /* ---- self-consistent iteration ----------------------------------------- */
 
 /* Run configuration: the fields of InputParser (src/system/input_parser.cpp:

@@ -100,6 +100,8 @@ SIGNATURES = {
                   _vp, C.POINTER(GcgStats)], _i),
     "ncgm_hf_run": ([C.POINTER(HFConfig), C.POINTER(HFResult), _vp, _vp, _vp,
                      _vp, _vp], _i),
+    "ncgm_densities": ([_vp, _vp, _i, _vp, _vp, _vp, _vp], _i),
+    "ncgm_poisson": ([_vp, _vp, _i, _vp, _vp, _vp, _vp], _i),
 }
 
 

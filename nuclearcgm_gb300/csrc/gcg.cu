@@ -179,7 +179,7 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
   size_t need = 0;
   need += N * (size_t)vmax * sizeof(double2) * 3; // V, Q, AV
   need += N * (size_t)vmax * sizeof(double2);     // Q1 (CholQR pass 1)
-  need += N * (size_t)nev * sizeof(double2) * 4;  // Xa, X0, Xn, AXn
+  need += N * (size_t)nev * sizeof(double2) * 5;  // Xa, X0, Xn, AXn, AXa
   need += N * (size_t)nev * (fp32 ? sizeof(float2) : sizeof(double2)) * 6;
   need += (size_t)mx * mx * sizeof(double2) * 8;  // small matrices
   need += maxChunks * (size_t)mx * mx * sizeof(double2);
@@ -190,7 +190,8 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
   double2 *V = ar.take<double2>(N * vmax), *Q = ar.take<double2>(N * vmax),
           *AV = ar.take<double2>(N * vmax), *Q1 = ar.take<double2>(N * vmax);
   double2 *Xa = ar.take<double2>(N * nev), *X0 = ar.take<double2>(N * nev),
-          *Xn = ar.take<double2>(N * nev), *AXn = ar.take<double2>(N * nev);
+          *Xn = ar.take<double2>(N * nev), *AXn = ar.take<double2>(N * nev),
+          *AXa = ar.take<double2>(N * nev);
   const size_t vbytes = fp32 ? sizeof(float2) : sizeof(double2);
   char *pv = ar.take<char>(N * nev * vbytes * 6);
   void *pX = pv, *pW = pv + N * nev * vbytes, *pR = pv + 2 * N * nev * vbytes,
@@ -249,6 +250,10 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
     gemmVC(Xa, N, nx, Ev, nx, nx, Xn, N, N, 0.0, s);
     NCGM_CUDA(cudaMemcpyAsync(Xa, Xn, N * (size_t)nx * sizeof(double2),
                               cudaMemcpyDeviceToDevice, s));
+    // A X of the rotated block (shift removed), kept for the FP32 correction
+    gemmVC(AV, N, nx, Ev, nx, nx, AXa, N, N, 0.0, s);
+    if (shift != 0.0)
+      axpyCols<<<gridN(nx), 256, 0, s>>>(AXa, Xa, N, nx, -shift);
     NCGM_CUDA(cudaMemcpyAsync(hw.data(), dW, sizeof(double) * nx,
                               cudaMemcpyDeviceToHost, s));
     NCGM_CUDA(cudaStreamSynchronize(s));
@@ -316,12 +321,14 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
         };
         pcgRun<double>(pl, s);
       } else {
-        convert64to32(Xa, static_cast<float2 *>(pX), N * (size_t)nact, s);
         PcgPlan<float> pl;
         pl.N = N;
         pl.ncols = nact;
         pl.X = pX;
         pl.ldx = N;
+        pl.X64 = Xa;
+        pl.AX64 = AXa;
+        pl.W64 = Wd;
         pl.W = pW;
         pl.R = pR;
         pl.Z = pZ;
@@ -342,7 +349,6 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
                    static_cast<float2 *>(Y), cols, (float)sh, st);
         };
         pcgRun<float>(pl, s);
-        convert32to64(static_cast<const float2 *>(pW), Wd, N * (size_t)nact, s);
       }
       if (stats) {
         std::vector<PcgCol> hs(nact);
@@ -418,6 +424,8 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
                                 cudaMemcpyHostToDevice, s));
       gatherCols<<<gridN((int)next.size()), 256, 0, s>>>(
           Xn, N, dIdx, (int)next.size(), Xa, N, N);
+      gatherCols<<<gridN((int)next.size()), 256, 0, s>>>(
+          AXn, N, dIdx, (int)next.size(), AXa, N, N);
     }
     NCGM_CUDA(cudaStreamSynchronize(s));
     nconv = (int)x0idx.size();

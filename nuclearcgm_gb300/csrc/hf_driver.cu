@@ -1,9 +1,1203 @@
-// Placeholder translation unit for the eigensolver and self-consistent driver
-// entry points; filled in by the GCG / HF implementation.
+// The self-consistent Hartree-Fock(-Bogoliubov) iteration on the device:
+// the GB300 form of main()'s run loop (src/main.cpp:59-342) with
+// IterationData::updateQuantities (src/util/iteration_data.cpp:852-1125),
+// the energies (iteration_data.cpp:153-271, iteration_data_integrals.cpp),
+// the Woods-Saxon + harmonic-oscillator guess (main.cpp:72-111) and the
+// augmented-Lagrangian constraints (src/skyrme/*_constraint.cpp).
+//
+// Lattice-sized data never leaves the device. The host keeps the O(M^2)
+// bookkeeping the reference does with scalars and small matrices: Kramers
+// pair matching, locking, constraint multipliers, bisection brackets.
+#include "k_dense.cuh"
+#include "k_density.cuh"
+#include "k_pairing.cuh"
+#include "k_poisson.cuh"
 #include "ncgm_internal.cuh"
 
-extern "C" int ncgm_hf_run(const ncgm_hf_config *, ncgm_hf_result *, double *,
-                           double *, double *, double *, double *) {
-  ncgm::setError("ncgm_hf_run: not available in this build");
-  return NCGM_ERR_ARG;
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <tuple>
+#include <vector>
+
+namespace ncgm {
+
+bool isDevicePtr(const void *p);
+int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
+           const double2 *ConjDir, int pcols, int nev,
+           const ncgm_gcg_params &prm, double2 *Xout, double *lamOut,
+           ncgm_gcg_stats *stats);
+
+namespace {
+
+constexpr double kHbar = 197.327053;
+constexpr double kMass = 938.91869;
+
+double now() {
+  return std::chrono::duration<double>(
+             std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+// constraint operators O(r) (xcm/ycm/zcm, x^2-y^2, 2xy, r^3 Y30, Q20)
+__device__ double constraintOp(int kind, double x, double y, double z) {
+  switch (kind) {
+  case 0: return x;
+  case 1: return y;
+  case 2: return z;
+  case 3: return x * x - y * y;
+  case 4: return 2.0 * x * y;
+  case 5: {
+    double r = sqrt(x * x + y * y + z * z);
+    double ct = z / r;
+    return r * r * r * sqrt(7.0 / (4.0 * M_PI)) * 0.5 * (5.0 * ct * ct * ct - 3.0 * ct);
+  }
+  default:
+    return 0.25 * sqrt(5 / (M_PI)) * (2.0 * z * z - y * y - x * x);
+  }
+}
+
+__device__ __forceinline__ double trapWd(size_t p, int n) {
+  const int i = (int)(p % n), j = (int)((p / n) % n), k = (int)(p / ((size_t)n * n));
+  double w = 1.0;
+  if (i == 0 || i == n - 1) w *= 0.5;
+  if (j == 0 || j == n - 1) w *= 0.5;
+  if (k == 0 || k == n - 1) w *= 0.5;
+  return w;
+}
+
+// partials[c * nblk + b] = int O_c (rhoN + rhoP), c < nc
+__global__ void constraintQ(const double *rN, const double *rP, int n,
+                            double a, double h, const int *kinds, int nc,
+                            double *partials) {
+  __shared__ double sh[256];
+  const size_t ns = (size_t)n * n * n;
+  const double hhh = h * h * h;
+  for (int c = 0; c < nc; ++c) {
+    double acc = 0;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < ns;
+         p += (size_t)gridDim.x * blockDim.x) {
+      const int i = (int)(p % n), j = (int)((p / n) % n), k = (int)(p / ((size_t)n * n));
+      double O = constraintOp(kinds[c], -a + i * h, -a + j * h, -a + k * h);
+      acc += (O * (rN[p] + rP[p])) * hhh * trapWd(p, n);
+    }
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) partials[(size_t)c * gridDim.x + blockIdx.x] = sh[0];
+    __syncthreads();
+  }
+}
+
+// Uconstr = sum_c coef_c O_c ; UN += Uconstr ; UP += Uconstr
+__global__ void constraintField(const int *kinds, const double *coef, int nc,
+                                int n, double a, double h, double *UC,
+                                double *UN, double *UP) {
+  const size_t ns = (size_t)n * n * n;
+  const size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (p >= ns) return;
+  const int i = (int)(p % n), j = (int)((p / n) % n), k = (int)(p / ((size_t)n * n));
+  double v = 0;
+  for (int c = 0; c < nc; ++c)
+    v += coef[c] * constraintOp(kinds[c], -a + i * h, -a + j * h, -a + k * h);
+  UC[p] = v;
+  UN[p] += v;
+  UP[p] += v;
+}
+
+__global__ void zeroKernel(double *x, size_t n) {
+  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e < n) x[e] = 0.0;
+}
+
+struct Constraint {
+  int kind;
+  double target, C, gamma, lambda = 0, value = 0;
+  bool first = true;
+  double error() const {
+    if (kind <= 2) return 0.0; // COM constraints (xcm_constraint.cpp:13)
+    double t = (kind == 6) ? target : 0.0;
+    if (std::abs(t) <= 1e-12) return std::abs(value);
+    return std::abs(value / t - 1.0);
+  }
+};
+
+Constraint makeConstraint(int kind, double target) {
+  Constraint c;
+  c.kind = kind;
+  c.target = target;
+  c.C = (kind <= 2) ? 0.05 : (kind == 5 ? 0.001 : 0.005);
+  c.gamma = (kind <= 2) ? 0.2 : 0.3;
+  return c;
+}
+
+struct BCSRes {
+  std::vector<double> u2, v2, Delta, qp;
+  double lambda = 0, Epair = 0;
+};
+struct HFBRes {
+  std::vector<double> U, V, kappa; // M x M col-major
+  int M = 0;
+  double lambda = 0, energy = 0;
+};
+
+struct Species {
+  int orb = 0;
+  double2 *X = nullptr, *Xn = nullptr, *CD = nullptr, *Phi = nullptr,
+          *TX = nullptr;
+  std::vector<double> e;
+  int cdCols = 0;
+  BCSRes bcs;
+  HFBRes hfb;
+  ncgm_pairing par;
+};
+
+struct Run {
+  ncgm_ctx *ctx = nullptr;
+  ncgm_hf_config cfg;
+  int n = 0;
+  size_t ns = 0, N = 0;
+  double a = 0, h = 0;
+  cudaStream_t s = nullptr;
+  // lattice state
+  double *rho[2], *tau[2], *J9[2], *divJ[2], *g[2], *lap[2];
+  double *f[2], *gf[2], *U[2], *W[2];
+  double *UCdir = nullptr, *UCoul = nullptr, *UConstr = nullptr;
+  double *nrho = nullptr, *ntau = nullptr, *nJ9 = nullptr, *ndivJ = nullptr;
+  double *scratch = nullptr, *poissonWork = nullptr, *energy = nullptr;
+  double2 *cplx = nullptr; // small complex matrices
+  double *small = nullptr; // small real matrices
+  int *ismall = nullptr;
+  bool have = false, haveCoul = false;
+  double massCorr = kMass, energyDiff = 1.0;
+  Species sp[2];
+  std::vector<Constraint> cons;
+  double tPair = 0, tFields = 0, tPoisson = 0, tGcg = 0;
+  std::vector<void *> allocs;
+
+  template <class T> T *alloc(size_t count) {
+    void *p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T)) != cudaSuccess)
+      return nullptr;
+    allocs.push_back(p);
+    return static_cast<T *>(p);
+  }
+  ~Run() {
+    for (void *p : allocs) cudaFree(p);
+    if (ctx) ncgm_destroy(ctx);
+  }
+};
+
+int sync(Run &R) {
+  cudaError_t e = cudaStreamSynchronize(R.s);
+  if (e != cudaSuccess) {
+    setError(std::string("hf: ") + cudaGetErrorString(e));
+    return NCGM_ERR_CUDA;
+  }
+  return NCGM_OK;
+}
+
+// gram of columns (N rows): C = A^H B into host matrix (p x q)
+int hostGram(Run &R, const double2 *A, int p, const double2 *B, int q,
+             std::vector<double2> &C) {
+  static thread_local double2 *parts = nullptr;
+  static thread_local size_t cap = 0;
+  const int maxChunks = 64;
+  size_t need = (size_t)maxChunks * p * q;
+  if (cap < need) {
+    if (parts) cudaFree(parts);
+    if (cudaMalloc(&parts, need * sizeof(double2)) != cudaSuccess) {
+      parts = nullptr;
+      cap = 0;
+      return NCGM_ERR_NOMEM;
+    }
+    cap = need;
+  }
+  gram(A, R.N, p, B, R.N, q, R.N, R.cplx, p, parts, maxChunks, R.s);
+  C.resize((size_t)p * q);
+  cudaMemcpyAsync(C.data(), R.cplx, sizeof(double2) * p * q,
+                  cudaMemcpyDeviceToHost, R.s);
+  return sync(R);
+}
+
+// --- BCS (iteration_data.cpp:384-465, bcs.cpp:65-321) ----------------------
+BCSRes nullBCS(const std::vector<double> &e, int num) {
+  BCSRes b;
+  const int M = (int)e.size();
+  b.u2.assign(M, 1.0);
+  b.v2.assign(M, 0.0);
+  for (int i = 0; i < num && i < M; ++i) {
+    b.u2[i] = 0.0;
+    b.v2[i] = 1.0;
+  }
+  b.Delta.assign(num, 0.0);
+  b.qp.resize(M);
+  for (int i = 0; i < M; ++i) b.qp[i] = b.v2[i] * e[i];
+  return b;
+}
+
+int bcsIter(Run &R, Species &S, int A, const std::vector<double> &oldDelta,
+            double oldLambda, BCSRes &out) {
+  const int M = S.orb;
+  // pair overlaps |phi^H T phi|^2 (bcs.cpp:65-70)
+  timeReverse(S.X, S.TX, R.ns, M, R.N, false, R.s);
+  std::vector<double2> ov;
+  NCGM_TRY(hostGram(R, S.X, M, S.TX, M, ov));
+  // match_time_reversal (bcs.cpp:71-105)
+  std::vector<std::tuple<double, int, int>> list;
+  for (int k = 0; k < M; ++k)
+    for (int j = 0; j < M; ++j) {
+      double2 z = ov[(size_t)j * M + k];
+      double v = z.x * z.x + z.y * z.y;
+      if (std::abs(v) > 1e-6) list.emplace_back(v, k, j);
+    }
+  std::stable_sort(list.begin(), list.end(), [](const auto &x, const auto &y) {
+    return std::get<0>(x) > std::get<0>(y);
+  });
+  std::vector<int> partner(M, -1);
+  std::vector<char> used(M, 0);
+  for (auto &t : list) {
+    int k = std::get<1>(t), j = std::get<2>(t);
+    if (used[k] || used[j] || k == j) continue;
+    partner[k] = j;
+    partner[j] = k;
+    used[k] = used[j] = 1;
+  }
+  std::vector<int> unique, s2p(M, 0);
+  std::vector<bool> visited(M, false);
+  for (int i = 0; i < M; ++i)
+    if (!visited[i]) {
+      int pt = partner[i];
+      if (pt != i && pt != -1) {
+        int pi = (int)unique.size();
+        unique.push_back(i);
+        s2p[i] = s2p[pt] = pi;
+        visited[i] = visited[pt] = true;
+      }
+    }
+  const int np = (int)unique.size();
+  std::vector<double> eps(np);
+  for (int p = 0; p < np; ++p) eps[p] = S.e[unique[p]];
+  std::vector<double> oldU;
+  if ((int)oldDelta.size() == np * 2) {
+    oldU.resize(std::min(M / 2, np));
+    for (size_t i = 0; i < oldU.size(); ++i) oldU[i] = oldDelta[unique[i]];
+  } else {
+    oldU = oldDelta;
+  }
+  bool useOld = (int)oldU.size() == np && np > 0 &&
+                *std::max_element(oldU.begin(), oldU.end()) > 1e-3;
+  // device work
+  int *dCols = R.ismall;
+  double *dG = R.small, *dEps = dG + (size_t)np * np, *dOld = dEps + np,
+         *du2 = dOld + np, *dv2 = du2 + np, *dD = dv2 + np, *dSc = dD + np,
+         *dW = dSc + 4;
+  cudaMemcpyAsync(dCols, unique.data(), sizeof(int) * np,
+                  cudaMemcpyHostToDevice, R.s);
+  densityGram(S.X, R.N, dCols, np, R.n, R.h, S.par.V0, dG, R.s);
+  std::vector<double> G((size_t)np * np);
+  cudaMemcpyAsync(G.data(), dG, sizeof(double) * np * np,
+                  cudaMemcpyDeviceToHost, R.s);
+  NCGM_TRY(sync(R));
+  std::vector<double> Gs((size_t)np * np);
+  for (int p = 0; p < np; ++p)
+    for (int q = 0; q < np; ++q)
+      Gs[(size_t)q * np + p] = 0.5 * (G[(size_t)q * np + p] + G[(size_t)p * np + q]);
+  cudaMemcpyAsync(dG, Gs.data(), sizeof(double) * np * np,
+                  cudaMemcpyHostToDevice, R.s);
+  cudaMemcpyAsync(dEps, eps.data(), sizeof(double) * np, cudaMemcpyHostToDevice,
+                  R.s);
+  if (useOld)
+    cudaMemcpyAsync(dOld, oldU.data(), sizeof(double) * np,
+                    cudaMemcpyHostToDevice, R.s);
+  bcsSolve(dEps, dG, np, A, S.par.window, S.par.window_both, dOld, useOld,
+           oldLambda, du2, dv2, dD, dSc, dW, R.s);
+  std::vector<double> u2(np), v2(np), D(np), sc(2);
+  cudaMemcpyAsync(u2.data(), du2, sizeof(double) * np, cudaMemcpyDeviceToHost, R.s);
+  cudaMemcpyAsync(v2.data(), dv2, sizeof(double) * np, cudaMemcpyDeviceToHost, R.s);
+  cudaMemcpyAsync(D.data(), dD, sizeof(double) * np, cudaMemcpyDeviceToHost, R.s);
+  cudaMemcpyAsync(sc.data(), dSc, sizeof(double) * 2, cudaMemcpyDeviceToHost, R.s);
+  NCGM_TRY(sync(R));
+  out.u2.assign(M, 0.0);
+  out.v2.assign(M, 0.0);
+  out.Delta.assign(M, 0.0);
+  for (int i = 0; i < M; ++i)
+    if (visited[i]) {
+      int pi = s2p[i];
+      out.u2[i] = u2[pi];
+      out.v2[i] = v2[pi];
+      out.Delta[i] = D[pi];
+    }
+  out.qp.resize(M);
+  for (int i = 0; i < M; ++i) out.qp[i] = S.e[i] * out.v2[i];
+  out.lambda = sc[0];
+  out.Epair = sc[1];
+  return NCGM_OK;
+}
+
+int solvePairingBCS(Run &R) {
+  const int A = R.cfg.A, Z = R.cfg.Z, N = A - Z;
+  BCSRes nN = nullBCS(R.sp[0].e, N), nP = nullBCS(R.sp[1].e, Z);
+  auto &sn = R.sp[0], &spp = R.sp[1];
+  if (R.cfg.pairing_type == NCGM_PAIRING_NONE) {
+    sn.bcs = nN;
+    spp.bcs = nP;
+  } else if (!R.have) {
+    std::vector<double> tmp(1, 0.0);
+    if (sn.par.active) {
+      NCGM_TRY(bcsIter(R, sn, N, tmp, 0.5 * (sn.e[N - 1] + sn.e[N]), sn.bcs));
+    } else sn.bcs = nN;
+    if (spp.par.active) {
+      NCGM_TRY(bcsIter(R, spp, Z, tmp, 0.5 * (spp.e[Z - 1] + spp.e[Z]), spp.bcs));
+    } else spp.bcs = nP;
+  } else {
+    if (sn.par.active) {
+      BCSRes o;
+      NCGM_TRY(bcsIter(R, sn, N, sn.bcs.Delta, sn.bcs.lambda, o));
+      sn.bcs = o;
+    } else sn.bcs = nN;
+    if (spp.par.active) {
+      BCSRes o;
+      NCGM_TRY(bcsIter(R, spp, Z, spp.bcs.Delta, spp.bcs.lambda, o));
+      spp.bcs = o;
+    } else spp.bcs = nP;
+  }
+  double a = 0, b = 0;
+  for (double v : sn.bcs.v2) a += v;
+  for (double v : spp.bcs.v2) b += v;
+  if (std::isnan(a) || std::isnan(b)) {
+    sn.bcs = nN;
+    spp.bcs = nP;
+  }
+  return NCGM_OK;
+}
+
+// --- HFB (iteration_data.cpp:605-850) ---------------------------------------
+int heigHost(Run &R, const std::vector<double2> &A, int m, std::vector<double> &w,
+             std::vector<double2> &V) {
+  double2 *dA = R.cplx, *dW = R.cplx + (size_t)m * m, *dV = dW + (size_t)m * m;
+  double *dw = R.small;
+  int *dperm = R.ismall, *dst = R.ismall + m + 8;
+  cudaMemcpyAsync(dA, A.data(), sizeof(double2) * m * m, cudaMemcpyHostToDevice,
+                  R.s);
+  heig(dA, m, m, dW, dV, dw, dperm, dst, R.s);
+  w.resize(m);
+  V.resize((size_t)m * m);
+  int st = 0;
+  cudaMemcpyAsync(w.data(), dw, sizeof(double) * m, cudaMemcpyDeviceToHost, R.s);
+  cudaMemcpyAsync(V.data(), dV, sizeof(double2) * m * m, cudaMemcpyDeviceToHost,
+                  R.s);
+  cudaMemcpyAsync(&st, dst, sizeof(int), cudaMemcpyDeviceToHost, R.s);
+  NCGM_TRY(sync(R));
+  if (st != 0) {
+    setError("hfb: dense eigensolver did not converge");
+    return NCGM_ERR_EIG;
+  }
+  return NCGM_OK;
+}
+
+HFBRes nullHFB(int target, const std::vector<double> &e) {
+  HFBRes h;
+  const int M = (int)e.size();
+  h.M = M;
+  h.lambda = e[target - 1];
+  h.U.assign((size_t)M * M, 0.0);
+  h.V.assign((size_t)M * M, 0.0);
+  h.kappa.assign((size_t)M * M, 0.0);
+  h.energy = 0.0;
+  for (int i = 0; i < target; ++i) h.V[(size_t)i * M + i] = 1.0;
+  return h;
+}
+
+int hfbSpecies(Run &R, Species &S, int target, HFBRes &out) {
+  const HFBRes &prev = S.hfb;
+  const int M = S.orb;
+  const double window = S.par.window, smooth = window / 10.0;
+  auto fac = [&](double en, double lam) {
+    double v = 1.0 / (1.0 + std::exp((en - lam - window) / smooth));
+    v *= 1.0 / (1.0 + std::exp(-(en - lam + window) / smooth));
+    return std::sqrt(v);
+  };
+  double lambda = prev.lambda;
+  std::vector<double> ff(M);
+  for (int i = 0; i < M; ++i) ff[i] = fac(S.e[i], lambda);
+  int start = 0, end = M - 1;
+  for (int i = 0; i < M; i += 2)
+    if (ff[i] > R.cfg.pairing_threshold) {
+      start = i;
+      break;
+    }
+  for (int i = start; i < M; i += 2)
+    if (ff[i] < R.cfg.pairing_threshold) {
+      end = i;
+      break;
+    }
+  const int nS = end - start + 1;
+  // phi_rev = numericalTR(phi)
+  timeReverse(S.X, S.TX, R.ns, M, R.N, true, R.s);
+  std::vector<double> Kff((size_t)nS * nS), ffs(nS);
+  for (int b = 0; b < nS; ++b) {
+    ffs[b] = ff[start + b];
+    for (int a = 0; a < nS; ++a)
+      Kff[(size_t)b * nS + a] =
+          prev.kappa[(size_t)(start + b) * M + (start + a)] * ff[start + a] *
+          ff[start + b];
+  }
+  double *dK = R.small, *dff = dK + (size_t)nS * nS, *dDelta = dff + nS,
+         *dkap = R.scratch;
+  cudaMemcpyAsync(dK, Kff.data(), sizeof(double) * nS * nS,
+                  cudaMemcpyHostToDevice, R.s);
+  cudaMemcpyAsync(dff, ffs.data(), sizeof(double) * nS, cudaMemcpyHostToDevice,
+                  R.s);
+  kappaField(S.TX, R.N, start, nS, dK, R.ns, dkap, R.s);
+  deltaMatrix(S.TX, R.N, start, nS, dff, dkap, R.n, R.h, S.par.V0, dDelta, R.s);
+  std::vector<double> Delta((size_t)nS * nS);
+  cudaMemcpyAsync(Delta.data(), dDelta, sizeof(double) * nS * nS,
+                  cudaMemcpyDeviceToHost, R.s);
+  NCGM_TRY(sync(R));
+  double dn = 0;
+  for (double x : Delta) dn += x * x;
+  if (std::sqrt(dn) < 1e-3) {
+    out = nullHFB(target, S.e);
+    return NCGM_OK;
+  }
+  double bmin = lambda - 1.7, bmax = lambda + 1.7, cur = lambda;
+  const int m2 = 2 * nS;
+  std::vector<double> U((size_t)nS * nS), V((size_t)nS * nS);
+  std::vector<double2> H((size_t)m2 * m2);
+  std::vector<double> w;
+  std::vector<double2> Ev;
+  for (int it = 0; it < 100; ++it) {
+    std::fill(H.begin(), H.end(), make_double2(0, 0));
+    for (int i = 0; i < nS; ++i) {
+      H[(size_t)i * m2 + i] = make_double2(S.e[start + i] - cur, 0);
+      H[(size_t)(nS + i) * m2 + nS + i] = make_double2(-(S.e[start + i] - cur), 0);
+    }
+    for (int j = 0; j < nS; ++j)
+      for (int i = 0; i < nS; ++i) {
+        H[(size_t)(nS + j) * m2 + i] = make_double2(Delta[(size_t)j * nS + i], 0);
+        H[(size_t)j * m2 + nS + i] = make_double2(-Delta[(size_t)j * nS + i], 0);
+      }
+    NCGM_TRY(heigHost(R, H, m2, w, Ev));
+    double num = 0;
+    for (int k = 0; k < nS; ++k) {
+      int q = k + nS;
+      for (int i = 0; i < nS; ++i) {
+        U[(size_t)k * nS + i] = Ev[(size_t)q * m2 + i].x;
+        V[(size_t)k * nS + i] = Ev[(size_t)q * m2 + nS + i].x;
+        num += V[(size_t)k * nS + i] * V[(size_t)k * nS + i];
+      }
+    }
+    num += start;
+    double diff = num - target;
+    if (std::abs(diff) < 1e-12) break;
+    if (diff > 0) bmax = cur;
+    else bmin = cur;
+    cur = (bmax + bmin) / 2.0;
+  }
+  lambda = cur;
+  double pe = 0;
+  for (int i = 0; i < nS; ++i)
+    for (int j = 0; j < nS; ++j) {
+      double kij = 0;
+      for (int k = 0; k < nS; ++k) kij += V[(size_t)k * nS + i] * U[(size_t)k * nS + j];
+      pe += Delta[(size_t)j * nS + i] * kij;
+    }
+  pe *= 0.5;
+  out.M = M;
+  out.U.assign((size_t)M * M, 0.0);
+  out.V.assign((size_t)M * M, 0.0);
+  for (int j = 0; j < nS; ++j)
+    for (int i = 0; i < nS; ++i) {
+      out.V[(size_t)(start + j) * M + start + i] = V[(size_t)j * nS + i];
+      out.U[(size_t)(start + j) * M + start + i] = U[(size_t)j * nS + i];
+    }
+  for (int i = 0; i < start; ++i) out.V[(size_t)i * M + i] = 1.0;
+  for (int i = end + 1; i < M; ++i) out.U[(size_t)i * M + i] = 1.0;
+  out.kappa.assign((size_t)M * M, 0.0);
+  for (int i = 0; i < M; ++i)
+    for (int j = 0; j < M; ++j) {
+      double sacc = 0;
+      for (int k = 0; k < M; ++k)
+        sacc += out.U[(size_t)k * M + i] * out.V[(size_t)k * M + j];
+      out.kappa[(size_t)j * M + i] = sacc;
+    }
+  out.lambda = lambda;
+  out.energy = pe;
+  return NCGM_OK;
+}
+
+// Phi = phi * T (occupation transform) ; T given on host (M x M, col-major)
+int occupy(Run &R, Species &S, const std::vector<double2> &T) {
+  const int M = S.orb;
+  cudaMemcpyAsync(R.cplx, T.data(), sizeof(double2) * M * M,
+                  cudaMemcpyHostToDevice, R.s);
+  gemmVC(S.X, R.N, M, R.cplx, M, M, S.Phi, R.N, R.N, 0.0, R.s);
+  return NCGM_OK;
+}
+
+int occupiedOrbitals(Run &R, int q, bool bcsOcc, int &ncols,
+                     const double2 *&Phi) {
+  Species &S = R.sp[q];
+  const int M = S.orb;
+  const bool pairing = R.cfg.pairing_type != NCGM_PAIRING_NONE;
+  if (bcsOcc || (pairing && S.par.active &&
+                 R.cfg.pairing_type == NCGM_PAIRING_BCS)) {
+    std::vector<double2> T((size_t)M * M, make_double2(0, 0));
+    for (int c = 0; c < M; ++c)
+      T[(size_t)c * M + c] = make_double2(std::sqrt(S.bcs.v2[c]), 0);
+    NCGM_TRY(occupy(R, S, T));
+    Phi = S.Phi;
+    ncols = M;
+    return NCGM_OK;
+  }
+  if (pairing && S.par.active && R.cfg.pairing_type == NCGM_PAIRING_HFB) {
+    // natural orbitals of rho = V V^T (iteration_data.cpp:326-338)
+    std::vector<double2> rho((size_t)M * M);
+    for (int i = 0; i < M; ++i)
+      for (int j = 0; j < M; ++j) {
+        double sacc = 0;
+        for (int k = 0; k < M; ++k)
+          sacc += S.hfb.V[(size_t)k * M + i] * S.hfb.V[(size_t)k * M + j];
+        rho[(size_t)j * M + i] = make_double2(sacc, 0);
+      }
+    std::vector<double> w;
+    std::vector<double2> Wm;
+    NCGM_TRY(heigHost(R, rho, M, w, Wm));
+    for (auto &x : w)
+      if (x < 1e-12) x = 0.0;
+    std::vector<double2> T((size_t)M * M);
+    for (int j = 0; j < M; ++j)
+      for (int i = 0; i < M; ++i) {
+        double2 v = Wm[(size_t)j * M + i];
+        double sq = std::sqrt(w[j]);
+        T[(size_t)j * M + i] = make_double2(v.x * sq, v.y * sq);
+      }
+    NCGM_TRY(occupy(R, S, T));
+    Phi = S.Phi;
+    ncols = M;
+    return NCGM_OK;
+  }
+  Phi = S.X; // phi * nullOcc(N): columns == particle number
+  ncols = M;
+  return NCGM_OK;
+}
+
+int updateQuantities(Run &R, int iter) {
+  const ncgm_hf_config &C = R.cfg;
+  const double mu = C.density_mix;
+  double t0 = now();
+  bool bcsOcc = false;
+  if (C.pairing_type == NCGM_PAIRING_HFB) {
+    if (iter < C.start_hfb_iter) {
+      NCGM_TRY(solvePairingBCS(R));
+      bcsOcc = true;
+    } else {
+      if (iter == C.start_hfb_iter) {
+        for (int q = 0; q < 2; ++q) {
+          Species &S = R.sp[q];
+          const int M = S.orb;
+          S.hfb.M = M;
+          S.hfb.kappa.assign((size_t)M * M, 0.0);
+          S.hfb.V.assign((size_t)M * M, 0.0);
+          S.hfb.lambda = S.bcs.lambda;
+          for (int i = 0; i < M - 1; ++i)
+            if (i % 2 == 0) {
+              double uv = std::sqrt(S.bcs.u2[i] * S.bcs.v2[i]);
+              S.hfb.kappa[(size_t)(i + 1) * M + i] = uv;
+              S.hfb.kappa[(size_t)i * M + i + 1] = -1.0 * uv;
+            }
+        }
+      }
+      const int targets[2] = {C.A - C.Z, C.Z};
+      for (int q = 0; q < 2; ++q) {
+        Species &S = R.sp[q];
+        if (!S.par.active) continue;
+        HFBRes nw;
+        NCGM_TRY(hfbSpecies(R, S, targets[q], nw));
+        if (std::isnan(nw.energy)) {
+        } else if (std::abs(nw.energy) < 1e-12) {
+          S.par.active = 0;
+        } else {
+          S.hfb = nw;
+        }
+      }
+    }
+  } else {
+    NCGM_TRY(solvePairingBCS(R));
+  }
+  R.tPair += now() - t0;
+  t0 = now();
+  const bool first = !R.have;
+  for (int q = 0; q < 2; ++q) {
+    int nc = 0;
+    const double2 *Phi = nullptr;
+    NCGM_TRY(occupiedOrbitals(R, q, bcsOcc, nc, Phi));
+    densities(Phi, R.N, nc, R.n, R.h, R.nrho, R.ntau, R.nJ9, R.ndivJ, R.s);
+    mix(R.rho[q], R.nrho, mu, R.ns, first, R.s);
+    mix(R.tau[q], R.ntau, mu, R.ns, first, R.s);
+    mix(R.J9[q], R.nJ9, mu, 9 * R.ns, first, R.s);
+    mix(R.divJ[q], R.ndivJ, mu, R.ns, first, R.s);
+  }
+  for (int q = 0; q < 2; ++q) gradLap(R.rho[q], R.n, R.h, R.g[q], R.lap[q], R.s);
+  FieldsIn in;
+  in.ns = R.ns;
+  in.edf = C.edf;
+  in.hbar2m = kHbar * kHbar / (2 * R.massCorr);
+  in.spinOrbit = C.spin_orbit;
+  in.useJ = C.use_j;
+  in.rhoN = R.rho[0];
+  in.rhoP = R.rho[1];
+  in.tauN = R.tau[0];
+  in.tauP = R.tau[1];
+  in.lapN = R.lap[0];
+  in.lapP = R.lap[1];
+  in.divJN = R.divJ[0];
+  in.divJP = R.divJ[1];
+  in.gN = R.g[0];
+  in.gP = R.g[1];
+  in.JN = R.J9[0];
+  in.JP = R.J9[1];
+  FieldsOut out{R.f[0], R.f[1], R.gf[0], R.gf[1], R.U[0], R.U[1], R.W[0], R.W[1]};
+  meanFields(in, out, R.s);
+  // constraints (iteration_data.cpp:1031-1038,1079-1086)
+  const int nc = (int)R.cons.size();
+  if (iter > 0 && nc > 0) {
+    std::vector<int> kinds(nc);
+    for (int c = 0; c < nc; ++c) kinds[c] = R.cons[c].kind;
+    const int nblk = 120;
+    cudaMemcpyAsync(R.ismall, kinds.data(), sizeof(int) * nc,
+                    cudaMemcpyHostToDevice, R.s);
+    constraintQ<<<nblk, 256, 0, R.s>>>(R.rho[0], R.rho[1], R.n, R.a, R.h,
+                                       R.ismall, nc, R.small);
+    std::vector<double> part((size_t)nc * nblk);
+    cudaMemcpyAsync(part.data(), R.small, sizeof(double) * nc * nblk,
+                    cudaMemcpyDeviceToHost, R.s);
+    NCGM_TRY(sync(R));
+    std::vector<double> coef(nc);
+    for (int c = 0; c < nc; ++c) {
+      double Q = 0;
+      for (int b = 0; b < nblk; ++b) Q += part[(size_t)c * nblk + b];
+      Constraint &k = R.cons[c];
+      double m;
+      if (k.first) {
+        k.first = false;
+        m = (k.kind == 6) ? k.target - k.lambda / (2.0 * k.C) : k.target;
+      } else {
+        if (k.kind > 2 || R.energyDiff < 5e-3)
+          k.lambda += k.gamma * 2.0 * k.C * (Q - k.target);
+        m = k.target - k.lambda / (2.0 * k.C);
+        k.value = Q;
+      }
+      coef[c] = 2.0 * k.C * (Q - m);
+    }
+    cudaMemcpyAsync(R.small + nc * nblk, coef.data(), sizeof(double) * nc,
+                    cudaMemcpyHostToDevice, R.s);
+    constraintField<<<(unsigned)((R.ns + 255) / 256), 256, 0, R.s>>>(
+        R.ismall, R.small + nc * nblk, nc, R.n, R.a, R.h, R.UConstr, R.U[0],
+        R.U[1]);
+  } else {
+    zeroKernel<<<(unsigned)((R.ns + 255) / 256), 256, 0, R.s>>>(R.UConstr,
+                                                                 R.ns);
+  }
+  NCGM_TRY(sync(R));
+  R.tFields += now() - t0;
+  if (C.use_coulomb) {
+    t0 = now();
+    PoissonArgs P;
+    P.n = R.n;
+    P.a = R.a;
+    P.h = R.h;
+    P.Z = C.Z;
+    P.rhoP = R.rho[1];
+    P.U = R.UCdir;
+    P.UC = R.UCoul;
+    P.warm = R.haveCoul;
+    P.tol = 1e-13;
+    P.work = R.poissonWork;
+    int its = 0;
+    int st = poissonSolve(P, R.s, &its);
+    if (st != NCGM_OK) {
+      setError("hf: Poisson solve failed");
+      return st;
+    }
+    R.haveCoul = true;
+    NCGM_TRY(sync(R));
+    R.tPoisson += now() - t0;
+  }
+  R.have = true;
+  return NCGM_OK;
+}
+
+double epair(Run &R, int q) {
+  const ncgm_hf_config &C = R.cfg;
+  if (C.pairing_type == NCGM_PAIRING_NONE) return 0.0;
+  if (!R.sp[q].par.active) return 0.0;
+  if (C.pairing_type == NCGM_PAIRING_HFB) return R.sp[q].hfb.energy;
+  return R.sp[q].bcs.Epair;
+}
+
+int energies(Run &R, double &Eint, double &EHF) {
+  const ncgm_hf_config &C = R.cfg;
+  EnergyIn in;
+  in.ns = R.ns;
+  in.n = R.n;
+  in.h = R.h;
+  in.edf = C.edf;
+  in.hbar2 = kHbar * kHbar;
+  in.massCorr = R.massCorr;
+  in.rhoN = R.rho[0];
+  in.rhoP = R.rho[1];
+  in.tauN = R.tau[0];
+  in.tauP = R.tau[1];
+  in.lapN = R.lap[0];
+  in.lapP = R.lap[1];
+  in.divJN = R.divJ[0];
+  in.divJP = R.divJ[1];
+  in.JN = R.J9[0];
+  in.JP = R.J9[1];
+  in.UCDir = C.use_coulomb ? R.UCdir : nullptr;
+  energyIntegrals(in, R.scratch, R.energy, R.s);
+  double e[kEnergyTerms];
+  cudaMemcpyAsync(e, R.energy, sizeof(e), cudaMemcpyDeviceToHost, R.s);
+  // constraint energies need int O rho with the current densities
+  const int nc = (int)R.cons.size();
+  std::vector<double> Qs(nc, 0.0);
+  if (nc) {
+    std::vector<int> kinds(nc);
+    for (int c = 0; c < nc; ++c) kinds[c] = R.cons[c].kind;
+    const int nblk = 120;
+    cudaMemcpyAsync(R.ismall, kinds.data(), sizeof(int) * nc,
+                    cudaMemcpyHostToDevice, R.s);
+    constraintQ<<<nblk, 256, 0, R.s>>>(R.rho[0], R.rho[1], R.n, R.a, R.h,
+                                       R.ismall, nc, R.small);
+    std::vector<double> part((size_t)nc * nblk);
+    cudaMemcpyAsync(part.data(), R.small, sizeof(double) * nc * nblk,
+                    cudaMemcpyDeviceToHost, R.s);
+    NCGM_TRY(sync(R));
+    for (int c = 0; c < nc; ++c)
+      for (int b = 0; b < nblk; ++b) Qs[c] += part[(size_t)c * nblk + b];
+  }
+  NCGM_TRY(sync(R));
+  const double cd = C.use_coulomb ? 0.5 * e[10] : 0.0;
+  const double sl = C.use_coulomb ? e[11] : 0.0;
+  const double total = e[0] + e[1] + e[2] + e[3] + e[4] + e[5] + cd +
+                       epair(R, 0) + epair(R, 1) + sl + e[6] + e[7] + e[8] +
+                       e[9];
+  const double kin = e[12];
+  Eint = total + kin;
+  double ce = 0;
+  for (int c = 0; c < nc; ++c) {
+    const Constraint &k = R.cons[c];
+    ce += k.C * std::pow(Qs[c] - k.target, 2) + k.lambda * (Qs[c] - k.target);
+  }
+  double qN = 0, qP = 0;
+  for (double v : R.sp[0].bcs.qp) qN += v;
+  for (double v : R.sp[1].bcs.qp) qP += v;
+  EHF = ce + 0.5 * (qN + qP + kin) + e[13] + sl / 3.0 + epair(R, 0) +
+        epair(R, 1);
+  return NCGM_OK;
+}
+
+// Wavefunction::TROrder (wavefunction.cpp:581-635)
+int trOrder(Run &R, Species &S, double2 *X) {
+  const int M = S.orb;
+  timeReverse(X, S.TX, R.ns, M, R.N, false, R.s);
+  std::vector<double2> ord;
+  NCGM_TRY(hostGram(R, X, M, S.TX, M, ord));
+  std::vector<bool> used(M, false);
+  std::vector<int> order;
+  int slot = 0;
+  bool fail = false;
+  for (int i = 0; i < M && !fail; ++i) {
+    if (used[i]) continue;
+    order.push_back(i);
+    used[i] = true;
+    int best = -1;
+    double mx = -1.0;
+    for (int j = 0; j < M; ++j) {
+      if (used[j]) continue;
+      double2 z = ord[(size_t)j * M + i];
+      double ov = std::sqrt(z.x * z.x + z.y * z.y);
+      if (ov > mx) {
+        mx = ov;
+        best = j;
+      }
+    }
+    if (best < 0) {
+      fail = true;
+      break;
+    }
+    order.push_back(best);
+    used[best] = true;
+    slot += 2;
+    if (slot >= M) break;
+  }
+  if (fail || (int)order.size() != M) return NCGM_OK; // keep psi as is
+  // gather columns in `order` (through TX as staging)
+  for (int c = 0; c < M; ++c)
+    cudaMemcpyAsync(S.TX + (size_t)c * R.N, X + (size_t)order[c] * R.N,
+                    sizeof(double2) * R.N, cudaMemcpyDeviceToDevice, R.s);
+  cudaMemcpyAsync(X, S.TX, sizeof(double2) * R.N * M, cudaMemcpyDeviceToDevice,
+                  R.s);
+  return sync(R);
+}
+
+// P = Xnew - Xold (Xold^H Xnew), columns normalised (main.cpp:267-282)
+int conjDir(Run &R, Species &S) {
+  const int M = S.orb;
+  std::vector<double2> tmp;
+  NCGM_TRY(hostGram(R, S.X, M, S.Xn, M, tmp));
+  for (auto &z : tmp) z = make_double2(-z.x, -z.y);
+  cudaMemcpyAsync(R.cplx, tmp.data(), sizeof(double2) * M * M,
+                  cudaMemcpyHostToDevice, R.s);
+  cudaMemcpyAsync(S.CD, S.Xn, sizeof(double2) * R.N * M,
+                  cudaMemcpyDeviceToDevice, R.s);
+  gemmVC(S.X, R.N, M, R.cplx, M, M, S.CD, R.N, R.N, 1.0, R.s);
+  normalizeEuclid(S.CD, R.N, R.N, M, R.small, R.s);
+  S.cdCols = M;
+  return sync(R);
+}
+
+void quadDef(Run &R, double &beta, double &gamma) {
+  // output only: beta2 and gamma from the total density
+  const int nblk = 120;
+  int kinds[2] = {6, 3};
+  cudaMemcpy(R.ismall, kinds, sizeof(kinds), cudaMemcpyHostToDevice);
+  constraintQ<<<nblk, 256, 0, R.s>>>(R.rho[0], R.rho[1], R.n, R.a, R.h,
+                                     R.ismall, 2, R.small);
+  std::vector<double> part(2 * nblk);
+  cudaMemcpyAsync(part.data(), R.small, sizeof(double) * 2 * nblk,
+                  cudaMemcpyDeviceToHost, R.s);
+  cudaStreamSynchronize(R.s);
+  double q20 = 0, x2y2 = 0;
+  for (int b = 0; b < nblk; ++b) {
+    q20 += part[b];
+    x2y2 += part[nblk + b];
+  }
+  // a20 = sqrt(5/16pi) (2z^2-x^2-y^2) = q20 * sqrt(5/16pi)/(0.25 sqrt(5/pi))
+  double a20 = q20 * std::sqrt(5.0 / (16.0 * M_PI)) / (0.25 * std::sqrt(5 / M_PI));
+  double a22 = x2y2 * std::sqrt(15.0 / (32.0 * M_PI));
+  double Rr = 1.2 * std::pow(R.cfg.A, 1.0 / 3.0);
+  gamma = std::atan2(std::sqrt(2) * a22, a20);
+  beta = 4 * M_PI * a20 / (3 * R.cfg.A * Rr * Rr);
+}
+
+std::vector<int4> hoOrbitals(int nev) {
+  std::vector<int4> orbs;
+  for (int Nsh = 0; (int)orbs.size() < nev; ++Nsh)
+    for (int nr = 0; nr <= Nsh / 2 && (int)orbs.size() < nev; ++nr) {
+      int l = Nsh - 2 * nr;
+      int jp = 2 * l + 1;
+      for (int m = 1; m <= jp && (int)orbs.size() < nev; m += 2) {
+        orbs.push_back(make_int4(nr, l, jp, m));
+        if ((int)orbs.size() < nev) orbs.push_back(make_int4(nr, l, jp, -m));
+      }
+      if (l > 0) {
+        int jm = 2 * l - 1;
+        for (int m = 1; m <= jm && (int)orbs.size() < nev; m += 2) {
+          orbs.push_back(make_int4(nr, l, jm, m));
+          if ((int)orbs.size() < nev) orbs.push_back(make_int4(nr, l, jm, -m));
+        }
+      }
+    }
+  return orbs;
+}
+
+int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
+          double *spe_p, double *rho_n, double *rho_p, double *energiesOut) {
+  const double tStart = now();
+  Run R;
+  R.cfg = cfg;
+  R.n = cfg.n;
+  R.a = cfg.box_size / 2.0;
+  R.h = 2.0 * R.a / (R.n - 1);
+  R.ns = (size_t)R.n * R.n * R.n;
+  R.N = 2 * R.ns;
+  const int A = cfg.A, Z = cfg.Z, N = A - Z;
+  const bool pairing = cfg.pairing_type != NCGM_PAIRING_NONE;
+  const int orbN = pairing && cfg.pair_n.active ? cfg.pair_n.basis_size : N;
+  const int orbP = pairing && cfg.pair_p.active ? cfg.pair_p.basis_size : Z;
+  const int mx = std::max(orbN, orbP);
+  NCGM_TRY(ncgm_create(&R.ctx, R.n, R.a, 4 * mx + 8, 0));
+  R.s = R.ctx->stream;
+  R.sp[0].orb = orbN;
+  R.sp[1].orb = orbP;
+  R.sp[0].par = cfg.pair_n;
+  R.sp[1].par = cfg.pair_p;
+  if (!pairing) R.sp[0].par.active = R.sp[1].par.active = 0;
+  for (int q = 0; q < 2; ++q) {
+    R.rho[q] = R.alloc<double>(R.ns);
+    R.tau[q] = R.alloc<double>(R.ns);
+    R.J9[q] = R.alloc<double>(9 * R.ns);
+    R.divJ[q] = R.alloc<double>(R.ns);
+    R.g[q] = R.alloc<double>(3 * R.ns);
+    R.lap[q] = R.alloc<double>(R.ns);
+    R.f[q] = R.alloc<double>(R.ns);
+    R.gf[q] = R.alloc<double>(3 * R.ns);
+    R.U[q] = R.alloc<double>(R.ns);
+    R.W[q] = R.alloc<double>(3 * R.ns);
+    Species &S = R.sp[q];
+    S.X = R.alloc<double2>(R.N * mx);
+    S.Xn = R.alloc<double2>(R.N * mx);
+    S.CD = R.alloc<double2>(R.N * mx);
+    S.Phi = R.alloc<double2>(R.N * mx);
+    S.TX = R.alloc<double2>(R.N * mx);
+    if (!S.TX) {
+      setError("hf: device allocation failed");
+      return NCGM_ERR_NOMEM;
+    }
+  }
+  R.UCdir = R.alloc<double>(R.ns);
+  R.UCoul = R.alloc<double>(R.ns);
+  R.UConstr = R.alloc<double>(R.ns);
+  R.nrho = R.alloc<double>(R.ns);
+  R.ntau = R.alloc<double>(R.ns);
+  R.nJ9 = R.alloc<double>(9 * R.ns);
+  R.ndivJ = R.alloc<double>(R.ns);
+  R.scratch = R.alloc<double>(std::max<size_t>(R.ns, 64 * 1024));
+  R.poissonWork = R.alloc<double>(poissonWorkDoubles(R.n));
+  R.energy = R.alloc<double>(64);
+  const size_t sm = std::max<size_t>((size_t)4 * mx * mx + 64, 3 * 4 * 512 * 512);
+  R.cplx = R.alloc<double2>(sm);
+  R.small = R.alloc<double>(std::max<size_t>(sm, 16 * 1024));
+  R.ismall = R.alloc<int>(16 * 1024);
+  if (!R.ismall) {
+    setError("hf: device allocation failed");
+    return NCGM_ERR_NOMEM;
+  }
+  R.massCorr = cfg.com_corr ? kMass * ((double)A) / ((double)(A - 1)) : kMass;
+  if (cfg.constrain_com)
+    for (int k = 0; k < 3; ++k) R.cons.push_back(makeConstraint(k, 0.0));
+  if (cfg.curve_mode) {
+    for (int k = 0; k < 3; ++k) R.cons.push_back(makeConstraint(k, 0.0));
+    R.cons.push_back(makeConstraint(3, 0.0));
+    R.cons.push_back(makeConstraint(4, 0.0));
+    R.cons.push_back(makeConstraint(5, 0.0));
+    R.cons.push_back(makeConstraint(6, cfg.mu20));
+  }
+
+  // --- Woods-Saxon guess (main.cpp:72-111) ---------------------------------
+  double t0 = now();
+  NCGM_TRY(ncgm_set_woods_saxon(R.ctx, 0, A, Z, cfg.ws_V0, cfg.ws_r0,
+                                cfg.ws_diff, cfg.ws_kappa, cfg.initial_beta,
+                                cfg.beta3, cfg.wsso_V0, cfg.spin_orbit));
+  {
+    std::vector<int4> orbs = hoOrbitals(mx);
+    int4 *dOrbs = reinterpret_cast<int4 *>(R.ismall);
+    cudaMemcpyAsync(dOrbs, orbs.data(), sizeof(int4) * mx,
+                    cudaMemcpyHostToDevice, R.s);
+    const double nucR = std::pow(A, 0.3333333) * 1.20;
+    hoGuess(dOrbs, mx, R.n, R.a, R.h, nucR, R.sp[1].Phi, R.N, R.small, R.s);
+    NCGM_TRY(sync(R));
+    std::vector<double> lam(mx);
+    NCGM_TRY(gcgRun(R.ctx, 0, R.sp[1].Phi, mx, nullptr, 0, mx, cfg.ws_gcg,
+                    R.sp[0].Phi, lam.data(), nullptr));
+    // neutrons/protons from the same eigenpairs (main.cpp:100-108)
+    for (int q = 0; q < 2; ++q) {
+      Species &S = R.sp[q];
+      const int cols = (q == 0) ? (N >= Z ? mx : orbN) : (N >= Z ? orbP : mx);
+      cudaMemcpyAsync(S.X, R.sp[0].Phi, sizeof(double2) * R.N * cols,
+                      cudaMemcpyDeviceToDevice, R.s);
+      S.e.assign(lam.begin(), lam.begin() + cols);
+      normalizeColumns(S.X, R.N, cols, R.n, R.h, R.small, R.s);
+    }
+    NCGM_TRY(sync(R));
+  }
+  R.tGcg += now() - t0;
+
+  double Eint = 0.0, EHF = 0.0, lastdE = 0.0;
+  int it = 0;
+  bool conv = false;
+  ncgm_gcg_params hp = cfg.hf_gcg;
+  for (it = 0; it < cfg.max_iterations; ++it) {
+    NCGM_TRY(updateQuantities(R, it));
+    NCGM_TRY(buildCoefficients(R.ctx, 0, R.f[0], R.gf[0], R.U[0],
+                               cfg.spin_orbit ? R.W[0] : nullptr, nullptr));
+    NCGM_TRY(buildCoefficients(R.ctx, 1, R.f[1], R.gf[1], R.U[1],
+                               cfg.spin_orbit ? R.W[1] : nullptr,
+                               cfg.use_coulomb ? R.UCoul : nullptr));
+    t0 = now();
+    std::vector<double> lamN(orbN), lamP(orbP);
+    Species &Sn = R.sp[0], &Sp = R.sp[1];
+    NCGM_TRY(gcgRun(R.ctx, 0, Sn.X, orbN, Sn.cdCols ? Sn.CD : nullptr,
+                    Sn.cdCols, orbN, hp, Sn.Xn, lamN.data(), nullptr));
+    if (cfg.use_coulomb || N != Z) {
+      NCGM_TRY(gcgRun(R.ctx, 1, Sp.X, orbP, Sp.cdCols ? Sp.CD : nullptr,
+                      Sp.cdCols, orbP, hp, Sp.Xn, lamP.data(), nullptr));
+    } else {
+      cudaMemcpyAsync(Sp.Xn, Sn.Xn, sizeof(double2) * R.N * orbP,
+                      cudaMemcpyDeviceToDevice, R.s);
+      std::copy(lamN.begin(), lamN.begin() + orbP, lamP.begin());
+    }
+    R.tGcg += now() - t0;
+    double maxd = 0;
+    for (int i = 0; i < orbN; ++i) maxd = std::max(maxd, std::abs(lamN[i] - Sn.e[i]));
+    for (int i = 0; i < orbP; ++i) maxd = std::max(maxd, std::abs(lamP[i] - Sp.e[i]));
+    normalizeColumns(Sn.Xn, R.N, orbN, R.n, R.h, R.small, R.s);
+    normalizeColumns(Sp.Xn, R.N, orbP, R.n, R.h, R.small, R.s);
+    if (pairing) {
+      NCGM_TRY(trOrder(R, Sn, Sn.Xn));
+      NCGM_TRY(trOrder(R, Sp, Sp.Xn));
+    }
+    if (it > 0) {
+      NCGM_TRY(conjDir(R, Sn));
+      NCGM_TRY(conjDir(R, Sp));
+    }
+    std::swap(Sn.X, Sn.Xn);
+    std::swap(Sp.X, Sp.Xn);
+    Sn.e = lamN;
+    Sp.e = lamP;
+    double nE = 0, nH = 0;
+    NCGM_TRY(energies(R, nE, nH));
+    bool cconv = true;
+    for (auto &c : R.cons)
+      if (c.error() != 0.0) cconv = cconv && (c.error() < cfg.constraints_tol);
+    if (energiesOut) {
+      energiesOut[2 * it] = nE;
+      energiesOut[2 * it + 1] = nH;
+    }
+    lastdE = std::abs(nE - Eint);
+    if (!std::isfinite(nE) || !std::isfinite(nH)) {
+      setError("hf: non-finite energy");
+      return NCGM_ERR_NAN;
+    }
+    const bool speOk = cfg.spe_tol <= 0 || maxd < cfg.spe_tol;
+    if (std::abs(nE - Eint) < cfg.energy_tol &&
+        std::abs(nH - EHF) < cfg.energy_tol && cconv && speOk) {
+      Eint = nE;
+      EHF = nH;
+      conv = true;
+      ++it;
+      break;
+    }
+    R.energyDiff = std::abs(nH - EHF);
+    Eint = nE;
+    EHF = nH;
+  }
+  res.iterations = it;
+  res.converged = conv;
+  res.E_int = Eint;
+  res.E_HF = EHF;
+  res.E_pair_n = epair(R, 0);
+  res.E_pair_p = epair(R, 1);
+  res.lambda_n = cfg.pairing_type == NCGM_PAIRING_HFB ? R.sp[0].hfb.lambda
+                                                       : R.sp[0].bcs.lambda;
+  res.lambda_p = cfg.pairing_type == NCGM_PAIRING_HFB ? R.sp[1].hfb.lambda
+                                                       : R.sp[1].bcs.lambda;
+  quadDef(R, res.beta, res.gamma);
+  res.last_dE = lastdE;
+  res.t_gcg_s = R.tGcg;
+  res.t_fields_s = R.tFields;
+  res.t_poisson_s = R.tPoisson;
+  res.t_pairing_s = R.tPair;
+  if (spe_n) std::copy(R.sp[0].e.begin(), R.sp[0].e.end(), spe_n);
+  if (spe_p) std::copy(R.sp[1].e.begin(), R.sp[1].e.end(), spe_p);
+  if (rho_n) cudaMemcpy(rho_n, R.rho[0], sizeof(double) * R.ns, cudaMemcpyDeviceToHost);
+  if (rho_p) cudaMemcpy(rho_p, R.rho[1], sizeof(double) * R.ns, cudaMemcpyDeviceToHost);
+  res.wall_s = now() - tStart;
+  return NCGM_OK;
+}
+
+} // namespace
+} // namespace ncgm
+
+using namespace ncgm;
+
+extern "C" int ncgm_hf_run(const ncgm_hf_config *cfg, ncgm_hf_result *res,
+                           double *spe_n, double *spe_p, double *rho_n,
+                           double *rho_p, double *energies) {
+  try {
+    if (!cfg || !res || cfg->n < 4 || cfg->box_size <= 0 || cfg->A < 2 ||
+        cfg->Z < 0 || cfg->Z > cfg->A || cfg->max_iterations < 0) {
+      setError("ncgm_hf_run: bad configuration");
+      return NCGM_ERR_ARG;
+    }
+    std::memset(res, 0, sizeof(*res));
+    return hfRun(*cfg, *res, spe_n, spe_p, rho_n, rho_p, energies);
+  } catch (const std::exception &e) {
+    setError(e.what());
+    return NCGM_ERR_ARG;
+  }
+}
+
+extern "C" int ncgm_densities(ncgm_ctx *ctx, const double *Phi, int ncols,
+                              double *rho, double *tau, double *J9,
+                              double *divJ) {
+  try {
+    if (!ctx || !Phi || ncols < 1 || !rho || !tau || !J9 || !divJ) {
+      setError("ncgm_densities: bad argument");
+      return NCGM_ERR_ARG;
+    }
+    const size_t N = ctx->N, ns = ctx->ns;
+    double2 *dX = static_cast<double2 *>(ctx->buf(23, N * ncols * sizeof(double2)));
+    double *d = static_cast<double *>(ctx->buf(24, 12 * ns * sizeof(double)));
+    if (!dX || !d) return NCGM_ERR_NOMEM;
+    NCGM_CUDA(cudaMemcpyAsync(dX, Phi, N * ncols * sizeof(double2),
+                              cudaMemcpyDefault, ctx->stream));
+    densities(dX, N, ncols, ctx->n, ctx->h, d, d + ns, d + 2 * ns, d + 11 * ns,
+              ctx->stream);
+    NCGM_CUDA(cudaMemcpyAsync(rho, d, ns * sizeof(double), cudaMemcpyDefault,
+                              ctx->stream));
+    NCGM_CUDA(cudaMemcpyAsync(tau, d + ns, ns * sizeof(double),
+                              cudaMemcpyDefault, ctx->stream));
+    NCGM_CUDA(cudaMemcpyAsync(J9, d + 2 * ns, 9 * ns * sizeof(double),
+                              cudaMemcpyDefault, ctx->stream));
+    NCGM_CUDA(cudaMemcpyAsync(divJ, d + 11 * ns, ns * sizeof(double),
+                              cudaMemcpyDefault, ctx->stream));
+    NCGM_CUDA(cudaStreamSynchronize(ctx->stream));
+    return NCGM_OK;
+  } catch (const std::exception &e) {
+    setError(e.what());
+    return NCGM_ERR_ARG;
+  }
+}
+
+extern "C" int ncgm_poisson(ncgm_ctx *ctx, const double *rhoP, int Z,
+                            const double *U_guess, double *U_out,
+                            double *UC_out, int *iterations) {
+  try {
+    if (!ctx || !rhoP || !U_out) {
+      setError("ncgm_poisson: bad argument");
+      return NCGM_ERR_ARG;
+    }
+    const size_t ns = ctx->ns;
+    double *d = static_cast<double *>(
+        ctx->buf(25, (3 * ns + poissonWorkDoubles(ctx->n)) * sizeof(double)));
+    if (!d) return NCGM_ERR_NOMEM;
+    NCGM_CUDA(cudaMemcpyAsync(d, rhoP, ns * sizeof(double), cudaMemcpyDefault,
+                              ctx->stream));
+    if (U_guess)
+      NCGM_CUDA(cudaMemcpyAsync(d + ns, U_guess, ns * sizeof(double),
+                                cudaMemcpyDefault, ctx->stream));
+    PoissonArgs P;
+    P.n = ctx->n;
+    P.a = ctx->a;
+    P.h = ctx->h;
+    P.Z = Z;
+    P.rhoP = d;
+    P.U = d + ns;
+    P.UC = d + 2 * ns;
+    P.warm = U_guess != nullptr;
+    P.tol = 1e-13;
+    P.work = d + 3 * ns;
+    int its = 0;
+    NCGM_TRY(poissonSolve(P, ctx->stream, &its));
+    NCGM_CUDA(cudaMemcpyAsync(U_out, d + ns, ns * sizeof(double),
+                              cudaMemcpyDefault, ctx->stream));
+    if (UC_out)
+      NCGM_CUDA(cudaMemcpyAsync(UC_out, d + 2 * ns, ns * sizeof(double),
+                                cudaMemcpyDefault, ctx->stream));
+    NCGM_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (iterations) *iterations = its;
+    return NCGM_OK;
+  } catch (const std::exception &e) {
+    setError(e.what());
+    return NCGM_ERR_ARG;
+  }
 }

@@ -138,12 +138,18 @@ __global__ void cholDropKernel(const double2 *G, int ldg, int m,
         double2 r = R[(size_t)j * m + k];
         d -= r.x * r.x + r.y * r.y;
       }
-      piv = d;
-      keep[j] = (d > dropTol) ? 1 : 0;
-      if (d > dropTol) R[(size_t)j * m + j] = make_double2(sqrt(d), 0.0);
+      // The Gram pivot carries a rounding floor of ~eps * G_jj, so a column
+      // whose residual is below that floor is dependent to working precision
+      // and is dropped, as MGS drops residual norms below 1e-12.
+      const double floor = fmax(dropTol, 64.0 * 2.220446049250313e-16 *
+                                             G[(size_t)j * ldg + j].x);
+      const int kp = (d > floor) ? 1 : 0;
+      piv = kp ? d : 0.0;
+      keep[j] = kp;
+      if (kp) R[(size_t)j * m + j] = make_double2(sqrt(d), 0.0);
     }
     __syncthreads();
-    if (piv > dropTol) {
+    if (piv > 0.0) {
       const double rjj = sqrt(piv);
       // R_ji = (G_ji - sum_{k<j} conj(R_kj) R_ki) / R_jj, i > j
       for (int i = j + 1 + tid; i < m; i += nt) {

@@ -79,6 +79,65 @@ __global__ void pcgInitKernel(const typename C2<T>::type *X, size_t ldx,
   }
 }
 
+// Correction form (mixed precision): solve (A + shift) d = b - (A + shift) x
+// from d = 0 with the initial residual r0 = x lam - A x evaluated in FP64
+// (b = x (lam + shift)); algebraically the same iterates as PCG on w with
+// guess x, w = x + d, but d carries only the correction so its FP32 rounding
+// stays relative to the correction, not to w.
+template <class T>
+__global__ void pcgInitCorrKernel(const double2 *X64, const double2 *AX64,
+                                  typename C2<T>::type *Dv,
+                                  typename C2<T>::type *R,
+                                  typename C2<T>::type *Z,
+                                  typename C2<T>::type *P, size_t N,
+                                  const double *lamShift, const double *coef,
+                                  double shift, double *partials, int nblk) {
+  __shared__ double sh[kThreads];
+  const int col = blockIdx.y;
+  const double ls = lamShift[col], lam = ls - shift;
+  double bb = 0, rr = 0, rz = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x) {
+    size_t o = (size_t)col * N + i;
+    double2 x = X64[o], ax = AX64[o];
+    double bx = x.x * ls, by = x.y * ls;
+    double rx = x.x * lam - ax.x, ry = x.y * lam - ax.y;
+    double m = invDiag(coef, i / 2, shift);
+    double zx = m * rx, zy = m * ry;
+    bb += bx * bx + by * by;
+    rr += rx * rx + ry * ry;
+    rz += rx * zx + ry * zy;
+    Dv[o] = {(T)0, (T)0};
+    R[o] = {(T)rx, (T)ry};
+    Z[o] = {(T)zx, (T)zy};
+    P[o] = {(T)zx, (T)zy};
+  }
+  double s0 = blockSum(bb, sh), s1 = blockSum(rr, sh), s2 = blockSum(rz, sh);
+  if (threadIdx.x == 0) {
+    double *pp = partials + (size_t)col * nblk * 3;
+    pp[blockIdx.x] = s0;
+    pp[nblk + blockIdx.x] = s1;
+    pp[2 * nblk + blockIdx.x] = s2;
+  }
+}
+
+// w = x + d (FP64 result); a column with b = 0 returns w = 0
+template <class T>
+__global__ void pcgCombineKernel(const double2 *X64,
+                                 const typename C2<T>::type *Dv, double2 *W64,
+                                 size_t N, const PcgCol *st) {
+  const int col = blockIdx.y;
+  const bool zero = st[col].zero;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x) {
+    size_t o = (size_t)col * N + i;
+    auto d = Dv[o];
+    double2 x = X64[o];
+    W64[o] = zero ? make_double2(0.0, 0.0)
+                  : make_double2(x.x + (double)d.x, x.y + (double)d.y);
+  }
+}
+
 __global__ void pcgInitFinish(PcgCol *st, const double *partials, int nblk,
                               double tol) {
   const int col = blockIdx.x;
@@ -250,14 +309,22 @@ void pcgRun(const PcgPlan<T> &pl, cudaStream_t s) {
   const int nblk = pcgBlocks(pl.N);
   dim3 grid(nblk, pl.ncols);
   using V = typename C2<T>::type;
-  // T = (A + shift) X
-  pl.apply(pl.X, pl.ldx, pl.AP, pl.ncols, pl.shift, s);
-  pcgInitKernel<T><<<grid, kThreads, 0, s>>>(
-      reinterpret_cast<const V *>(pl.X), pl.ldx,
-      reinterpret_cast<const V *>(pl.AP), reinterpret_cast<V *>(pl.W),
-      reinterpret_cast<V *>(pl.R), reinterpret_cast<V *>(pl.Z),
-      reinterpret_cast<V *>(pl.P), pl.N, pl.lamShift, pl.coef, pl.shift,
-      pl.partials, nblk);
+  if (pl.AX64) {
+    pcgInitCorrKernel<T><<<grid, kThreads, 0, s>>>(
+        pl.X64, pl.AX64, reinterpret_cast<V *>(pl.W),
+        reinterpret_cast<V *>(pl.R), reinterpret_cast<V *>(pl.Z),
+        reinterpret_cast<V *>(pl.P), pl.N, pl.lamShift, pl.coef, pl.shift,
+        pl.partials, nblk);
+  } else {
+    // T = (A + shift) X
+    pl.apply(pl.X, pl.ldx, pl.AP, pl.ncols, pl.shift, s);
+    pcgInitKernel<T><<<grid, kThreads, 0, s>>>(
+        reinterpret_cast<const V *>(pl.X), pl.ldx,
+        reinterpret_cast<const V *>(pl.AP), reinterpret_cast<V *>(pl.W),
+        reinterpret_cast<V *>(pl.R), reinterpret_cast<V *>(pl.Z),
+        reinterpret_cast<V *>(pl.P), pl.N, pl.lamShift, pl.coef, pl.shift,
+        pl.partials, nblk);
+  }
   pcgInitFinish<<<pl.ncols, 32, 0, s>>>(pl.st, pl.partials, nblk, pl.tol);
   for (int it = 0; it < pl.maxSteps; ++it) {
     pl.apply(pl.P, pl.N, pl.AP, pl.ncols, pl.shift, s);
@@ -275,8 +342,12 @@ void pcgRun(const PcgPlan<T> &pl, cudaStream_t s) {
         reinterpret_cast<V *>(pl.P), reinterpret_cast<const V *>(pl.Z), pl.N,
         pl.st);
   }
-  pcgZeroKernel<T><<<grid, kThreads, 0, s>>>(reinterpret_cast<V *>(pl.W),
-                                             pl.N, pl.st);
+  if (pl.AX64)
+    pcgCombineKernel<T><<<grid, kThreads, 0, s>>>(
+        pl.X64, reinterpret_cast<const V *>(pl.W), pl.W64, pl.N, pl.st);
+  else
+    pcgZeroKernel<T><<<grid, kThreads, 0, s>>>(reinterpret_cast<V *>(pl.W),
+                                               pl.N, pl.st);
 }
 
 template void pcgRun<double>(const PcgPlan<double> &, cudaStream_t);

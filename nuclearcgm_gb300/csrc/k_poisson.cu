@@ -1,0 +1,338 @@
+// Coulomb direct potential by the Poisson equation, the device form of
+// Wavefunction::coulombFieldPoisson (src/util/wavefunction.cpp:55-229):
+//   L U = -4 pi e^2 rho_p - (boundary terms),
+// L the 5-point (4th-order) Laplacian truncated at the box edge
+// (LaplacianPotential, src/coulomb/laplacianp_potential.cpp:18-73), with a
+// Dirichlet halo potential e^2 Z / r + e^2 (Y20 Q20 + 2 Y22 Q22) / r two
+// layers deep. The halo is indexed i*dim*dim + j*dim + k while the
+// right-hand side uses the same index expression, so the halo's x and z roles
+// are swapped relative to the lattice; that is kept. The reference solves with
+// BiCGSTAB to machine epsilon; L is symmetric negative definite, so the device
+// uses conjugate gradients on -L to a relative residual of 1e-13 (warm start
+// from the previous potential), which reaches the same solution to rounding.
+#include "k_poisson.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+namespace ncgm {
+
+namespace {
+
+__device__ __forceinline__ double trapW(size_t p, int n) {
+  const int i = (int)(p % n), j = (int)((p / n) % n), k = (int)(p / ((size_t)n * n));
+  double w = 1.0;
+  if (i == 0 || i == n - 1) w *= 0.5;
+  if (j == 0 || j == n - 1) w *= 0.5;
+  if (k == 0 || k == n - 1) w *= 0.5;
+  return w;
+}
+
+__device__ double blockReduce(double v, double *sh) {
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  double r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+// Q20 / Q22 integrals of rho_p (wavefunction.cpp:74-92), partials per block
+__global__ void quadKernel(const double *rho, int n, double a, double h,
+                           double *partials) {
+  __shared__ double sh[256];
+  const size_t ns = (size_t)n * n * n;
+  const double hhh = h * h * h;
+  double q20 = 0, q22 = 0;
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < ns;
+       p += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(p % n), j = (int)((p / n) % n), k = (int)(p / ((size_t)n * n));
+    const double x = -a + i * h, y = -a + j * h, z = -a + k * h;
+    const double w = trapW(p, n) * hhh;
+    q20 += (rho[p] * (2.0 * z * z - x * x - y * y)) * sqrt(5.0 / (16.0 * M_PI)) * w;
+    q22 += (rho[p] * (x * x - y * y)) * sqrt(15.0 / (32.0 * M_PI)) * w;
+  }
+  double s0 = blockReduce(q20, sh), s1 = blockReduce(q22, sh);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = s0;
+    partials[gridDim.x + blockIdx.x] = s1;
+  }
+}
+
+// halo potential at halo index (a, b, c) of the (n+4)^3 box
+__device__ __forceinline__ double haloV(int ia, int ib, int ic, double A,
+                                        double h, double Z, double Q20,
+                                        double Q22) {
+  const double x = -A - 2 * h + ia * h, y = -A - 2 * h + ib * h,
+               z = -A - 2 * h + ic * h;
+  double r = sqrt(x * x + y * y + z * z);
+  const double rr = r;
+  if (r < 1e-9) r = 1e-9;
+  const double theta = acos(z / rr);
+  const double phi = atan2(y, x);
+  const double y20 = sqrt(5.0 / (16.0 * M_PI)) * (3.0 * cos(theta) * cos(theta) - 1.0);
+  const double y22 = sqrt(15.0 / (32.0 * M_PI)) * cos(2 * phi) * sin(theta) * sin(theta);
+  double v = (kE2Poisson * Z) / r;
+  v += kE2Poisson * (y20 * Q20 + 2.0 * y22 * Q22) / r;
+  return v;
+}
+
+__global__ void rhsKernel(const double *rho, int n, double A, double h,
+                          double Z, const double *q, double *rhs) {
+  const size_t ns = (size_t)n * n * n;
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= ns) return;
+  const double Q20 = q[0], Q22 = q[1];
+  const double hh = h * h;
+  const double eps0inv = kE2Poisson * 4 * M_PI;
+  double v = -eps0inv * rho[e];
+  // rhs index e = a n^2 + b n + c (the reference's face lambda)
+  const int a = (int)(e / ((size_t)n * n)), b = (int)((e / n) % n),
+            c = (int)(e % n);
+  auto H = [&](int ia, int ib, int ic) {
+    return haloV(ia, ib, ic, A, h, Z, Q20, Q22);
+  };
+  // faces in the reference's order: first, second, third lambda index
+  if (a == 0) {
+    v -= (16.0 / 12.0) * H(1, b + 2, c + 2) / hh;
+    v += (1.0 / 12.0) * H(0, b + 2, c + 2) / hh;
+  }
+  if (a == 1) v += (1.0 / 12.0) * H(1, b + 2, c + 2) / hh;
+  if (a == n - 1) {
+    v -= (16.0 / 12.0) * H(n + 2, b + 2, c + 2) / hh;
+    v += (1.0 / 12.0) * H(n + 3, b + 2, c + 2) / hh;
+  }
+  if (a == n - 2) v += (1.0 / 12.0) * H(n + 2, b + 2, c + 2) / hh;
+  if (b == 0) {
+    v -= (16.0 / 12.0) * H(a + 2, 1, c + 2) / hh;
+    v += (1.0 / 12.0) * H(a + 2, 0, c + 2) / hh;
+  }
+  if (b == 1) v += (1.0 / 12.0) * H(a + 2, 1, c + 2) / hh;
+  if (b == n - 1) {
+    v -= (16.0 / 12.0) * H(a + 2, n + 2, c + 2) / hh;
+    v += (1.0 / 12.0) * H(a + 2, n + 3, c + 2) / hh;
+  }
+  if (b == n - 2) v += (1.0 / 12.0) * H(a + 2, n + 2, c + 2) / hh;
+  if (c == 0) {
+    v -= (16.0 / 12.0) * H(a + 2, b + 2, 1) / hh;
+    v += (1.0 / 12.0) * H(a + 2, b + 2, 0) / hh;
+  }
+  if (c == 1) v += (1.0 / 12.0) * H(a + 2, b + 2, 1) / hh;
+  if (c == n - 1) {
+    v -= (16.0 / 12.0) * H(a + 2, b + 2, n + 2) / hh;
+    v += (1.0 / 12.0) * H(a + 2, b + 2, n + 3) / hh;
+  }
+  if (c == n - 2) v += (1.0 / 12.0) * H(a + 2, b + 2, n + 2) / hh;
+  rhs[e] = v;
+}
+
+// y = -L x (positive definite form), partial sums of x.y
+__global__ void negLapKernel(const double *x, double *y, int n, double h,
+                             double *partials) {
+  __shared__ double sh[256];
+  const size_t ns = (size_t)n * n * n;
+  const double hh = h * h;
+  const double c0 = (90.0 / 12.0) / hh, c1 = -(16.0 / 12.0) / hh,
+               c2 = (1.0 / 12.0) / hh;
+  double acc = 0;
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < ns;
+       p += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(p % n), j = (int)((p / n) % n), k = (int)(p / ((size_t)n * n));
+    const size_t sy = n, sz = (size_t)n * n;
+    double s = c0 * x[p];
+    if (i >= 1) s += c1 * x[p - 1];
+    if (i >= 2) s += c2 * x[p - 2];
+    if (i + 1 < n) s += c1 * x[p + 1];
+    if (i + 2 < n) s += c2 * x[p + 2];
+    if (j >= 1) s += c1 * x[p - sy];
+    if (j >= 2) s += c2 * x[p - 2 * sy];
+    if (j + 1 < n) s += c1 * x[p + sy];
+    if (j + 2 < n) s += c2 * x[p + 2 * sy];
+    if (k >= 1) s += c1 * x[p - sz];
+    if (k >= 2) s += c2 * x[p - 2 * sz];
+    if (k + 1 < n) s += c1 * x[p + sz];
+    if (k + 2 < n) s += c2 * x[p + 2 * sz];
+    y[p] = s;
+    acc += x[p] * s;
+  }
+  double t = blockReduce(acc, sh);
+  if (partials && threadIdx.x == 0) partials[blockIdx.x] = t;
+}
+
+// r = b - (-L) U from y = -L U ; partials |r|^2, |b|^2 ; p = r
+__global__ void cgInitKernel(const double *rhs, const double *y, double *r,
+                             double *p, size_t ns, double *partials) {
+  __shared__ double sh[256];
+  double rr = 0, bb = 0;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < ns;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const double b = -rhs[e];
+    const double v = b - y[e];
+    r[e] = v;
+    p[e] = v;
+    rr += v * v;
+    bb += b * b;
+  }
+  double s0 = blockReduce(rr, sh), s1 = blockReduce(bb, sh);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = s0;
+    partials[gridDim.x + blockIdx.x] = s1;
+  }
+}
+
+// scalars: s[0] = rr, s[1] = bb, s[2] = pAp, s[3] = done
+__global__ void cgScalarInit(const double *partials, int nblk, double *s) {
+  if (threadIdx.x) return;
+  double rr = 0, bb = 0;
+  for (int b = 0; b < nblk; ++b) {
+    rr += partials[b];
+    bb += partials[nblk + b];
+  }
+  s[0] = rr;
+  s[1] = bb;
+  s[3] = (bb == 0.0) ? 1.0 : 0.0;
+}
+
+// alpha = rr / pAp; x += alpha p; r -= alpha Ap; partial |r|^2
+__global__ void cgUpdateKernel(double *x, double *r, const double *p,
+                               const double *Ap, size_t ns,
+                               const double *pApPartials, int nblk,
+                               const double *s, double *partials) {
+  __shared__ double sh[256];
+  __shared__ double alpha;
+  if (s[3] != 0.0) return;
+  if (threadIdx.x == 0) {
+    double pAp = 0;
+    for (int b = 0; b < nblk; ++b) pAp += pApPartials[b];
+    alpha = s[0] / pAp;
+  }
+  __syncthreads();
+  const double al = alpha;
+  double rr = 0;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < ns;
+       e += (size_t)gridDim.x * blockDim.x) {
+    x[e] += al * p[e];
+    const double v = r[e] - al * Ap[e];
+    r[e] = v;
+    rr += v * v;
+  }
+  double t = blockReduce(rr, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = t;
+}
+
+// beta = rr_new / rr; p = r + beta p; s[0] = rr_new; done when below tol
+__global__ void cgDirKernel(double *p, const double *r, size_t ns,
+                            const double *partials, int nblk, double *s,
+                            double tol2) {
+  __shared__ double beta, rrn;
+  if (s[3] != 0.0) return;
+  if (threadIdx.x == 0) {
+    double v = 0;
+    for (int b = 0; b < nblk; ++b) v += partials[b];
+    rrn = v;
+    beta = v / s[0];
+  }
+  __syncthreads();
+  const double bt = beta;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < ns;
+       e += (size_t)gridDim.x * blockDim.x)
+    p[e] = r[e] + bt * p[e];
+  // Blocks of this launch still read s[0], so the new residual goes to s[4]
+  // and cgCommit (the next launch) moves it into place.
+  __syncthreads();
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    s[4] = rrn;
+    s[5] = (rrn <= tol2 * s[1]) ? 1.0 : 0.0;
+  }
+}
+
+__global__ void cgCommit(double *s) {
+  if (threadIdx.x) return;
+  if (s[3] != 0.0) return;
+  s[0] = s[4];
+  s[3] = s[5];
+}
+
+__global__ void exchangeKernel(const double *rhoP, const double *Ud,
+                               double *UC, size_t ns) {
+  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= ns) return;
+  double v = 0.0;
+  v -= kE2Poisson * pow(3.0 / M_PI, 1.0 / 3.0) * pow(rhoP[e], 1.0 / 3.0);
+  UC[e] = Ud[e] + v;
+}
+
+} // namespace
+
+int poissonSolve(const PoissonArgs &P, cudaStream_t s, int *iterations) {
+  const int n = P.n;
+  const size_t ns = (size_t)n * n * n;
+  const int nblk = 120;
+  double *q = P.work;                 // 2
+  double *sc = P.work + 8;            // 8 scalars
+  double *part = P.work + 16;         // 2 * nblk
+  double *part2 = part + 2 * nblk;    // nblk
+  double *rhs = P.work + 16 + 4 * nblk;
+  double *r = rhs + ns, *p = r + ns, *Ap = p + ns;
+  quadKernel<<<nblk, 256, 0, s>>>(P.rhoP, n, P.a, P.h, part);
+  // reduce Q20, Q22 (2 values)
+  {
+    std::vector<double> hp(2 * nblk);
+    cudaMemcpyAsync(hp.data(), part, sizeof(double) * 2 * nblk,
+                    cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return NCGM_ERR_CUDA;
+    double qq[2] = {0, 0};
+    for (int b = 0; b < nblk; ++b) {
+      qq[0] += hp[b];
+      qq[1] += hp[nblk + b];
+    }
+    cudaMemcpyAsync(q, qq, sizeof(double) * 2, cudaMemcpyHostToDevice, s);
+  }
+  rhsKernel<<<(unsigned)((ns + 255) / 256), 256, 0, s>>>(P.rhoP, n, P.a, P.h,
+                                                          P.Z, q, rhs);
+  if (!P.warm) cudaMemsetAsync(P.U, 0, ns * sizeof(double), s);
+  negLapKernel<<<nblk, 256, 0, s>>>(P.U, Ap, n, P.h, nullptr);
+  cgInitKernel<<<nblk, 256, 0, s>>>(rhs, Ap, r, p, ns, part);
+  cgScalarInit<<<1, 32, 0, s>>>(part, nblk, sc);
+  const double tol2 = P.tol * P.tol;
+  int it = 0;
+  const int maxit = std::max(100, (int)std::min<size_t>(4 * ns, 20000));
+  double hs[8];
+  double best = 1e300;
+  int sinceBest = 0;
+  for (; it < maxit;) {
+    for (int b = 0; b < 16; ++b, ++it) {
+      negLapKernel<<<nblk, 256, 0, s>>>(p, Ap, n, P.h, part2);
+      cgUpdateKernel<<<nblk, 256, 0, s>>>(P.U, r, p, Ap, ns, part2, nblk, sc,
+                                          part);
+      cgDirKernel<<<nblk, 256, 0, s>>>(p, r, ns, part, nblk, sc, tol2);
+      cgCommit<<<1, 32, 0, s>>>(sc);
+    }
+    cudaMemcpyAsync(hs, sc, sizeof(double) * 8, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return NCGM_ERR_CUDA;
+    if (!std::isfinite(hs[0])) return NCGM_ERR_NAN;
+    if (hs[3] != 0.0) break;
+    // stagnation guard: rounding floor reached
+    if (hs[0] < 0.5 * best) {
+      best = hs[0];
+      sinceBest = 0;
+    } else if (++sinceBest > 8) {
+      break;
+    }
+  }
+  exchangeKernel<<<(unsigned)((ns + 255) / 256), 256, 0, s>>>(P.rhoP, P.U,
+                                                               P.UC, ns);
+  if (iterations) *iterations = it;
+  return cudaGetLastError() == cudaSuccess ? NCGM_OK : NCGM_ERR_CUDA;
+}
+
+size_t poissonWorkDoubles(int n) {
+  const size_t ns = (size_t)n * n * n;
+  return 16 + 4 * 120 + 4 * ns + 64;
+}
+
+} // namespace ncgm

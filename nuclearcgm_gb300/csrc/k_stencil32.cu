@@ -1,0 +1,426 @@
+// FP32 H.X stencil: persistent streaming kernel on TMA tensor tiles.
+//
+// Same operator as stencilPoint in k_hamiltonian.cu (the matrix-free form of
+// Hamiltonian::buildMatrix, src/hamiltonian/hamiltonian.cpp:303-372), built
+// for HBM bandwidth on GB300:
+//  * A 5-D tensor map views X as [col][k][j][i][4 floats]. One TMA box is a
+//    padded (TY+4) x (n+4) band of one z plane starting at i = -2,
+//    j = y0 - 2; out-of-range coordinates (also z < 0, z >= n) are zero-filled
+//    by the TMA unit, which is the reference's Dirichlet truncation, so the
+//    arithmetic has no bounds checks.
+//  * The grid is a fixed number of CTAs per SM. The (column, band, z) output
+//    planes are flattened and split into equal contiguous ranges, one per
+//    CTA; a CTA streams its range through a shared-memory ring with one TMA
+//    pipeline that runs across column/band boundaries (4 extra halo planes
+//    at each boundary), so loads stay `ring - 5` planes ahead of the compute.
+//  * Every thread owns fixed in-band points; the per-point field coefficients
+//    (L2 resident, shared by all columns) are loaded before the plane wait.
+//  * mbarrier waits are bounded: on timeout the CTA records an error flag,
+//    drains its own copies (bounded) and returns.
+#include "ncgm_internal.cuh"
+#include "stencil_core.cuh"
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <vector>
+
+namespace ncgm {
+
+int *stencilErrWord();
+
+namespace {
+
+constexpr int kPPT = 4;       // max owned points per thread
+constexpr int kMaxRuns = 48;  // (column, band) runs per CTA
+
+__device__ __forceinline__ uint32_t smemAddr(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbarInit(uint64_t *bar, int count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(bar)),
+               "r"(count));
+}
+__device__ __forceinline__ void mbarExpectTx(uint64_t *bar, uint32_t bytes) {
+  asm volatile(
+      "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+          smemAddr(bar)),
+      "r"(bytes)
+      : "memory");
+}
+__device__ __forceinline__ bool mbarWait(uint64_t *bar, uint32_t phase,
+                                         uint32_t limit) {
+  for (uint32_t it = 0; it < limit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n"
+        " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smemAddr(bar)), "r"(phase)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void tmaTile5(void *dst, const CUtensorMap *map,
+                                         int c1, int c2, int c3, int c4,
+                                         uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::"
+      "complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(
+          smemAddr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(c1), "r"(c2), "r"(c3),
+      "r"(c4), "r"(smemAddr(bar))
+      : "memory");
+}
+
+struct StreamArgs {
+  float4 *Y;
+  const float4 *coef;
+  int n, TY, nbands, ring, ppt;
+  size_t ns;
+  long long total; // ncols * nbands * n output band-planes
+  float shift;
+  int *err;
+};
+
+struct Run {
+  int cb, ka, kb, base;
+};
+
+__global__ void __launch_bounds__(512)
+    stencilStream32(const __grid_constant__ CUtensorMap map, StreamArgs A) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ Run runs[kMaxRuns];
+  __shared__ int nruns, totalSeq;
+  const int n = A.n, W = n + 4;
+  const int boxElems = (A.TY + 4) * W;
+  const int slotElems = (boxElems + 7) & ~7; // 128-byte aligned slots
+  const uint32_t boxBytes = boxElems * 16u;
+  float4 *ring = reinterpret_cast<float4 *>(smem_raw);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(
+      smem_raw + (size_t)A.ring * slotElems * 16u);
+  const long long t0 = (long long)blockIdx.x * A.total / gridDim.x;
+  const long long t1 = (long long)(blockIdx.x + 1) * A.total / gridDim.x;
+
+  if (threadIdx.x == 0) {
+    int r = 0, seq = 0;
+    for (long long t = t0; t < t1 && r < kMaxRuns;) {
+      const int cb = (int)(t / n), ka = (int)(t % n);
+      const long long rem = t1 - t;
+      const int kb = (rem < (long long)(n - ka)) ? ka + (int)rem : n;
+      runs[r] = {cb, ka, kb, seq};
+      seq += kb - ka + 4;
+      t += kb - ka;
+      ++r;
+    }
+    nruns = r;
+    totalSeq = seq;
+    for (int s = 0; s < A.ring; ++s) mbarInit(&bars[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const int NR = nruns, TS = totalSeq;
+
+  // owned points of a band: q = tid + t * blockDim, lr its padded slot index
+  int qv[kPPT], lr[kPPT];
+#pragma unroll
+  for (int t = 0; t < kPPT; ++t) {
+    int q = threadIdx.x + t * blockDim.x;
+    if (t >= A.ppt || q >= A.TY * n) q = 0x7fffffff;
+    qv[t] = q;
+    lr[t] = (q == 0x7fffffff) ? 0 : ((q / n) + 2) * W + (q % n) + 2;
+  }
+
+  // producer state (thread 0): run cursor and next z in that run
+  int pr = 0, pz = (NR > 0) ? runs[0].ka - 2 : 0, nextSeq = 0;
+  auto issue = [&]() {
+    const Run &R = runs[pr];
+    const int s = nextSeq;
+    const int slot = s % A.ring;
+    const int col = R.cb / A.nbands, band = R.cb % A.nbands;
+    mbarExpectTx(&bars[slot], boxBytes);
+    tmaTile5(ring + (size_t)slot * slotElems, &map, -2, band * A.TY - 2, pz,
+             col, &bars[slot]);
+    ++nextSeq;
+    if (++pz >= R.kb + 2 && pr + 1 < NR) {
+      ++pr;
+      pz = runs[pr].ka - 2;
+    }
+  };
+  if (threadIdx.x == 0)
+    while (nextSeq < TS && nextSeq < A.ring) issue();
+
+  const uint32_t kLimit = 1u << 22;
+  bool ok = true;
+  int waited = -1;
+  for (int r = 0; r < NR && ok; ++r) {
+    const Run R = runs[r];
+    const int col = R.cb / A.nbands, band = R.cb % A.nbands;
+    const int y0 = band * A.TY;
+    const int tyn = min(A.TY, n - y0) * n;
+    float4 *Yc = A.Y + (size_t)col * A.ns;
+    for (int k = R.ka; k < R.kb; ++k) {
+      const int s0 = R.base + (k - R.ka);
+      // field coefficients first: independent of the plane data
+      const unsigned pbase = (unsigned)k * (unsigned)(n * n) + (unsigned)(y0 * n);
+      float4 ca[kPPT], cbv[kPPT];
+#pragma unroll
+      for (int t = 0; t < kPPT; ++t)
+        if (qv[t] < tyn) {
+          const float4 *c2 = A.coef + 2 * (size_t)(pbase + qv[t]);
+          ca[t] = __ldg(c2);
+          cbv[t] = __ldg(c2 + 1);
+        }
+      while (ok && waited < s0 + 4) {
+        const int s = waited + 1;
+        if (!mbarWait(&bars[s % A.ring], (s / A.ring) & 1u, kLimit)) ok = false;
+        else waited = s;
+      }
+      ok = __syncthreads_and(ok);
+      if (!ok) break;
+      const float4 *pm2 = ring + (size_t)((s0) % A.ring) * slotElems;
+      const float4 *pm1 = ring + (size_t)((s0 + 1) % A.ring) * slotElems;
+      const float4 *pc = ring + (size_t)((s0 + 2) % A.ring) * slotElems;
+      const float4 *pp1 = ring + (size_t)((s0 + 3) % A.ring) * slotElems;
+      const float4 *pp2 = ring + (size_t)((s0 + 4) % A.ring) * slotElems;
+#pragma unroll
+      for (int t = 0; t < kPPT; ++t)
+        if (qv[t] < tyn) {
+          const int l = lr[t];
+          float c[8] = {ca[t].x, ca[t].y, ca[t].z, ca[t].w,
+                        cbv[t].x, cbv[t].y, cbv[t].z, cbv[t].w};
+          auto S = [](float4 v) { return Spinor<float>{v.x, v.y, v.z, v.w}; };
+          Spinor<float> o = pointH<float>(
+              c, A.shift, S(pc[l]), S(pc[l + 1]), S(pc[l - 1]), S(pc[l + 2]),
+              S(pc[l - 2]), S(pc[l + W]), S(pc[l - W]), S(pc[l + 2 * W]),
+              S(pc[l - 2 * W]), S(pp1[l]), S(pm1[l]), S(pp2[l]), S(pm2[l]));
+          Yc[pbase + qv[t]] = make_float4(o.r0, o.i0, o.r1, o.i1);
+        }
+      __syncthreads(); // every seq below the next plane's first is free now
+      if (threadIdx.x == 0) {
+        // lowest sequence still needed: the next plane of this run, or the
+        // first plane of the next run (the tail halo of this run is done)
+        const int low = (k + 1 < R.kb) ? s0 + 1
+                                        : (r + 1 < NR ? runs[r + 1].base : TS);
+        while (nextSeq < TS && nextSeq < low + A.ring) issue();
+      }
+    }
+  }
+  if (!ok) {
+    if (threadIdx.x == 0) atomicExch(A.err, 1);
+    for (int s = waited + 1; s < nextSeq; ++s)
+      mbarWait(&bars[s % A.ring], (s / A.ring) & 1u, kLimit);
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encodeFn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void *p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                         cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+struct MapEntry {
+  const void *ptr;
+  int n, ncols, TY;
+  CUtensorMap map;
+};
+std::vector<MapEntry> g_maps;
+
+// 5-D map of X: dims (4 floats, i, j, k, col), box (4, n+4, TY+4, 1, 1).
+bool tensorMapFor(const void *X, int n, int ncols, int TY, CUtensorMap *out) {
+  for (auto &e : g_maps)
+    if (e.ptr == X && e.n == n && e.ncols == ncols && e.TY == TY) {
+      *out = e.map;
+      return true;
+    }
+  auto fn = encodeFn();
+  if (!fn) return false;
+  cuuint64_t dims[5] = {4, (cuuint64_t)n, (cuuint64_t)n, (cuuint64_t)n,
+                        (cuuint64_t)ncols};
+  cuuint64_t strides[4] = {16, (cuuint64_t)16 * n, (cuuint64_t)16 * n * n,
+                           (cuuint64_t)16 * n * n * n};
+  cuuint32_t box[5] = {4, (cuuint32_t)(n + 4), (cuuint32_t)(TY + 4), 1, 1};
+  cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  CUtensorMap m;
+  CUresult r = fn(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, const_cast<void *>(X),
+                  dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return false;
+  if (g_maps.size() > 64) g_maps.erase(g_maps.begin());
+  g_maps.push_back({X, n, ncols, TY, m});
+  *out = m;
+  return true;
+}
+
+size_t streamSmem(int n, int TY, int ring) {
+  size_t slot = (((size_t)(TY + 4) * (n + 4) + 7) & ~size_t(7)) * 16;
+  return (size_t)ring * slot + (size_t)ring * 8;
+}
+
+int smCount() {
+  static int c = 0;
+  if (!c) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev);
+    if (c <= 0) c = 1;
+  }
+  return c;
+}
+
+struct Shape {
+  int TY, ring, ppt, ctasPerSM;
+};
+
+bool validShape(int n, const Shape &s, int &threads) {
+  if (s.TY < 1 || s.TY > n || s.ring < 6 || s.ppt < 1 || s.ppt > kPPT)
+    return false;
+  if (s.TY + 4 > 256 || n + 4 > 256) return false;
+  const int pts = s.TY * n;
+  threads = ((pts + s.ppt - 1) / s.ppt + 31) / 32 * 32;
+  if (threads > 512 || threads < 32) return false;
+  if (streamSmem(n, s.TY, s.ring) * s.ctasPerSM > 220 * 1024) return false;
+  return true;
+}
+
+bool launchStream(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
+                  int ncols, float shift, cudaStream_t st, const Shape &sh) {
+  const int n = ctx->n;
+  int threads = 0;
+  if (!validShape(n, sh, threads)) return false;
+  CUtensorMap map;
+  if (!tensorMapFor(X, n, ncols, sh.TY, &map)) return false;
+  StreamArgs A;
+  A.Y = reinterpret_cast<float4 *>(Y);
+  A.coef = reinterpret_cast<const float4 *>(ctx->sp[species].coef32);
+  A.n = n;
+  A.TY = sh.TY;
+  A.nbands = (n + sh.TY - 1) / sh.TY;
+  A.ring = sh.ring;
+  A.ppt = sh.ppt;
+  A.ns = ctx->ns;
+  A.total = (long long)ncols * A.nbands * n;
+  A.shift = shift;
+  A.err = stencilErrWord();
+  // enough CTAs that no CTA holds more than kMaxRuns runs
+  long long ctas = (long long)smCount() * sh.ctasPerSM;
+  const long long minCtas = (A.total + (long long)(kMaxRuns - 2) * n - 1) /
+                            ((long long)(kMaxRuns - 2) * n);
+  ctas = std::max(ctas, minCtas);
+  ctas = std::min<long long>(ctas, A.total);
+  stencilStream32<<<(unsigned)ctas, threads, streamSmem(n, sh.TY, sh.ring),
+                    st>>>(map, A);
+  return true;
+}
+
+struct TunedShape {
+  ncgm_ctx *ctx;
+  Shape s;
+};
+std::vector<TunedShape> g_tuned;
+
+Shape defaultShape(int n) {
+  Shape s{n, 8, 4, 1};
+  int th;
+  while (!validShape(n, s, th) && s.TY > 1) {
+    if (s.TY * n > 512 * s.ppt && s.ppt < kPPT) {
+      s.ppt *= 2;
+      continue;
+    }
+    s.TY = (s.TY + 1) / 2;
+  }
+  return s;
+}
+
+} // namespace
+
+// Project autotuner for the FP32 stencil: times candidate (band rows, ring
+// depth, points per thread, CTAs per SM) on the context's own lattice with
+// CUDA events and keeps the fastest. Runs once per context.
+static Shape tune(ncgm_ctx *ctx, int species, int ncols) {
+  const int n = ctx->n;
+  ncols = std::max(1, std::min(ncols, ctx->max_cols));
+  size_t bytes = ctx->N * ncols * sizeof(float2);
+  float2 *X = static_cast<float2 *>(ctx->buf(1, bytes));
+  float2 *Y = static_cast<float2 *>(ctx->buf(2, bytes));
+  Shape best = defaultShape(n);
+  if (!X || !Y) return best;
+  cudaMemsetAsync(X, 0, bytes, ctx->stream);
+  std::vector<int> rows;
+  for (int r = n;; r = (r + 1) / 2) {
+    rows.push_back(r);
+    if (r <= 4) break;
+  }
+  float bestMs = 1e30f;
+  for (int TY : rows)
+    for (int ring : {6, 8, 10, 12})
+      for (int ppt : {1, 2, 4})
+        for (int cps : {1, 2}) {
+          Shape s{TY, ring, ppt, cps};
+          int th;
+          if (!validShape(n, s, th)) continue;
+          if (!launchStream(ctx, species, X, Y, ncols, 0.f, ctx->stream, s))
+            continue;
+          cudaEventRecord(ctx->ev0, ctx->stream);
+          for (int r = 0; r < 3; ++r)
+            launchStream(ctx, species, X, Y, ncols, 0.f, ctx->stream, s);
+          cudaEventRecord(ctx->ev1, ctx->stream);
+          if (cudaEventSynchronize(ctx->ev1) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+          }
+          float ms = 0;
+          cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+          if (ms < bestMs) {
+            bestMs = ms;
+            best = s;
+          }
+        }
+  return best;
+}
+
+void applyH32(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
+              int ncols, float shift, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(stencilStream32,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         220 * 1024);
+    attr = true;
+  }
+  Shape *sh = nullptr;
+  for (auto &t : g_tuned)
+    if (t.ctx == ctx) sh = &t.s;
+  if (!sh) {
+    g_tuned.push_back({ctx, defaultShape(ctx->n)});
+    Shape tuned = tune(ctx, species, ncols);
+    for (auto &t : g_tuned)
+      if (t.ctx == ctx) {
+        t.s = tuned;
+        sh = &t.s;
+      }
+  }
+  if (!launchStream(ctx, species, X, Y, ncols, shift, s, *sh))
+    setError("FP32 stencil: launch shape or tensor map unavailable");
+}
+
+void forgetStencilShape(ncgm_ctx *ctx) {
+  for (size_t i = 0; i < g_tuned.size(); ++i)
+    if (g_tuned[i].ctx == ctx) {
+      g_tuned.erase(g_tuned.begin() + i);
+      return;
+    }
+}
+
+} // namespace ncgm

@@ -80,16 +80,10 @@ void applyH64(ncgm_ctx *ctx, int species, const double2 *X, double2 *Y,
               int ncols, double shift, cudaStream_t s);
 void applyH32(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
               int ncols, float shift, cudaStream_t s);
-// Tuned launch shape of the FP32 stencil (chosen by the autotuner).
-struct StencilShape {
-  int kchunk = 8;
-  int threads = 256;
-  int rows = 0; // lattice rows per CTA band (0: default)
-  int ring = 6; // shared-memory ring slots
-  bool tuned = false, tuning = false;
-};
-StencilShape &stencilShape32(ncgm_ctx *ctx);
-int autotuneStencil32(ncgm_ctx *ctx, int species, int ncols);
+// Drops the FP32 stencil launch shape tuned for a context (on destroy).
+void forgetStencilShape(ncgm_ctx *ctx);
+// Non-zero when a stencil's bounded wait gave up since the last reset.
+int stencilErrorFlag();
 
 void convert64to32(const double2 *in, float2 *out, size_t count,
                    cudaStream_t s);
