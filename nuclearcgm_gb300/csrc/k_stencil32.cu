@@ -90,12 +90,16 @@ struct Run {
   int cb, ka, kb, base;
 };
 
-__global__ void __launch_bounds__(512)
+// PPT: points owned per thread (register budget); WFIX: padded row width
+// n + 4 fixed at compile time for the common lattices (0: runtime), which
+// turns the +-W, +-2W neighbour offsets into immediates.
+template <int PPT, int WFIX>
+__global__ void __launch_bounds__(512, PPT == 1 ? 2 : 1)
     stencilStream32(const __grid_constant__ CUtensorMap map, StreamArgs A) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ Run runs[kMaxRuns];
   __shared__ int nruns, totalSeq;
-  const int n = A.n, W = n + 4;
+  const int n = A.n, W = WFIX ? WFIX : n + 4;
   const int boxElems = (A.TY + 4) * W;
   const int slotElems = (boxElems + 7) & ~7; // 128-byte aligned slots
   const uint32_t boxBytes = boxElems * 16u;
@@ -125,11 +129,11 @@ __global__ void __launch_bounds__(512)
   const int NR = nruns, TS = totalSeq;
 
   // owned points of a band: q = tid + t * blockDim, lr its padded slot index
-  int qv[kPPT], lr[kPPT];
+  int qv[PPT], lr[PPT];
 #pragma unroll
-  for (int t = 0; t < kPPT; ++t) {
+  for (int t = 0; t < PPT; ++t) {
     int q = threadIdx.x + t * blockDim.x;
-    if (t >= A.ppt || q >= A.TY * n) q = 0x7fffffff;
+    if (q >= A.TY * n) q = 0x7fffffff;
     qv[t] = q;
     lr[t] = (q == 0x7fffffff) ? 0 : ((q / n) + 2) * W + (q % n) + 2;
   }
@@ -166,19 +170,22 @@ __global__ void __launch_bounds__(512)
       const int s0 = R.base + (k - R.ka);
       // field coefficients first: independent of the plane data
       const unsigned pbase = (unsigned)k * (unsigned)(n * n) + (unsigned)(y0 * n);
-      float4 ca[kPPT], cbv[kPPT];
+      float4 ca[PPT], cbv[PPT];
 #pragma unroll
-      for (int t = 0; t < kPPT; ++t)
+      for (int t = 0; t < PPT; ++t)
         if (qv[t] < tyn) {
           const float4 *c2 = A.coef + 2 * (size_t)(pbase + qv[t]);
           ca[t] = __ldg(c2);
           cbv[t] = __ldg(c2 + 1);
         }
-      while (ok && waited < s0 + 4) {
-        const int s = waited + 1;
-        if (!mbarWait(&bars[s % A.ring], (s / A.ring) & 1u, kLimit)) ok = false;
-        else waited = s;
-      }
+      // one thread polls the mbarrier (bounded); the others wait at the
+      // CTA barrier, which does not take issue slots
+      if (threadIdx.x == 0)
+        while (ok && waited < s0 + 4) {
+          const int s = waited + 1;
+          if (!mbarWait(&bars[s % A.ring], (s / A.ring) & 1u, kLimit)) ok = false;
+          else waited = s;
+        }
       ok = __syncthreads_and(ok);
       if (!ok) break;
       const float4 *pm2 = ring + (size_t)((s0) % A.ring) * slotElems;
@@ -187,7 +194,7 @@ __global__ void __launch_bounds__(512)
       const float4 *pp1 = ring + (size_t)((s0 + 3) % A.ring) * slotElems;
       const float4 *pp2 = ring + (size_t)((s0 + 4) % A.ring) * slotElems;
 #pragma unroll
-      for (int t = 0; t < kPPT; ++t)
+      for (int t = 0; t < PPT; ++t)
         if (qv[t] < tyn) {
           const int l = lr[t];
           float c[8] = {ca[t].x, ca[t].y, ca[t].z, ca[t].w,
@@ -209,11 +216,38 @@ __global__ void __launch_bounds__(512)
       }
     }
   }
-  if (!ok) {
-    if (threadIdx.x == 0) atomicExch(A.err, 1);
+  if (!ok && threadIdx.x == 0) {
+    atomicExch(A.err, 1);
     for (int s = waited + 1; s < nextSeq; ++s)
       mbarWait(&bars[s % A.ring], (s / A.ring) & 1u, kLimit);
   }
+}
+
+using StreamKernel = void (*)(const CUtensorMap, StreamArgs);
+constexpr int kWidths[] = {0, 34, 36, 40, 44, 52};
+template <int PPT> StreamKernel pickW(int W) {
+  switch (W) {
+  case 34: return stencilStream32<PPT, 34>;
+  case 36: return stencilStream32<PPT, 36>;
+  case 40: return stencilStream32<PPT, 40>;
+  case 44: return stencilStream32<PPT, 44>;
+  case 52: return stencilStream32<PPT, 52>;
+  default: return stencilStream32<PPT, 0>;
+  }
+}
+StreamKernel pickKernel(int ppt, int W) {
+  static bool attr = false;
+  if (!attr) {
+    for (int w : kWidths) {
+      cudaFuncSetAttribute(pickW<1>(w), cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+      cudaFuncSetAttribute(pickW<2>(w), cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+      cudaFuncSetAttribute(pickW<4>(w), cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    }
+    attr = true;
+  }
+  if (ppt == 1) return pickW<1>(W);
+  if (ppt == 2) return pickW<2>(W);
+  return pickW<4>(W);
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encodeFn() {
@@ -284,7 +318,8 @@ struct Shape {
 };
 
 bool validShape(int n, const Shape &s, int &threads) {
-  if (s.TY < 1 || s.TY > n || s.ring < 6 || s.ppt < 1 || s.ppt > kPPT)
+  if (s.TY < 1 || s.TY > n || s.ring < 6 ||
+      !(s.ppt == 1 || s.ppt == 2 || s.ppt == 4))
     return false;
   if (s.TY + 4 > 256 || n + 4 > 256) return false;
   const int pts = s.TY * n;
@@ -319,8 +354,8 @@ bool launchStream(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
                             ((long long)(kMaxRuns - 2) * n);
   ctas = std::max(ctas, minCtas);
   ctas = std::min<long long>(ctas, A.total);
-  stencilStream32<<<(unsigned)ctas, threads, streamSmem(n, sh.TY, sh.ring),
-                    st>>>(map, A);
+  StreamKernel kern = pickKernel(sh.ppt, n + 4);
+  kern<<<(unsigned)ctas, threads, streamSmem(n, sh.TY, sh.ring), st>>>(map, A);
   return true;
 }
 
@@ -392,13 +427,6 @@ static Shape tune(ncgm_ctx *ctx, int species, int ncols) {
 
 void applyH32(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
               int ncols, float shift, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(stencilStream32,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         220 * 1024);
-    attr = true;
-  }
   Shape *sh = nullptr;
   for (auto &t : g_tuned)
     if (t.ctx == ctx) sh = &t.s;
