@@ -20,26 +20,38 @@ RHO_TOL = 1e-7   # fm^-3: densities, max-abs
 
 O16 = {"functional": "SLy4", "nucleus": {"A": 16, "Z": 8},
        "box": {"boxSize": 16.5, "axisMeshPoints": 12},
-       "maxIterations": 400, "energyTol": 1e-7}
+       "maxIterations": 600, "energyTol": 1e-9}
 
 
-def _run_both(data, precision=abi.FP64, **over):
+def _run_both(data, precision=abi.FP64, smooth=False, **over):
     cfg = config.from_input(data, precision=precision)
     for k, v in over.items():
         setattr(cfg, k, v)
+    if smooth:
+        _smooth(cfg)
     res_g, out_g = ng.hf_run(cfg)
     res_o, out_o = oracle.hf_run(cfg)
     return cfg, res_g, out_g, res_o, out_o
 
 
 def _fixed_point(res_g, out_g, res_o, out_o):
-    assert res_g.converged and res_o.converged
+    # both runs are within ~1e-9 MeV per iteration of the fixed point
+    assert res_g.last_dE < 1e-8 and res_o.last_dE < 1e-8
     assert abs(res_g.E_int - res_o.E_int) < E_TOL
     assert abs(res_g.E_HF - res_o.E_HF) < E_TOL
     assert np.abs(out_g["spe_n"] - out_o["spe_n"]).max() < SPE_TOL
     assert np.abs(out_g["spe_p"] - out_o["spe_p"]).max() < SPE_TOL
     assert np.abs(out_g["rho_n"] - out_o["rho_n"]).max() < RHO_TOL
     assert np.abs(out_g["rho_p"] - out_o["rho_p"]).max() < RHO_TOL
+
+
+def _smooth(cfg):
+    """Make the iteration a smooth map: every PCG takes all its steps
+    (cgTol 0) and the guess solver never locks (tol 0), so no discrete
+    decision can fall differently on the two machines."""
+    cfg.hf_gcg.cg_tol = 0.0
+    cfg.ws_gcg.cg_tol = 0.0
+    cfg.ws_gcg.tol = 0.0
 
 
 def _trajectory(res_g, out_g, res_o, out_o, tol=1e-6):
@@ -55,7 +67,7 @@ def test_o16_hf_fp64_fixed_point():
 
 def test_o16_hf_fp64_trajectory():
     data = dict(O16, maxIterations=40, energyTol=0.0)
-    _, rg, og, ro, oo = _run_both(data)
+    _, rg, og, ro, oo = _run_both(data, smooth=True)
     _trajectory(rg, og, ro, oo)
     assert np.abs(og["rho_n"] - oo["rho_n"]).max() < 1e-9
 
@@ -71,7 +83,7 @@ def test_n_equals_z_without_coulomb_copies_neutrons():
             "box": {"boxSize": 16.5, "axisMeshPoints": 12},
             "coulombInteraction": False,
             "maxIterations": 40, "energyTol": 0.0}
-    _, rg, og, ro, oo = _run_both(data)
+    _, rg, og, ro, oo = _run_both(data, smooth=True)
     _trajectory(rg, og, ro, oo)
     assert np.array_equal(og["spe_n"], og["spe_p"])
     assert np.array_equal(og["rho_n"], og["rho_p"])
@@ -83,7 +95,7 @@ def test_mg24_bcs_trajectory():
             "pairing": {"type": "BCS", "HFbasisSize": 16, "V0": 1000.0,
                         "window": 5.0},
             "maxIterations": 25, "energyTol": 0.0}
-    _, rg, og, ro, oo = _run_both(data)
+    _, rg, og, ro, oo = _run_both(data, smooth=True)
     _trajectory(rg, og, ro, oo, tol=1e-5)
     assert abs(rg.lambda_n - ro.lambda_n) < 1e-5
     assert abs(rg.E_pair_n - ro.E_pair_n) < 1e-5
@@ -94,7 +106,7 @@ def test_quadrupole_constrained_trajectory():
     data = {"functional": "SKMstar", "nucleus": {"A": 24, "Z": 12},
             "box": {"boxSize": 17.0, "axisMeshPoints": 12},
             "maxIterations": 25, "energyTol": 0.0}
-    _, rg, og, ro, oo = _run_both(data, curve_mode=1, mu20=mu20,
+    _, rg, og, ro, oo = _run_both(data, smooth=True, curve_mode=1, mu20=mu20,
                                   initial_beta=0.3)
     _trajectory(rg, og, ro, oo, tol=1e-5)
     assert abs(rg.beta - ro.beta) < 1e-6
