@@ -90,24 +90,53 @@ struct Run {
   int cb, ka, kb, base;
 };
 
-// PPT: points owned per thread (register budget); WFIX: padded row width
-// n + 4 fixed at compile time for the common lattices (0: runtime), which
-// turns the +-W, +-2W neighbour offsets into immediates.
+__device__ __forceinline__ void mbarArrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smemAddr(bar))
+               : "memory");
+}
+// bounded wait that lets the warp sleep between polls (suspend-time hint)
+__device__ __forceinline__ bool mbarWaitSleep(uint64_t *bar, uint32_t phase,
+                                              uint32_t limit) {
+  for (uint32_t it = 0; it < limit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n"
+        " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smemAddr(bar)), "r"(phase), "r"(1000u)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// Warp-specialised form. Warp 0 is the producer: one lane issues the TMA
+// loads of the CTA's plane sequence, waiting on the slot's `empty` barrier
+// before reusing it. Warps 1..C are consumers: each waits on the `full`
+// barrier of the planes it needs, computes its points and releases the
+// planes it no longer needs with one arrive per warp. No CTA-wide barrier
+// in the loop. PPT: points per consumer thread; WFIX: padded row width
+// n + 4 fixed at compile time (0: runtime), making +-W offsets immediates.
 template <int PPT, int WFIX>
-__global__ void __launch_bounds__(512, PPT == 1 ? 2 : 1)
+__global__ void __launch_bounds__(512, 1)
     stencilStream32(const __grid_constant__ CUtensorMap map, StreamArgs A) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ Run runs[kMaxRuns];
-  __shared__ int nruns, totalSeq;
+  __shared__ int nruns, totalSeq, failed;
   const int n = A.n, W = WFIX ? WFIX : n + 4;
   const int boxElems = (A.TY + 4) * W;
   const int slotElems = (boxElems + 7) & ~7; // 128-byte aligned slots
   const uint32_t boxBytes = boxElems * 16u;
+  const int nCons = blockDim.x / 32 - 1;      // consumer warps
   float4 *ring = reinterpret_cast<float4 *>(smem_raw);
-  uint64_t *bars = reinterpret_cast<uint64_t *>(
+  uint64_t *full = reinterpret_cast<uint64_t *>(
       smem_raw + (size_t)A.ring * slotElems * 16u);
+  uint64_t *empty = full + A.ring;
   const long long t0 = (long long)blockIdx.x * A.total / gridDim.x;
   const long long t1 = (long long)(blockIdx.x + 1) * A.total / gridDim.x;
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const uint32_t kLimit = 1u << 20; // x ~1 us suspend hint: bounded (~1 s)
 
   if (threadIdx.x == 0) {
     int r = 0, seq = 0;
@@ -122,45 +151,67 @@ __global__ void __launch_bounds__(512, PPT == 1 ? 2 : 1)
     }
     nruns = r;
     totalSeq = seq;
-    for (int s = 0; s < A.ring; ++s) mbarInit(&bars[s], 1);
+    failed = 0;
+    for (int s = 0; s < A.ring; ++s) {
+      mbarInit(&full[s], 1);
+      mbarInit(&empty[s], nCons);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
   const int NR = nruns, TS = totalSeq;
 
-  // owned points of a band: q = tid + t * blockDim, lr its padded slot index
+  if (warp == 0) {
+    // ---- producer ----
+    if (lane == 0) {
+      int pr = 0, pz = (NR > 0) ? runs[0].ka - 2 : 0;
+      int issued = 0;
+      bool ok = true;
+      for (int s = 0; s < TS; ++s) {
+        const int slot = s % A.ring;
+        if (s >= A.ring) {
+          // slot reuse: every consumer warp released seq s - ring
+          if (!mbarWaitSleep(&empty[slot], ((s / A.ring) - 1) & 1u, kLimit) ||
+              *(volatile int *)&failed) {
+            ok = false;
+            break;
+          }
+        }
+        const Run &R = runs[pr];
+        const int col = R.cb / A.nbands, band = R.cb % A.nbands;
+        mbarExpectTx(&full[slot], boxBytes);
+        tmaTile5(ring + (size_t)slot * slotElems, &map, -2, band * A.TY - 2,
+                 pz, col, &full[slot]);
+        issued = s + 1;
+        if (++pz >= R.kb + 2 && pr + 1 < NR) {
+          ++pr;
+          pz = runs[pr].ka - 2;
+        }
+      }
+      if (!ok) {
+        atomicExch(A.err, 1);
+        *(volatile int *)&failed = 1;
+        // drain: wait (bounded) for every copy this CTA issued
+        for (int s = (issued > A.ring ? issued - A.ring : 0); s < issued; ++s)
+          mbarWaitSleep(&full[s % A.ring], (s / A.ring) & 1u, kLimit);
+      }
+    }
+    return;
+  }
+
+  // ---- consumers ----
+  const int ct = threadIdx.x - 32; // consumer thread index
+  const int nct = nCons * 32;
   int qv[PPT], lr[PPT];
 #pragma unroll
   for (int t = 0; t < PPT; ++t) {
-    int q = threadIdx.x + t * blockDim.x;
+    int q = ct + t * nct;
     if (q >= A.TY * n) q = 0x7fffffff;
     qv[t] = q;
     lr[t] = (q == 0x7fffffff) ? 0 : ((q / n) + 2) * W + (q % n) + 2;
   }
-
-  // producer state (thread 0): run cursor and next z in that run
-  int pr = 0, pz = (NR > 0) ? runs[0].ka - 2 : 0, nextSeq = 0;
-  auto issue = [&]() {
-    const Run &R = runs[pr];
-    const int s = nextSeq;
-    const int slot = s % A.ring;
-    const int col = R.cb / A.nbands, band = R.cb % A.nbands;
-    mbarExpectTx(&bars[slot], boxBytes);
-    tmaTile5(ring + (size_t)slot * slotElems, &map, -2, band * A.TY - 2, pz,
-             col, &bars[slot]);
-    ++nextSeq;
-    if (++pz >= R.kb + 2 && pr + 1 < NR) {
-      ++pr;
-      pz = runs[pr].ka - 2;
-    }
-  };
-  if (threadIdx.x == 0)
-    while (nextSeq < TS && nextSeq < A.ring) issue();
-
-  const uint32_t kLimit = 1u << 22;
-  bool ok = true;
   int waited = -1;
-  for (int r = 0; r < NR && ok; ++r) {
+  for (int r = 0; r < NR; ++r) {
     const Run R = runs[r];
     const int col = R.cb / A.nbands, band = R.cb % A.nbands;
     const int y0 = band * A.TY;
@@ -168,7 +219,6 @@ __global__ void __launch_bounds__(512, PPT == 1 ? 2 : 1)
     float4 *Yc = A.Y + (size_t)col * A.ns;
     for (int k = R.ka; k < R.kb; ++k) {
       const int s0 = R.base + (k - R.ka);
-      // field coefficients first: independent of the plane data
       const unsigned pbase = (unsigned)k * (unsigned)(n * n) + (unsigned)(y0 * n);
       float4 ca[PPT], cbv[PPT];
 #pragma unroll
@@ -178,16 +228,22 @@ __global__ void __launch_bounds__(512, PPT == 1 ? 2 : 1)
           ca[t] = __ldg(c2);
           cbv[t] = __ldg(c2 + 1);
         }
-      // one thread polls the mbarrier (bounded); the others wait at the
-      // CTA barrier, which does not take issue slots
-      if (threadIdx.x == 0)
-        while (ok && waited < s0 + 4) {
-          const int s = waited + 1;
-          if (!mbarWait(&bars[s % A.ring], (s / A.ring) & 1u, kLimit)) ok = false;
-          else waited = s;
+      bool ok = true;
+      while (waited < s0 + 4) {
+        const int s = waited + 1;
+        if (!mbarWaitSleep(&full[s % A.ring], (s / A.ring) & 1u, kLimit)) {
+          ok = false;
+          break;
         }
-      ok = __syncthreads_and(ok);
-      if (!ok) break;
+        waited = s;
+      }
+      if (!ok || *(volatile int *)&failed) {
+        if (lane == 0) {
+          atomicExch(A.err, 1);
+          *(volatile int *)&failed = 1;
+        }
+        return;
+      }
       const float4 *pm2 = ring + (size_t)((s0) % A.ring) * slotElems;
       const float4 *pm1 = ring + (size_t)((s0 + 1) % A.ring) * slotElems;
       const float4 *pc = ring + (size_t)((s0 + 2) % A.ring) * slotElems;
@@ -206,20 +262,14 @@ __global__ void __launch_bounds__(512, PPT == 1 ? 2 : 1)
               S(pc[l - 2 * W]), S(pp1[l]), S(pm1[l]), S(pp2[l]), S(pm2[l]));
           Yc[pbase + qv[t]] = make_float4(o.r0, o.i0, o.r1, o.i1);
         }
-      __syncthreads(); // every seq below the next plane's first is free now
-      if (threadIdx.x == 0) {
-        // lowest sequence still needed: the next plane of this run, or the
-        // first plane of the next run (the tail halo of this run is done)
-        const int low = (k + 1 < R.kb) ? s0 + 1
-                                        : (r + 1 < NR ? runs[r + 1].base : TS);
-        while (nextSeq < TS && nextSeq < low + A.ring) issue();
+      // release the planes this warp no longer needs: seq s0, or all five at
+      // the end of the run
+      __syncwarp();
+      if (lane == 0) {
+        const int last = (k + 1 < R.kb) ? s0 : s0 + 4;
+        for (int s = s0; s <= last; ++s) mbarArrive(&empty[s % A.ring]);
       }
     }
-  }
-  if (!ok && threadIdx.x == 0) {
-    atomicExch(A.err, 1);
-    for (int s = waited + 1; s < nextSeq; ++s)
-      mbarWait(&bars[s % A.ring], (s / A.ring) & 1u, kLimit);
   }
 }
 
@@ -299,7 +349,7 @@ bool tensorMapFor(const void *X, int n, int ncols, int TY, CUtensorMap *out) {
 
 size_t streamSmem(int n, int TY, int ring) {
   size_t slot = (((size_t)(TY + 4) * (n + 4) + 7) & ~size_t(7)) * 16;
-  return (size_t)ring * slot + (size_t)ring * 8;
+  return (size_t)ring * slot + (size_t)ring * 16; // slots + full/empty bars
 }
 
 int smCount() {
@@ -323,8 +373,9 @@ bool validShape(int n, const Shape &s, int &threads) {
     return false;
   if (s.TY + 4 > 256 || n + 4 > 256) return false;
   const int pts = s.TY * n;
-  threads = ((pts + s.ppt - 1) / s.ppt + 31) / 32 * 32;
-  if (threads > 512 || threads < 32) return false;
+  // one producer warp + consumer warps covering the band
+  threads = 32 + ((pts + s.ppt - 1) / s.ppt + 31) / 32 * 32;
+  if (threads > 512 || threads < 64) return false;
   if (streamSmem(n, s.TY, s.ring) * s.ctasPerSM > 220 * 1024) return false;
   return true;
 }
