@@ -166,6 +166,26 @@ int ncgm_poisson(ncgm_ctx *ctx, const double *rhoP, int Z,
                  const double *U_guess, double *U_out, double *UC_out,
                  int *iterations);
 
+/* Allocation-free form of ncgm_poisson, for callers that cannot allocate
+ * device memory: hosts that hand the whole GPU to their own memory pool up
+ * front, and loops that must not stall on cudaMalloc/cudaFree, which
+ * synchronise the device. It has no counterpart in the reference. It needs
+ * no context and allocates nothing: rhoP, U_guess (may be NULL for a cold
+ * start), U_out and UC_out (may be NULL) must be device buffers of n^3
+ * doubles, a is the box half-width and stream a cudaStream_t (NULL: the
+ * default stream). The solver's scratch (4 n^3 + 560 doubles) is a static
+ * device array sized for n <= NCGM_POISSON_NOALLOC_MAX_N (about 3.5 MB, held
+ * by every GPU that loads the library until the process exits); larger n is
+ * rejected with NCGM_ERR_ARG. The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture. All calls on a device share
+ * the array: calls that overlap on the GPU race. Nothing in the scratch needs
+ * to start at zero (every word is written before it is read). */
+#define NCGM_POISSON_NOALLOC_MAX_N 48
+int ncgm_poisson_noalloc(int n, double a, const double *rhoP, int Z,
+                         const double *U_guess, double *U_out, double *UC_out,
+                         void *stream, int *iterations);
+
 /* ---- self-consistent iteration ----------------------------------------- */
 
 /* Run configuration: the fields of InputParser (src/system/input_parser.cpp:

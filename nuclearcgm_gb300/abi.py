@@ -102,6 +102,7 @@ SIGNATURES = {
                      _vp, _vp], _i),
     "ncgm_densities": ([_vp, _vp, _i, _vp, _vp, _vp, _vp], _i),
     "ncgm_poisson": ([_vp, _vp, _i, _vp, _vp, _vp, _vp], _i),
+    "ncgm_poisson_noalloc": ([_i, _d, _vp, _i, _vp, _vp, _vp, _vp, _vp], _i),
 }
 
 

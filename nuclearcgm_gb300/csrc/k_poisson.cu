@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <string>
 #include <vector>
 
 namespace ncgm {
@@ -335,4 +336,177 @@ size_t poissonWorkDoubles(int n) {
   return 16 + 4 * 120 + 4 * ns + 64;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free variant. Its scratch (right-hand side, CG vectors and
+// reduction partials) lives in this file-scope device array, sized for
+// lattices up to NCGM_POISSON_NOALLOC_MAX_N points per axis; every GPU that
+// loads the library holds it until the process exits. Host code never uses
+// the symbol's host-side name as a device address: the address is looked up
+// once per device with cudaGetSymbolAddress and handed to the kernels.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoAllocMaxN = NCGM_POISSON_NOALLOC_MAX_N;
+constexpr size_t kNoAllocDoubles =
+    16 + 4 * 120 + 4 * kNoAllocMaxN * kNoAllocMaxN * kNoAllocMaxN + 64;
+static __device__ __align__(256) double g_poissonScratch[kNoAllocDoubles];
+
+constexpr int kMaxDevices = 64;
+double *g_scratchAddr[kMaxDevices] = {nullptr};
+
+// device address of the static scratch on the current device (set-up on the
+// first call per device)
+int staticScratch(double **out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return NCGM_ERR_CUDA;
+  if (dev < 0 || dev >= kMaxDevices) return NCGM_ERR_ARG;
+  if (!g_scratchAddr[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_poissonScratch);
+    if (e != cudaSuccess || !p) return NCGM_ERR_CUDA;
+    g_scratchAddr[dev] = static_cast<double *>(p);
+  }
+  *out = g_scratchAddr[dev];
+  return NCGM_OK;
+}
+
+// Same sequence of kernels as poissonSolve, with the host-side reduction
+// buffers on the stack instead of the heap.
+int poissonSolveNoAlloc(const PoissonArgs &P, cudaStream_t s,
+                        int *iterations) {
+  const int n = P.n;
+  const size_t ns = (size_t)n * n * n;
+  constexpr int nblk = 120;
+  double *q = P.work;
+  double *sc = P.work + 8;
+  double *part = P.work + 16;
+  double *part2 = part + 2 * nblk;
+  double *rhs = P.work + 16 + 4 * nblk;
+  double *r = rhs + ns, *p = r + ns, *Ap = p + ns;
+  quadKernel<<<nblk, 256, 0, s>>>(P.rhoP, n, P.a, P.h, part);
+  double hp[2 * nblk];
+  if (cudaMemcpyAsync(hp, part, sizeof(hp), cudaMemcpyDeviceToHost, s) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return NCGM_ERR_CUDA;
+  double qq[2] = {0, 0};
+  for (int b = 0; b < nblk; ++b) {
+    qq[0] += hp[b];
+    qq[1] += hp[nblk + b];
+  }
+  if (cudaMemcpyAsync(q, qq, sizeof(qq), cudaMemcpyHostToDevice, s) !=
+      cudaSuccess)
+    return NCGM_ERR_CUDA;
+  rhsKernel<<<(unsigned)((ns + 255) / 256), 256, 0, s>>>(P.rhoP, n, P.a, P.h,
+                                                          P.Z, q, rhs);
+  negLapKernel<<<nblk, 256, 0, s>>>(P.U, Ap, n, P.h, nullptr);
+  cgInitKernel<<<nblk, 256, 0, s>>>(rhs, Ap, r, p, ns, part);
+  cgScalarInit<<<1, 32, 0, s>>>(part, nblk, sc);
+  const double tol2 = P.tol * P.tol;
+  int it = 0;
+  const int maxit = std::max(100, (int)std::min<size_t>(4 * ns, 20000));
+  double hs[8];
+  double best = 1e300;
+  int sinceBest = 0;
+  for (; it < maxit;) {
+    for (int b = 0; b < 16; ++b, ++it) {
+      negLapKernel<<<nblk, 256, 0, s>>>(p, Ap, n, P.h, part2);
+      cgUpdateKernel<<<nblk, 256, 0, s>>>(P.U, r, p, Ap, ns, part2, nblk, sc,
+                                          part);
+      cgDirKernel<<<nblk, 256, 0, s>>>(p, r, ns, part, nblk, sc, tol2);
+      cgCommit<<<1, 32, 0, s>>>(sc);
+    }
+    if (cudaMemcpyAsync(hs, sc, sizeof(hs), cudaMemcpyDeviceToHost, s) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      return NCGM_ERR_CUDA;
+    if (!std::isfinite(hs[0])) return NCGM_ERR_NAN;
+    if (hs[3] != 0.0) break;
+    if (hs[0] < 0.5 * best) {
+      best = hs[0];
+      sinceBest = 0;
+    } else if (++sinceBest > 8) {
+      break;
+    }
+  }
+  if (P.UC)
+    exchangeKernel<<<(unsigned)((ns + 255) / 256), 256, 0, s>>>(P.rhoP, P.U,
+                                                                 P.UC, ns);
+  if (iterations) *iterations = it;
+  return cudaGetLastError() == cudaSuccess ? NCGM_OK : NCGM_ERR_CUDA;
+}
+
+bool onDevice(const void *p) {
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+}
+
+} // namespace
+
+void setError(const std::string &msg);
+
 } // namespace ncgm
+
+// Allocation-free Coulomb Poisson solve (see ncgm.h). For callers that cannot
+// allocate device memory; the scratch is the static array above, shared by
+// every call on a device, so calls that overlap on the GPU race.
+extern "C" int ncgm_poisson_noalloc(int n, double a, const double *rhoP,
+                                    int Z, const double *U_guess,
+                                    double *U_out, double *UC_out,
+                                    void *stream, int *iterations) {
+  using namespace ncgm;
+  if (n < 2 || !(a > 0) || !rhoP || !U_out) {
+    setError("ncgm_poisson_noalloc: need n >= 2, a > 0, rhoP and U_out");
+    return NCGM_ERR_ARG;
+  }
+  if ((size_t)n > kNoAllocMaxN) {
+    setError("ncgm_poisson_noalloc: n = " + std::to_string(n) +
+             " exceeds the static scratch limit of " +
+             std::to_string(kNoAllocMaxN) + " points per axis");
+    return NCGM_ERR_ARG;
+  }
+  if (!onDevice(rhoP) || !onDevice(U_out) || (UC_out && !onDevice(UC_out)) ||
+      (U_guess && !onDevice(U_guess))) {
+    setError("ncgm_poisson_noalloc: all buffers must be device memory");
+    return NCGM_ERR_ARG;
+  }
+  double *scratch = nullptr;
+  int st = staticScratch(&scratch);
+  if (st != NCGM_OK) {
+    setError("ncgm_poisson_noalloc: static scratch address lookup failed");
+    return st;
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t ns = (size_t)n * n * n;
+  // the solver iterates in place on U_out: start from the guess or from zero
+  if (U_guess && U_guess != U_out) {
+    if (cudaMemcpyAsync(U_out, U_guess, ns * sizeof(double),
+                        cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+      return NCGM_ERR_CUDA;
+  } else if (!U_guess) {
+    if (cudaMemsetAsync(U_out, 0, ns * sizeof(double), s) != cudaSuccess)
+      return NCGM_ERR_CUDA;
+  }
+  PoissonArgs P;
+  P.n = n;
+  P.a = a;
+  P.h = 2.0 * a / (n - 1);
+  P.Z = Z;
+  P.rhoP = rhoP;
+  P.U = U_out;
+  P.UC = UC_out;
+  P.warm = 1;
+  P.tol = 1e-13;
+  P.work = scratch;
+  st = poissonSolveNoAlloc(P, s, iterations);
+  if (st != NCGM_OK) {
+    setError("ncgm_poisson_noalloc: solve failed");
+    return st;
+  }
+  if (cudaStreamSynchronize(s) != cudaSuccess) return NCGM_ERR_CUDA;
+  return NCGM_OK;
+}
