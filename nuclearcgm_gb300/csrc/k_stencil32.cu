@@ -24,6 +24,8 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 namespace ncgm {
@@ -129,6 +131,7 @@ __global__ void __launch_bounds__(512, 1)
   const int slotElems = (boxElems + 7) & ~7; // 128-byte aligned slots
   const uint32_t boxBytes = boxElems * 16u;
   const int nCons = blockDim.x / 32 - 1;      // consumer warps
+  const int rmask = A.ring - 1, rlog = __ffs(A.ring) - 1; // ring = 2^rlog
   float4 *ring = reinterpret_cast<float4 *>(smem_raw);
   uint64_t *full = reinterpret_cast<uint64_t *>(
       smem_raw + (size_t)A.ring * slotElems * 16u);
@@ -168,10 +171,10 @@ __global__ void __launch_bounds__(512, 1)
       int issued = 0;
       bool ok = true;
       for (int s = 0; s < TS; ++s) {
-        const int slot = s % A.ring;
+        const int slot = s & rmask;
         if (s >= A.ring) {
           // slot reuse: every consumer warp released seq s - ring
-          if (!mbarWaitSleep(&empty[slot], ((s / A.ring) - 1) & 1u, kLimit) ||
+          if (!mbarWaitSleep(&empty[slot], ((s >> rlog) - 1) & 1u, kLimit) ||
               *(volatile int *)&failed) {
             ok = false;
             break;
@@ -193,7 +196,7 @@ __global__ void __launch_bounds__(512, 1)
         *(volatile int *)&failed = 1;
         // drain: wait (bounded) for every copy this CTA issued
         for (int s = (issued > A.ring ? issued - A.ring : 0); s < issued; ++s)
-          mbarWaitSleep(&full[s % A.ring], (s / A.ring) & 1u, kLimit);
+          mbarWaitSleep(&full[s & rmask], (s >> rlog) & 1u, kLimit);
       }
     }
     return;
@@ -231,7 +234,7 @@ __global__ void __launch_bounds__(512, 1)
       bool ok = true;
       while (waited < s0 + 4) {
         const int s = waited + 1;
-        if (!mbarWaitSleep(&full[s % A.ring], (s / A.ring) & 1u, kLimit)) {
+        if (!mbarWaitSleep(&full[s & rmask], (s >> rlog) & 1u, kLimit)) {
           ok = false;
           break;
         }
@@ -244,11 +247,11 @@ __global__ void __launch_bounds__(512, 1)
         }
         return;
       }
-      const float4 *pm2 = ring + (size_t)((s0) % A.ring) * slotElems;
-      const float4 *pm1 = ring + (size_t)((s0 + 1) % A.ring) * slotElems;
-      const float4 *pc = ring + (size_t)((s0 + 2) % A.ring) * slotElems;
-      const float4 *pp1 = ring + (size_t)((s0 + 3) % A.ring) * slotElems;
-      const float4 *pp2 = ring + (size_t)((s0 + 4) % A.ring) * slotElems;
+      const float4 *pm2 = ring + ((s0) & rmask) * slotElems;
+      const float4 *pm1 = ring + ((s0 + 1) & rmask) * slotElems;
+      const float4 *pc = ring + ((s0 + 2) & rmask) * slotElems;
+      const float4 *pp1 = ring + ((s0 + 3) & rmask) * slotElems;
+      const float4 *pp2 = ring + ((s0 + 4) & rmask) * slotElems;
 #pragma unroll
       for (int t = 0; t < PPT; ++t)
         if (qv[t] < tyn) {
@@ -267,7 +270,7 @@ __global__ void __launch_bounds__(512, 1)
       __syncwarp();
       if (lane == 0) {
         const int last = (k + 1 < R.kb) ? s0 : s0 + 4;
-        for (int s = s0; s <= last; ++s) mbarArrive(&empty[s % A.ring]);
+        for (int s = s0; s <= last; ++s) mbarArrive(&empty[s & rmask]);
       }
     }
   }
@@ -368,7 +371,7 @@ struct Shape {
 };
 
 bool validShape(int n, const Shape &s, int &threads) {
-  if (s.TY < 1 || s.TY > n || s.ring < 6 ||
+  if (s.TY < 1 || s.TY > n || s.ring < 8 || (s.ring & (s.ring - 1)) ||
       !(s.ppt == 1 || s.ppt == 2 || s.ppt == 4))
     return false;
   if (s.TY + 4 > 256 || n + 4 > 256) return false;
@@ -417,7 +420,7 @@ struct TunedShape {
 std::vector<TunedShape> g_tuned;
 
 Shape defaultShape(int n) {
-  Shape s{n, 8, 4, 1};
+  Shape s{n, 8, 4, 1};  // ring: a power of two
   int th;
   while (!validShape(n, s, th) && s.TY > 1) {
     if (s.TY * n > 512 * s.ppt && s.ppt < kPPT) {
@@ -449,10 +452,13 @@ static Shape tune(ncgm_ctx *ctx, int species, int ncols) {
     if (r <= 4) break;
   }
   float bestMs = 1e30f;
+  // NCGM_TUNE_LOG=1 prints every candidate's time to stderr
+  const char *lg = std::getenv("NCGM_TUNE_LOG");
+  const bool log = lg && lg[0] == '1';
   for (int TY : rows)
-    for (int ring : {6, 8, 10, 12})
+    for (int ring : {8, 16})
       for (int ppt : {1, 2, 4})
-        for (int cps : {1, 2}) {
+        for (int cps : {1, 2, 4}) {
           Shape s{TY, ring, ppt, cps};
           int th;
           if (!validShape(n, s, th)) continue;
@@ -468,6 +474,11 @@ static Shape tune(ncgm_ctx *ctx, int species, int ncols) {
           }
           float ms = 0;
           cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+          if (log)
+            std::fprintf(stderr,
+                         "[ncgm tune] n=%d cols=%d rows=%d ring=%d ppt=%d "
+                         "ctas/SM=%d: %.1f us\n",
+                         n, ncols, TY, ring, ppt, cps, 1e3f * ms / 3);
           if (ms < bestMs) {
             bestMs = ms;
             best = s;
