@@ -494,7 +494,16 @@ void applyH32(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
     if (t.ctx == ctx) sh = &t.s;
   if (!sh) {
     g_tuned.push_back({ctx, defaultShape(ctx->n)});
-    Shape tuned = tune(ctx, species, ncols);
+    // NCGM_STENCIL_SHAPE="rows,ring,ppt,ctasPerSM" fixes the shape (no tuning)
+    Shape tuned{}, fixed{};
+    int th = 0;
+    const char *env = std::getenv("NCGM_STENCIL_SHAPE");
+    if (env && std::sscanf(env, "%d,%d,%d,%d", &fixed.TY, &fixed.ring,
+                           &fixed.ppt, &fixed.ctasPerSM) == 4 &&
+        validShape(ctx->n, fixed, th))
+      tuned = fixed;
+    else
+      tuned = tune(ctx, species, ncols);
     for (auto &t : g_tuned)
       if (t.ctx == ctx) {
         t.s = tuned;
