@@ -42,6 +42,10 @@ extern "C" {
 #define NCGM_ORDER_ASCENDING 1      /* EigenpairsOrdering::ASCENDING_ENERGIES */
 
 typedef struct ncgm_ctx ncgm_ctx;
+typedef struct ncgm_lp ncgm_lp; /* learned preconditioner (network + data) */
+
+#define NCGM_PRECOND_JACOBI 0  /* reference: Jacobi PCG from d = 0 */
+#define NCGM_PRECOND_LEARNED 1 /* Jacobi PCG from the network's d0 */
 
 /* Skyrme EDF coupling constants, in the order of FunctionalParameters
  * (include/EDF.hpp:20-23). */
@@ -67,7 +71,7 @@ typedef struct ncgm_gcg_params {
   double shift;    /* initial shift (reference passes 0) */
   int ordering;    /* NCGM_ORDER_* */
   int precision;   /* precision of the PCG correction applies: NCGM_FP64/FP32 */
-  int precond;     /* 0: Jacobi (reference); 1: learned correction, Jacobi judge */
+  int precond;     /* NCGM_PRECOND_*: 1 needs a network (ncgm_set_lp) */
 } ncgm_gcg_params;
 
 typedef struct ncgm_gcg_stats {
@@ -79,6 +83,7 @@ typedef struct ncgm_gcg_stats {
   double max_residual;  /* max residual norm of the returned pairs */
   double ms_total;      /* device wall time of the call */
   double ms_pcg;        /* part spent in the PCG correction */
+  int lp_columns;       /* PCG columns started from the learned correction */
 } ncgm_gcg_stats;
 
 /* ---- context: grid and device state ------------------------------------ */
@@ -228,6 +233,9 @@ typedef struct ncgm_hf_config {
   double constraints_tol;
   /* stop rule extensions (0 = reference rule only) */
   double spe_tol;      /* also require max |dSPE| < spe_tol when > 0 */
+  /* learned preconditioner (no reference counterpart; NULL / 0 = off) */
+  ncgm_lp *lp;          /* network used when hf_gcg.precond = LEARNED */
+  int lp_collect_every; /* > 0: log training pairs every k-th HF iteration */
 } ncgm_hf_config;
 
 typedef struct ncgm_hf_result {
@@ -248,6 +256,47 @@ typedef struct ncgm_hf_result {
  * rho_n/rho_p (n^3), energies (max_iterations x 2: E_int, E_HF per iter). */
 int ncgm_hf_run(const ncgm_hf_config *cfg, ncgm_hf_result *res, double *spe_n,
                 double *spe_p, double *rho_n, double *rho_p, double *energies);
+
+/* ---- learned preconditioner (no reference counterpart) ----------------
+ * The reference's GCG correction is Jacobi PCG from d = 0 on
+ * (A + shift) d = x lambda - A x (src/solver/solver.cpp:723-745). With
+ * precond = NCGM_PRECOND_LEARNED the PCG starts from d0 = N(r), a 3-D
+ * convolutional network (4-level U-Net, 47,489 BF16 weights, FP32
+ * accumulation) of the residual component and the local fields, scaled by
+ * the step that minimises the CG energy along it (a column where that step
+ * is not positive starts from 0 as before); the Jacobi PCG then runs to the
+ * usual tolerance and the GCG locks on the FP64 residual. The
+ * network is trained on the device on pairs (r, exact d) that the solver
+ * itself produces. */
+int ncgm_lp_num_params(void);
+int ncgm_lp_create(ncgm_lp **lp, unsigned long long seed); /* He-normal init */
+int ncgm_lp_destroy(ncgm_lp *lp);
+/* FP32 master weights, ncgm_lp_num_params() floats (host or device) */
+int ncgm_lp_get_params(ncgm_lp *lp, float *theta);
+int ncgm_lp_set_params(ncgm_lp *lp, const float *theta);
+/* y [batch][n^3] = N(x [batch][3][n^3]) (host or device buffers) */
+int ncgm_lp_forward(ncgm_lp *lp, int n, int batch, const float *x, float *y);
+/* loss (mean relative squared error against t [batch][n^3]) and its
+ * gradient with respect to the FP32 master weights */
+int ncgm_lp_gradient(ncgm_lp *lp, int n, int batch, const float *x,
+                     const float *t, float *loss, float *grad);
+/* Adds 4 training pairs per column: r = X lambda - H X (X: N x ncols, host
+ * or device; lambda: host) and the exact correction d of (H + shift) d = r
+ * from FP64 Jacobi PCG (cg_steps, relative cg_tol) on ctx's fields. Columns
+ * whose solve does not reach cg_tol (H + shift indefinite) are skipped;
+ * ncgm_lp_dataset_size reports what was kept. */
+int ncgm_lp_collect(ncgm_lp *lp, ncgm_ctx *ctx, int species, const double *X,
+                    int ncols, const double *lambda, double shift,
+                    int cg_steps, double cg_tol);
+int ncgm_lp_dataset_size(ncgm_lp *lp, int n);
+/* Adam on random minibatches of the collected pairs; loss_curve (host,
+ * steps floats, may be NULL) receives the minibatch losses. */
+int ncgm_lp_train(ncgm_lp *lp, int steps, int batch, double lr,
+                  unsigned long long seed, float *loss_curve);
+/* mean per-pair loss over the pairs of lattice n */
+int ncgm_lp_eval(ncgm_lp *lp, int n, double *mean_loss);
+/* network used by ncgm_gcg with precond = NCGM_PRECOND_LEARNED */
+int ncgm_set_lp(ncgm_ctx *ctx, ncgm_lp *lp);
 
 #ifdef __cplusplus
 }

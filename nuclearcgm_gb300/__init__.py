@@ -223,3 +223,88 @@ def hf_run(cfg: abi.HFConfig):
                               rho_p.ctypes.data, en.ctypes.data))
     return res, {"spe_n": spe_n, "spe_p": spe_p, "rho_n": rho_n,
                  "rho_p": rho_p, "energies": en[:res.iterations]}
+
+
+class LearnedPreconditioner:
+    """The GCG correction network (ncgm_lp_*): a 4-level 3-D convolutional
+    U-Net with BF16 weights that maps one real component of a GCG residual,
+    with the local fields, to a start d0 for the correction PCG. Trained on
+    the device on residual / exact-correction pairs that the solver itself
+    produces. The reference has no counterpart (its PCG starts from 0)."""
+
+    def __init__(self, seed: int = 1):
+        h = C.c_void_p()
+        _check(load().ncgm_lp_create(C.byref(h), int(seed)))
+        self.h = h
+        self.P = load().ncgm_lp_num_params()
+
+    def close(self):
+        if self.h:
+            load().ncgm_lp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def params(self):
+        th = np.zeros(self.P, np.float32)
+        _check(load().ncgm_lp_get_params(self.h, th.ctypes.data))
+        return th
+
+    @params.setter
+    def params(self, th):
+        th = np.ascontiguousarray(th, np.float32)
+        _check(load().ncgm_lp_set_params(self.h, th.ctypes.data))
+
+    def forward(self, x):
+        """x [B, 3, n, n, n] float32 -> y [B, 1, n, n, n]."""
+        x = np.ascontiguousarray(x, np.float32)
+        B, n = x.shape[0], x.shape[-1]
+        y = np.zeros((B, 1, n, n, n), np.float32)
+        _check(load().ncgm_lp_forward(self.h, n, B, x.ctypes.data,
+                                      y.ctypes.data))
+        return y
+
+    def gradient(self, x, t):
+        """(loss, dloss/dtheta) for inputs x [B, 3, n^3] and targets t."""
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        B, n = x.shape[0], x.shape[-1]
+        g = np.zeros(self.P, np.float32)
+        loss = C.c_float()
+        _check(load().ncgm_lp_gradient(self.h, n, B, x.ctypes.data,
+                                       t.ctypes.data, C.byref(loss),
+                                       g.ctypes.data))
+        return float(loss.value), g
+
+    def collect(self, H: "Hamiltonian", X, lam, shift, cg_steps=2000,
+                cg_tol=1e-10):
+        """Adds 4 ncols pairs (r = X lam - H X, exact d of (H + shift) d = r)."""
+        X = np.asfortranarray(X, np.complex128)
+        lam = np.ascontiguousarray(lam, np.float64)
+        _check(load().ncgm_lp_collect(self.h, H.ctx.h, H.species,
+                                      X.ctypes.data, X.shape[1],
+                                      lam.ctypes.data, float(shift),
+                                      int(cg_steps), float(cg_tol)))
+
+    def dataset_size(self, n):
+        return load().ncgm_lp_dataset_size(self.h, int(n))
+
+    def train(self, steps, batch=16, lr=1e-3, seed=1):
+        curve = np.zeros(steps, np.float32)
+        _check(load().ncgm_lp_train(self.h, int(steps), int(batch), float(lr),
+                                    int(seed), curve.ctypes.data))
+        return curve
+
+    def eval(self, n):
+        out = C.c_double()
+        _check(load().ncgm_lp_eval(self.h, int(n), C.byref(out)))
+        return out.value
+
+    def bind(self, ctx: Context):
+        """Network used by ncgm_gcg on ctx with precond = LEARNED."""
+        _check(load().ncgm_set_lp(ctx.h, self.h))

@@ -34,7 +34,8 @@ class GcgStats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("converged", C.c_int),
                 ("pcg_steps_max", C.c_int), ("pcg_steps_total", C.c_int),
                 ("basis_cols", C.c_int), ("max_residual", C.c_double),
-                ("ms_total", C.c_double), ("ms_pcg", C.c_double)]
+                ("ms_total", C.c_double), ("ms_pcg", C.c_double),
+                ("lp_columns", C.c_int)]
 
 
 class Pairing(C.Structure):
@@ -57,7 +58,8 @@ class HFConfig(C.Structure):
         ("start_hfb_iter", C.c_int), ("pairing_threshold", C.c_double),
         ("constrain_com", C.c_int), ("curve_mode", C.c_int),
         ("mu20", C.c_double), ("constraints_tol", C.c_double),
-        ("spe_tol", C.c_double)]
+        ("spe_tol", C.c_double), ("lp", C.c_void_p),
+        ("lp_collect_every", C.c_int)]
 
 
 class HFResult(C.Structure):
@@ -77,6 +79,7 @@ STATUS = {0: "NCGM_OK", 1: "NCGM_ERR_ARG", 2: "NCGM_ERR_CUDA",
           3: "NCGM_ERR_NAN", 4: "NCGM_ERR_RANK", 5: "NCGM_ERR_TIMEOUT",
           6: "NCGM_ERR_EIG", 7: "NCGM_ERR_NOMEM"}
 FP64, FP32 = 0, 1
+PRECOND_JACOBI, PRECOND_LEARNED = 0, 1
 NEUTRON, PROTON = 0, 1
 ORDER_MATCH_PREVIOUS, ORDER_ASCENDING = 0, 1
 PAIRING_NONE, PAIRING_HFB, PAIRING_BCS = 0, 1, 2
@@ -103,6 +106,18 @@ SIGNATURES = {
     "ncgm_densities": ([_vp, _vp, _i, _vp, _vp, _vp, _vp], _i),
     "ncgm_poisson": ([_vp, _vp, _i, _vp, _vp, _vp, _vp], _i),
     "ncgm_poisson_noalloc": ([_i, _d, _vp, _i, _vp, _vp, _vp, _vp, _vp], _i),
+    "ncgm_lp_num_params": ([], _i),
+    "ncgm_lp_create": ([C.POINTER(_vp), C.c_ulonglong], _i),
+    "ncgm_lp_destroy": ([_vp], _i),
+    "ncgm_lp_get_params": ([_vp, _vp], _i),
+    "ncgm_lp_set_params": ([_vp, _vp], _i),
+    "ncgm_lp_forward": ([_vp, _i, _i, _vp, _vp], _i),
+    "ncgm_lp_gradient": ([_vp, _i, _i, _vp, _vp, _vp, _vp], _i),
+    "ncgm_lp_collect": ([_vp, _vp, _i, _vp, _i, _vp, _d, _i, _d], _i),
+    "ncgm_lp_dataset_size": ([_vp, _i], _i),
+    "ncgm_lp_train": ([_vp, _i, _i, _d, C.c_ulonglong, _vp], _i),
+    "ncgm_lp_eval": ([_vp, _i, _vp], _i),
+    "ncgm_set_lp": ([_vp, _vp], _i),
 }
 
 

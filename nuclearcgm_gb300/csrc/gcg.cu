@@ -13,6 +13,7 @@
 // Everything runs on the device; the host keeps only O(m) scalars (Ritz
 // values, residual norms) to take the locking decisions.
 #include "k_dense.cuh"
+#include "k_learned.cuh"
 #include "k_pcg.cuh"
 #include "ncgm_internal.cuh"
 
@@ -175,12 +176,18 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
   const size_t maxChunks = std::max<size_t>(
       1, std::min<size_t>(256, (size_t)8 * 1024 * 1024 / ((size_t)mx * mx)));
   const bool fp32 = prm.precision == NCGM_FP32;
+  const bool learned = prm.precond == NCGM_PRECOND_LEARNED;
+  if (learned && !ctx->lp) {
+    setError("ncgm_gcg: learned preconditioner requested but no network set "
+             "(ncgm_set_lp)");
+    return NCGM_ERR_ARG;
+  }
   // workspace
   size_t need = 0;
   need += N * (size_t)vmax * sizeof(double2) * 3; // V, Q, AV
   need += N * (size_t)vmax * sizeof(double2);     // Q1 (CholQR pass 1)
   need += N * (size_t)nev * sizeof(double2) * 5;  // Xa, X0, Xn, AXn, AXa
-  need += N * (size_t)nev * (fp32 ? sizeof(float2) : sizeof(double2)) * 6;
+  need += N * (size_t)nev * (fp32 ? sizeof(float2) : sizeof(double2)) * 7;
   need += (size_t)mx * mx * sizeof(double2) * 8;  // small matrices
   need += maxChunks * (size_t)mx * mx * sizeof(double2);
   need += (size_t)nev * 128 * 5 * sizeof(double) + 64 * 1024;
@@ -193,21 +200,22 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
           *Xn = ar.take<double2>(N * nev), *AXn = ar.take<double2>(N * nev),
           *AXa = ar.take<double2>(N * nev);
   const size_t vbytes = fp32 ? sizeof(float2) : sizeof(double2);
-  char *pv = ar.take<char>(N * nev * vbytes * 6);
+  char *pv = ar.take<char>(N * nev * vbytes * 7);
   void *pX = pv, *pW = pv + N * nev * vbytes, *pR = pv + 2 * N * nev * vbytes,
        *pZ = pv + 3 * N * nev * vbytes, *pP = pv + 4 * N * nev * vbytes,
-       *pAP = pv + 5 * N * nev * vbytes;
+       *pAP = pv + 5 * N * nev * vbytes, *pD0 = pv + 6 * N * nev * vbytes;
   double2 *small = ar.take<double2>((size_t)mx * mx * 8);
   double2 *partials = ar.take<double2>(maxChunks * (size_t)mx * mx);
   double *dW = ar.take<double>(mx), *dL = ar.take<double>(mx),
          *dRes = ar.take<double>(mx), *dXax = ar.take<double>(mx),
          *dLs = ar.take<double>(mx);
   int *dKeep = ar.take<int>(mx), *dIdx = ar.take<int>(mx),
-      *dPerm = ar.take<int>(mx), *dStat = ar.take<int>(4);
+      *dPerm = ar.take<int>(mx), *dStat = ar.take<int>(4),
+      *dUse = ar.take<int>(mx);
   PcgCol *dSt = ar.take<PcgCol>(nev);
   double *pp1 = ar.take<double>((size_t)nev * 128 * 3),
          *pp2 = ar.take<double>((size_t)nev * 128 * 2);
-  int *dLive = ar.take<int>(1);
+  int *dLive = ar.take<int>(1), *dNdone = ar.take<int>(1);
   double2 *Gs = small, *Cw = small + 4 * (size_t)mx * mx,
           *Ev = small + 5 * (size_t)mx * mx, *Ap = small + 6 * (size_t)mx * mx;
 
@@ -264,7 +272,7 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
   std::vector<double> x0lam; // Re(x^H A x) of the locked columns
   bool early = false;
   double msPcg = 0;
-  int iterations = 0, lastBasis = 0, pcgMax = 0;
+  int iterations = 0, lastBasis = 0, pcgMax = 0, lpCols = 0;
   int pc = pcols;
   for (int iter = 0; iter < prm.max_iter; ++iter) {
     if (nconv == nev) {
@@ -294,7 +302,51 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
       NCGM_CUDA(cudaMemcpyAsync(dLs, ls.data(), sizeof(double) * nact,
                                 cudaMemcpyHostToDevice, s));
       auto tp = std::chrono::steady_clock::now();
-      if (!fp32) {
+      if (learned) {
+        // network start d0 = N(x lambda - A x) for every active column
+        NCGM_CUDA(cudaMemcpyAsync(dL, Lambda.data(), sizeof(double) * nact,
+                                  cudaMemcpyHostToDevice, s));
+        int rc = fp32 ? lpInitialCorrection<float>(
+                            ctx->lp, ctx, species, Xa, AXa, dL, shift, nact,
+                            static_cast<float *>(pD0), s)
+                      : lpInitialCorrection<double>(
+                            ctx->lp, ctx, species, Xa, AXa, dL, shift, nact,
+                            static_cast<double *>(pD0), s);
+        if (rc != NCGM_OK) return rc;
+      }
+      if (!fp32 && learned) {
+        PcgPlan<double> pl;
+        pl.N = N;
+        pl.ncols = nact;
+        pl.X = Xa;
+        pl.ldx = N;
+        pl.X64 = Xa;
+        pl.AX64 = AXa;
+        pl.W64 = Wd;
+        pl.W = pW;
+        pl.R = pR;
+        pl.Z = pZ;
+        pl.P = pP;
+        pl.AP = pAP;
+        pl.D0 = pD0;
+        pl.useNet = dUse;
+        pl.lamShift = dLs;
+        pl.coef = ctx->sp[species].coef64;
+        pl.shift = shift;
+        pl.tol = prm.cg_tol;
+        pl.maxSteps = prm.cg_steps;
+        pl.st = dSt;
+        pl.partials = pp1;
+        pl.partials2 = pp2;
+        pl.live = dLive;
+        pl.ndone = dNdone;
+        pl.apply = [&](const void *X, size_t, void *Y, int cols, double sh,
+                       cudaStream_t st) {
+          applyH64(ctx, species, static_cast<const double2 *>(X),
+                   static_cast<double2 *>(Y), cols, sh, st);
+        };
+        pcgRun<double>(pl, s);
+      } else if (!fp32) {
         PcgPlan<double> pl;
         pl.N = N;
         pl.ncols = nact;
@@ -314,6 +366,7 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
         pl.partials = pp1;
         pl.partials2 = pp2;
         pl.live = dLive;
+        pl.ndone = dNdone;
         pl.apply = [&](const void *X, size_t, void *Y, int cols, double sh,
                        cudaStream_t st) {
           applyH64(ctx, species, static_cast<const double2 *>(X),
@@ -334,6 +387,10 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
         pl.Z = pZ;
         pl.P = pP;
         pl.AP = pAP;
+        if (learned) {
+          pl.D0 = pD0;
+          pl.useNet = dUse;
+        }
         pl.lamShift = dLs;
         pl.coef = ctx->sp[species].coef64;
         pl.shift = shift;
@@ -343,6 +400,7 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
         pl.partials = pp1;
         pl.partials2 = pp2;
         pl.live = dLive;
+        pl.ndone = dNdone;
         pl.apply = [&](const void *X, size_t, void *Y, int cols, double sh,
                        cudaStream_t st) {
           applyH32(ctx, species, static_cast<const float2 *>(X),
@@ -356,6 +414,12 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
                                   cudaMemcpyDeviceToHost, s));
         NCGM_CUDA(cudaStreamSynchronize(s));
         for (auto &c : hs) pcgMax = std::max(pcgMax, c.iters);
+        if (learned) {
+          std::vector<int> hu(nact);
+          NCGM_CUDA(cudaMemcpy(hu.data(), dUse, sizeof(int) * nact,
+                               cudaMemcpyDeviceToHost));
+          for (int u : hu) lpCols += u;
+        }
       }
       msPcg += msSince(tp);
     }
@@ -477,6 +541,7 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
     stats->max_residual = mr;
     stats->ms_total = msSince(tStart);
     stats->ms_pcg = msPcg;
+    stats->lp_columns = lpCols;
   }
   return NCGM_OK;
 }

@@ -926,6 +926,11 @@ int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
   const int mx = std::max(orbN, orbP);
   NCGM_TRY(ncgm_create(&R.ctx, R.n, R.a, 4 * mx + 8, 0));
   R.s = R.ctx->stream;
+  if (cfg.hf_gcg.precond == NCGM_PRECOND_LEARNED && !cfg.lp) {
+    setError("hf: learned preconditioner requested without a network");
+    return NCGM_ERR_ARG;
+  }
+  R.ctx->lp = cfg.lp;
   R.sp[0].orb = orbN;
   R.sp[1].orb = orbP;
   R.sp[0].par = cfg.pair_n;
@@ -1036,6 +1041,18 @@ int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
       std::copy(lamN.begin(), lamN.begin() + orbP, lamP.begin());
     }
     R.tGcg += now() - t0;
+    // training pairs for the learned preconditioner: the new eigenpairs on
+    // this iteration's Hamiltonians, with the shift the next GCG call uses
+    if (cfg.lp && cfg.lp_collect_every > 0 && it % cfg.lp_collect_every == 0) {
+      const double shN = (lamN.back() - 100.0 * lamN[0]) / 99.0;
+      const double shP = (lamP.back() - 100.0 * lamP[0]) / 99.0;
+      NCGM_TRY(ncgm_lp_collect(cfg.lp, R.ctx, 0,
+                               reinterpret_cast<const double *>(Sn.Xn), orbN,
+                               lamN.data(), shN, 2000, 1e-10));
+      NCGM_TRY(ncgm_lp_collect(cfg.lp, R.ctx, 1,
+                               reinterpret_cast<const double *>(Sp.Xn), orbP,
+                               lamP.data(), shP, 2000, 1e-10));
+    }
     double maxd = 0;
     for (int i = 0; i < orbN; ++i) maxd = std::max(maxd, std::abs(lamN[i] - Sn.e[i]));
     for (int i = 0; i < orbP; ++i) maxd = std::max(maxd, std::abs(lamP[i] - Sp.e[i]));

@@ -10,6 +10,7 @@
 #include "k_pcg.cuh"
 
 #include <cfloat>
+#include <vector>
 
 namespace ncgm {
 
@@ -121,6 +122,99 @@ __global__ void pcgInitCorrKernel(const double2 *X64, const double2 *AX64,
   }
 }
 
+// partials of Re(d0^H r0) and Re(d0^H T) per column, r0 = x lam - A x
+// (FP64), T = (A + shift) d0 for the learned initial correction d0
+template <class T>
+__global__ void pcgNetNormKernel(const double2 *X64, const double2 *AX64,
+                                 const typename C2<T>::type *D0,
+                                 const typename C2<T>::type *Td, size_t N,
+                                 const double *lamShift, double shift,
+                                 double *partials, int nblk) {
+  __shared__ double sh[kThreads];
+  const int col = blockIdx.y;
+  const double lam = lamShift[col] - shift;
+  double a = 0, b = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x) {
+    size_t o = (size_t)col * N + i;
+    double2 x = X64[o], ax = AX64[o];
+    auto d = D0[o];
+    auto t = Td[o];
+    double rx = x.x * lam - ax.x, ry = x.y * lam - ax.y;
+    a += (double)d.x * rx + (double)d.y * ry;
+    b += (double)d.x * t.x + (double)d.y * t.y;
+  }
+  double s0 = blockSum(a, sh), s1 = blockSum(b, sh);
+  if (threadIdx.x == 0) {
+    double *pp = partials + (size_t)col * nblk * 2;
+    pp[blockIdx.x] = s0;
+    pp[nblk + blockIdx.x] = s1;
+  }
+}
+
+// Correction-form start from the learned d0, scaled by the step that
+// minimises the CG energy Phi(d) = d^H (A + shift) d / 2 - Re(d^H r0) along
+// d0: alpha = Re(d0^H r0) / Re(d0^H (A + shift) d0). Phi(alpha d0) <= Phi(0),
+// so the start is never worse than the reference's d = 0 in the A-norm the
+// PCG minimises; a column with alpha <= 0 (or a non-positive curvature)
+// starts from 0. d = alpha d0, r = r0 - alpha T, z = Minv r, p = z.
+template <class T>
+__global__ void pcgInitNetKernel(const double2 *X64, const double2 *AX64,
+                                 const typename C2<T>::type *D0,
+                                 const typename C2<T>::type *Td,
+                                 typename C2<T>::type *Dv,
+                                 typename C2<T>::type *R,
+                                 typename C2<T>::type *Z,
+                                 typename C2<T>::type *P, size_t N,
+                                 const double *lamShift, const double *coef,
+                                 double shift, const double *normPart,
+                                 double *partials, int nblk, int *useNet) {
+  __shared__ double sh[kThreads];
+  __shared__ double alpha;
+  const int col = blockIdx.y;
+  if (threadIdx.x == 0) {
+    const double *pp = normPart + (size_t)col * nblk * 2;
+    double dr = 0, dad = 0;
+    for (int k = 0; k < nblk; ++k) {
+      dr += pp[k];
+      dad += pp[nblk + k];
+    }
+    alpha = (dr > 0.0 && dad > 0.0) ? dr / dad : 0.0;
+    if (blockIdx.x == 0 && useNet) useNet[col] = alpha > 0.0;
+  }
+  __syncthreads();
+  const double al = alpha;
+  const double ls = lamShift[col], lam = ls - shift;
+  double bb = 0, rr = 0, rz = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x) {
+    size_t o = (size_t)col * N + i;
+    double2 x = X64[o], ax = AX64[o];
+    double bx = x.x * ls, by = x.y * ls;
+    double rx = x.x * lam - ax.x, ry = x.y * lam - ax.y;
+    auto d0 = D0[o];
+    auto t = Td[o];
+    rx -= al * (double)t.x;
+    ry -= al * (double)t.y;
+    double m = invDiag(coef, i / 2, shift);
+    double zx = m * rx, zy = m * ry;
+    bb += bx * bx + by * by;
+    rr += rx * rx + ry * ry;
+    rz += rx * zx + ry * zy;
+    Dv[o] = {(T)(al * (double)d0.x), (T)(al * (double)d0.y)};
+    R[o] = {(T)rx, (T)ry};
+    Z[o] = {(T)zx, (T)zy};
+    P[o] = {(T)zx, (T)zy};
+  }
+  double s0 = blockSum(bb, sh), s1 = blockSum(rr, sh), s2 = blockSum(rz, sh);
+  if (threadIdx.x == 0) {
+    double *pp = partials + (size_t)col * nblk * 3;
+    pp[blockIdx.x] = s0;
+    pp[nblk + blockIdx.x] = s1;
+    pp[2 * nblk + blockIdx.x] = s2;
+  }
+}
+
 // w = x + d (FP64 result); a column with b = 0 returns w = 0
 template <class T>
 __global__ void pcgCombineKernel(const double2 *X64,
@@ -139,7 +233,7 @@ __global__ void pcgCombineKernel(const double2 *X64,
 }
 
 __global__ void pcgInitFinish(PcgCol *st, const double *partials, int nblk,
-                              double tol) {
+                              double tol, int *ndone) {
   const int col = blockIdx.x;
   if (threadIdx.x != 0) return;
   const double *pp = partials + (size_t)col * nblk * 3;
@@ -159,6 +253,7 @@ __global__ void pcgInitFinish(PcgCol *st, const double *partials, int nblk,
   c.zero = (bb == 0.0);
   c.done = (bb == 0.0) || (rr < c.thr);
   st[col] = c;
+  if (c.done && ndone) atomicAdd(ndone, 1);
 }
 
 // partial p^H Ap (complex)
@@ -246,7 +341,7 @@ __global__ void pcgUpdateKernel(typename C2<T>::type *Wv,
 }
 
 __global__ void pcgFinishKernel(PcgCol *st, const double *partials2, int nblk,
-                                int *live) {
+                                int *live, int *ndone) {
   const int col = blockIdx.x;
   if (threadIdx.x != 0) return;
   PcgCol c = st[col];
@@ -259,6 +354,7 @@ __global__ void pcgFinishKernel(PcgCol *st, const double *partials2, int nblk,
   }
   if (rr < c.thr) {
     c.done = 1;
+    if (ndone) atomicAdd(ndone, 1);
   } else {
     c.absOld = c.absNew;
     c.absNew = rz;
@@ -297,6 +393,32 @@ __global__ void pcgZeroKernel(typename C2<T>::type *Wv, size_t N,
 
 } // namespace
 
+constexpr int kLag = 2, kPollEvents = 4, kPollSlots = 4096;
+struct ExitPoll {
+  int device = -1;
+  int *host = nullptr; // pinned, kPollSlots
+  cudaEvent_t ev[kPollEvents];
+};
+// one pinned slot array and event ring per host thread and device
+ExitPoll *exitPoll() {
+  thread_local std::vector<ExitPoll *> pool;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  for (auto *p : pool)
+    if (p->device == dev) return p;
+  auto *p = new ExitPoll;
+  p->device = dev;
+  if (cudaHostAlloc(reinterpret_cast<void **>(&p->host),
+                    sizeof(int) * kPollSlots, cudaHostAllocDefault) !=
+      cudaSuccess) {
+    delete p;
+    return nullptr;
+  }
+  for (auto &e : p->ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  pool.push_back(p);
+  return p;
+}
+
 int pcgBlocks(size_t N) {
   size_t b = (N + kThreads * 4 - 1) / (kThreads * 4);
   if (b > 128) b = 128;
@@ -309,7 +431,20 @@ void pcgRun(const PcgPlan<T> &pl, cudaStream_t s) {
   const int nblk = pcgBlocks(pl.N);
   dim3 grid(nblk, pl.ncols);
   using V = typename C2<T>::type;
-  if (pl.AX64) {
+  if (pl.AX64 && pl.D0) {
+    // T = (A + shift) d0 into AP (free until the first step)
+    pl.apply(pl.D0, pl.N, pl.AP, pl.ncols, pl.shift, s);
+    pcgNetNormKernel<T><<<grid, kThreads, 0, s>>>(
+        pl.X64, pl.AX64, reinterpret_cast<const V *>(pl.D0),
+        reinterpret_cast<const V *>(pl.AP), pl.N, pl.lamShift, pl.shift,
+        pl.partials2, nblk);
+    pcgInitNetKernel<T><<<grid, kThreads, 0, s>>>(
+        pl.X64, pl.AX64, reinterpret_cast<const V *>(pl.D0),
+        reinterpret_cast<const V *>(pl.AP), reinterpret_cast<V *>(pl.W),
+        reinterpret_cast<V *>(pl.R), reinterpret_cast<V *>(pl.Z),
+        reinterpret_cast<V *>(pl.P), pl.N, pl.lamShift, pl.coef, pl.shift,
+        pl.partials2, pl.partials, nblk, pl.useNet);
+  } else if (pl.AX64) {
     pcgInitCorrKernel<T><<<grid, kThreads, 0, s>>>(
         pl.X64, pl.AX64, reinterpret_cast<V *>(pl.W),
         reinterpret_cast<V *>(pl.R), reinterpret_cast<V *>(pl.Z),
@@ -325,8 +460,29 @@ void pcgRun(const PcgPlan<T> &pl, cudaStream_t s) {
         reinterpret_cast<V *>(pl.P), pl.N, pl.lamShift, pl.coef, pl.shift,
         pl.partials, nblk);
   }
-  pcgInitFinish<<<pl.ncols, 32, 0, s>>>(pl.st, pl.partials, nblk, pl.tol);
+  if (pl.ndone) cudaMemsetAsync(pl.ndone, 0, sizeof(int), s);
+  pcgInitFinish<<<pl.ncols, 32, 0, s>>>(pl.st, pl.partials, nblk, pl.tol,
+                                        pl.ndone);
+  // Early exit: after the init and after every step the count of finished
+  // columns is copied to pinned host memory behind an event; before step
+  // `it` the host reads the count of step it - kLag (already complete, so
+  // the device queue never drains) and stops issuing steps once every
+  // column has finished. Later steps would only launch no-op kernels.
+  ExitPoll *poll = pl.ndone ? exitPoll() : nullptr;
+  auto mark = [&](int slot) {
+    if (!poll) return;
+    cudaMemcpyAsync(poll->host + slot, pl.ndone, sizeof(int),
+                    cudaMemcpyDeviceToHost, s);
+    cudaEventRecord(poll->ev[slot % kPollEvents], s);
+  };
+  mark(0);
   for (int it = 0; it < pl.maxSteps; ++it) {
+    if (poll && it + 1 - kLag >= 0 && it + 1 - kLag < kPollSlots) {
+      const int slot = it + 1 - kLag;
+      if (cudaEventSynchronize(poll->ev[slot % kPollEvents]) == cudaSuccess &&
+          poll->host[slot] >= pl.ncols)
+        break;
+    }
     pl.apply(pl.P, pl.N, pl.AP, pl.ncols, pl.shift, s);
     pcgDotKernel<T><<<grid, kThreads, 0, s>>>(
         reinterpret_cast<const V *>(pl.P), reinterpret_cast<const V *>(pl.AP),
@@ -337,10 +493,11 @@ void pcgRun(const PcgPlan<T> &pl, cudaStream_t s) {
         reinterpret_cast<const V *>(pl.AP), pl.N, pl.st, pl.coef, pl.shift,
         pl.partials, pl.partials2, nblk);
     pcgFinishKernel<<<pl.ncols, 32, 0, s>>>(pl.st, pl.partials2, nblk,
-                                            pl.live);
+                                            pl.live, pl.ndone);
     pcgPKernel<T><<<grid, kThreads, 0, s>>>(
         reinterpret_cast<V *>(pl.P), reinterpret_cast<const V *>(pl.Z), pl.N,
         pl.st);
+    if (it + 1 < kPollSlots) mark(it + 1);
   }
   if (pl.AX64)
     pcgCombineKernel<T><<<grid, kThreads, 0, s>>>(

@@ -27,10 +27,16 @@ template <class T> struct PcgPlan {
   PcgCol *st = nullptr;
   double *partials = nullptr, *partials2 = nullptr; // ncols*128*3, ncols*128*2
   int *live = nullptr; // count of column-iterations (stats)
+  int *ndone = nullptr; // device counter of finished columns: early exit
   // correction form: when AX64 is set the plan solves for d = w - x from the
   // FP64 residual x lam - A x; X64 = x, W64 receives w = x + d (FP64)
   const double2 *X64 = nullptr, *AX64 = nullptr;
   double2 *W64 = nullptr;
+  // correction form only: initial correction d0 (precision T, N x ncols);
+  // the PCG starts from alpha d0 with the energy-minimising alpha, or from 0
+  // when alpha <= 0 (useNet[col] records the choice, device, may be null)
+  const void *D0 = nullptr;
+  int *useNet = nullptr;
   // Y = (A + shift) X on device buffers (ld of X given, Y stride N)
   std::function<void(const void *, size_t, void *, int, double, cudaStream_t)>
       apply;

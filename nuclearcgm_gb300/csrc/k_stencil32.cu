@@ -276,6 +276,296 @@ __global__ void __launch_bounds__(512, 1)
   }
 }
 
+// ---- packed FP32 pair arithmetic (f32x2: one instruction, two lanes) ----
+using f2x = unsigned long long;
+__device__ __forceinline__ f2x pk(float a, float b) {
+  f2x r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float2 upk(f2x v) {
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+  return r;
+}
+__device__ __forceinline__ f2x add2(f2x a, f2x b) {
+  f2x r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2x sub2(f2x a, f2x b) {
+  f2x r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2x mul2(f2x a, f2x b) {
+  f2x r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c) {
+  f2x r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+__device__ __forceinline__ f2x bc(float a) { return pk(a, a); }
+
+// pointH (stencil_core.cuh) with each spin component held as one (re, im)
+// pair: the kinetic, derivative and gradient terms are real coefficients
+// times pairs; the spin-orbit matrix is split as A + iB (A, B real), so
+// (A + iB) D = A D + i (B D) and only one i-rotation per spin is needed.
+__device__ __forceinline__ float4 pointH2(const float4 ca, const float4 cb,
+                                          float shift, float4 v, float4 xp1,
+                                          float4 xm1, float4 xp2, float4 xm2,
+                                          float4 yp1, float4 ym1, float4 yp2,
+                                          float4 ym2, float4 zp1, float4 zm1,
+                                          float4 zp2, float4 zm2) {
+  const f2x D = bc(ca.x + shift), NF = bc(-ca.y);
+  const f2x GX = bc(ca.z), GY = bc(ca.w), GZ = bc(cb.x);
+  const f2x WX = bc(cb.y), WY = bc(cb.z), WZ = bc(cb.w);
+  const f2x NWX = bc(-cb.y), NWY = bc(-cb.z), NWZ = bc(-cb.w);
+  const f2x C43 = bc(4.0f / 3.0f), NC112 = bc(-1.0f / 12.0f), EIGHT = bc(8.f);
+  f2x o[2], Dx[2], Dy[2], Dz[2];
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    auto A = [s](float4 q) { return s ? pk(q.z, q.w) : pk(q.x, q.y); };
+    const f2x a_xp1 = A(xp1), a_xm1 = A(xm1), a_xp2 = A(xp2), a_xm2 = A(xm2);
+    const f2x a_yp1 = A(yp1), a_ym1 = A(ym1), a_yp2 = A(yp2), a_ym2 = A(ym2);
+    const f2x a_zp1 = A(zp1), a_zm1 = A(zm1), a_zp2 = A(zp2), a_zm2 = A(zm2);
+    f2x s1 = add2(add2(add2(a_xp1, a_xm1), add2(a_yp1, a_ym1)),
+                  add2(a_zp1, a_zm1));
+    f2x s2 = add2(add2(add2(a_xp2, a_xm2), add2(a_yp2, a_ym2)),
+                  add2(a_zp2, a_zm2));
+    f2x t = fma2(C43, s1, mul2(NC112, s2));
+    f2x os = fma2(NF, t, mul2(D, A(v)));
+    Dx[s] = fma2(EIGHT, sub2(a_xp1, a_xm1), sub2(a_xm2, a_xp2));
+    Dy[s] = fma2(EIGHT, sub2(a_yp1, a_ym1), sub2(a_ym2, a_yp2));
+    Dz[s] = fma2(EIGHT, sub2(a_zp1, a_zm1), sub2(a_zm2, a_zp2));
+    os = fma2(GX, Dx[s], os);
+    os = fma2(GY, Dy[s], os);
+    o[s] = fma2(GZ, Dz[s], os);
+  }
+  // spin-orbit: real parts (A) into o, imaginary parts (B) into u, o += i u
+  o[0] = fma2(NWZ, Dx[1], o[0]);
+  o[0] = fma2(WX, Dz[1], o[0]);
+  f2x u0 = mul2(WY, Dx[0]);
+  u0 = fma2(NWX, Dy[0], u0);
+  u0 = fma2(WZ, Dy[1], u0);
+  u0 = fma2(NWY, Dz[1], u0);
+  o[1] = fma2(WZ, Dx[0], o[1]);
+  o[1] = fma2(NWX, Dz[0], o[1]);
+  f2x u1 = mul2(NWY, Dx[1]);
+  u1 = fma2(WZ, Dy[0], u1);
+  u1 = fma2(WX, Dy[1], u1);
+  u1 = fma2(NWY, Dz[0], u1);
+  const float2 p0 = upk(o[0]), p1 = upk(o[1]), q0 = upk(u0), q1 = upk(u1);
+  return make_float4(p0.x - q0.y, p0.y + q0.x, p1.x - q1.y, p1.y + q1.x);
+}
+
+// z-marching form. Same producer and plane sequence as stencilStream32, but
+// every consumer thread owns one point of the band and keeps its z-column
+// (z-2 .. z+2) in registers while it walks the planes of a run: per step it
+// reads the new plane z+2 at its point and the x/y neighbours in the centre
+// plane (9 shared loads per point instead of 13), and releases the centre
+// plane as soon as the step is done. The
+// per-point field coefficients of the next plane are copied one step ahead
+// into a per-thread shared staging buffer (cp.async), so no global-load
+// latency sits on the step's critical path.
+// Release rule per warp and run (seq base <-> plane ka-2): base and base+1
+// after the window load, base+2+m after step ka+m, base+len+2 and base+len+3
+// after the last step.
+constexpr int kMarchThreads = 512;
+template <int WFIX>
+__global__ void __launch_bounds__(kMarchThreads, 1)
+    stencilMarch32(const __grid_constant__ CUtensorMap map, StreamArgs A) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ Run runs[kMaxRuns];
+  __shared__ int nruns, totalSeq, failed;
+  const int n = A.n, W = WFIX ? WFIX : n + 4;
+  const int boxElems = (A.TY + 4) * W;
+  const int slotElems = (boxElems + 7) & ~7;
+  const uint32_t boxBytes = boxElems * 16u;
+  const int nCons = blockDim.x / 32 - 1;
+  const int rmask = A.ring - 1, rlog = __ffs(A.ring) - 1;
+  float4 *ring = reinterpret_cast<float4 *>(smem_raw);
+  uint64_t *full = reinterpret_cast<uint64_t *>(
+      smem_raw + (size_t)A.ring * slotElems * 16u);
+  uint64_t *empty = full + A.ring;
+  const long long t0 = (long long)blockIdx.x * A.total / gridDim.x;
+  const long long t1 = (long long)(blockIdx.x + 1) * A.total / gridDim.x;
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const uint32_t kLimit = 1u << 20;
+
+  if (threadIdx.x == 0) {
+    int r = 0, seq = 0;
+    for (long long t = t0; t < t1 && r < kMaxRuns;) {
+      const int cb = (int)(t / n), ka = (int)(t % n);
+      const long long rem = t1 - t;
+      const int kb = (rem < (long long)(n - ka)) ? ka + (int)rem : n;
+      runs[r] = {cb, ka, kb, seq};
+      seq += kb - ka + 4;
+      t += kb - ka;
+      ++r;
+    }
+    nruns = r;
+    totalSeq = seq;
+    failed = 0;
+    for (int s = 0; s < A.ring; ++s) {
+      mbarInit(&full[s], 1);
+      mbarInit(&empty[s], nCons);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const int NR = nruns, TS = totalSeq;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int pr = 0, pz = (NR > 0) ? runs[0].ka - 2 : 0;
+      int issued = 0;
+      bool ok = true;
+      for (int s = 0; s < TS; ++s) {
+        const int slot = s & rmask;
+        if (s >= A.ring) {
+          if (!mbarWaitSleep(&empty[slot], ((s >> rlog) - 1) & 1u, kLimit) ||
+              *(volatile int *)&failed) {
+            ok = false;
+            break;
+          }
+        }
+        const Run &R = runs[pr];
+        const int col = R.cb / A.nbands, band = R.cb % A.nbands;
+        mbarExpectTx(&full[slot], boxBytes);
+        tmaTile5(ring + (size_t)slot * slotElems, &map, -2, band * A.TY - 2,
+                 pz, col, &full[slot]);
+        issued = s + 1;
+        if (++pz >= R.kb + 2 && pr + 1 < NR) {
+          ++pr;
+          pz = runs[pr].ka - 2;
+        }
+      }
+      if (!ok) {
+        atomicExch(A.err, 1);
+        *(volatile int *)&failed = 1;
+        for (int s = (issued > A.ring ? issued - A.ring : 0); s < issued; ++s)
+          mbarWaitSleep(&full[s & rmask], (s >> rlog) & 1u, kLimit);
+      }
+    }
+    return;
+  }
+
+  // ---- consumers: thread ct owns point (i, j) of the band ----
+  // (adjacent threads take adjacent i: conflict-free 16-byte shared loads)
+  const int ct = threadIdx.x - 32, nct = blockDim.x - 32;
+  const bool own = ct < A.TY * n;
+  const int ii = own ? ct % n : 0, jj = own ? ct / n : 0;
+  const int l = (jj + 2) * W + ii + 2;
+  // per-thread coefficient staging, two buffers x 2 float4 (cp.async)
+  float4 *stage = reinterpret_cast<float4 *>(
+      smem_raw + (size_t)A.ring * slotElems * 16u + (size_t)A.ring * 16u);
+  const uint32_t stage0 = smemAddr(stage + ct), dstep = nct * 16u;
+  auto prefetch = [&](bool act, unsigned pidx, int buf) {
+    if (act) {
+      const float4 *c0 = A.coef + 2 * (size_t)pidx;
+      const uint32_t d0 = stage0 + buf * 2 * dstep;
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d0),
+                   "l"(c0)
+                   : "memory");
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                       d0 + dstep),
+                   "l"(c0 + 1)
+                   : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  int waited = -1, sc = 0; // sc: running step count (staging buffer parity)
+  bool ok = true;
+  auto waitTo = [&](int upto) {
+    while (waited < upto) {
+      const int s = waited + 1;
+      if (!mbarWaitSleep(&full[s & rmask], (s >> rlog) & 1u, kLimit))
+        return false;
+      waited = s;
+    }
+    return !*(volatile int *)&failed;
+  };
+  auto slotp = [&](int s) {
+    return (const float4 *)(ring + (size_t)(s & rmask) * slotElems);
+  };
+  auto release = [&](int s) {
+    __syncwarp();
+    if (lane == 0) mbarArrive(&empty[s & rmask]);
+  };
+  for (int r = 0; r < NR && ok; ++r) {
+    const Run R = runs[r];
+    const int col = R.cb / A.nbands, band = R.cb % A.nbands;
+    const int y0 = band * A.TY;
+    const bool act = own && (y0 + jj) < n;
+    float4 *Yc = A.Y + (size_t)col * A.ns;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const unsigned rowOff = (unsigned)((y0 + jj) * n + ii);
+    const unsigned nn = (unsigned)(n * n);
+    prefetch(act, (unsigned)R.ka * nn + rowOff, sc & 1);
+    float4 a[5]; // z-window of the point, rotating by 5
+    if (!waitTo(R.base + 3)) {
+      ok = false;
+      break;
+    }
+#pragma unroll
+    for (int d = 0; d < 4; ++d) a[d] = act ? slotp(R.base + d)[l] : z4;
+    a[4] = z4;
+    release(R.base);
+    if (lane == 0) mbarArrive(&empty[(R.base + 1) & rmask]);
+    int k = R.ka;
+#define NCGM_MARCH_STEP(P)                                                     \
+  {                                                                            \
+    const int s0 = R.base + (k - R.ka);                                        \
+    const unsigned pidx = (unsigned)k * nn + rowOff;                           \
+    asm volatile("cp.async.wait_group 0;" ::: "memory");                       \
+    const int cur = sc & 1;                                                    \
+    float4 ca, cb;                                                             \
+    if (act) {                                                                 \
+      ca = stage[(cur * 2) * nct + ct];                                        \
+      cb = stage[(cur * 2 + 1) * nct + ct];                                    \
+    }                                                                          \
+    if (k + 1 < R.kb) prefetch(act, pidx + nn, cur ^ 1);                       \
+    ++sc;                                                                      \
+    if (!waitTo(s0 + 4)) {                                                     \
+      ok = false;                                                              \
+      break;                                                                   \
+    }                                                                          \
+    if (act) {                                                                 \
+      const float4 *pc = slotp(s0 + 2);                                        \
+      a[(P + 4) % 5] = slotp(s0 + 4)[l];                                       \
+      Yc[pidx] = pointH2(ca, cb, A.shift, a[(P + 2) % 5], pc[l + 1],           \
+                         pc[l - 1], pc[l + 2], pc[l - 2], pc[l + W],           \
+                         pc[l - W], pc[l + 2 * W], pc[l - 2 * W],              \
+                         a[(P + 3) % 5], a[(P + 1) % 5], a[(P + 4) % 5],       \
+                         a[P % 5]);                                            \
+    }                                                                          \
+    release(s0 + 2);                                                           \
+    if (k + 1 == R.kb && lane == 0) {                                          \
+      mbarArrive(&empty[(s0 + 3) & rmask]);                                    \
+      mbarArrive(&empty[(s0 + 4) & rmask]);                                    \
+    }                                                                          \
+    if (++k >= R.kb) break;                                                    \
+  }
+    while (true) {
+      NCGM_MARCH_STEP(0)
+      NCGM_MARCH_STEP(1)
+      NCGM_MARCH_STEP(2)
+      NCGM_MARCH_STEP(3)
+      NCGM_MARCH_STEP(4)
+    }
+#undef NCGM_MARCH_STEP
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  if (!ok && lane == 0) {
+    atomicExch(A.err, 1);
+    *(volatile int *)&failed = 1;
+  }
+}
+
 using StreamKernel = void (*)(const CUtensorMap, StreamArgs);
 constexpr int kWidths[] = {0, 34, 36, 40, 44, 52};
 template <int PPT> StreamKernel pickW(int W) {
@@ -288,16 +578,29 @@ template <int PPT> StreamKernel pickW(int W) {
   default: return stencilStream32<PPT, 0>;
   }
 }
-StreamKernel pickKernel(int ppt, int W) {
+StreamKernel pickMarch(int W) {
+  switch (W) {
+  case 34: return stencilMarch32<34>;
+  case 36: return stencilMarch32<36>;
+  case 40: return stencilMarch32<40>;
+  case 44: return stencilMarch32<44>;
+  case 52: return stencilMarch32<52>;
+  default: return stencilMarch32<0>;
+  }
+}
+// kind 0: stencilStream32 with `ppt` points per thread; kind 1: z-marching
+StreamKernel pickKernel(int kind, int ppt, int W) {
   static bool attr = false;
   if (!attr) {
     for (int w : kWidths) {
       cudaFuncSetAttribute(pickW<1>(w), cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
       cudaFuncSetAttribute(pickW<2>(w), cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
       cudaFuncSetAttribute(pickW<4>(w), cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+      cudaFuncSetAttribute(pickMarch(w), cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     }
     attr = true;
   }
+  if (kind == 1) return pickMarch(W);
   if (ppt == 1) return pickW<1>(W);
   if (ppt == 2) return pickW<2>(W);
   return pickW<4>(W);
@@ -354,6 +657,12 @@ size_t streamSmem(int n, int TY, int ring) {
   size_t slot = (((size_t)(TY + 4) * (n + 4) + 7) & ~size_t(7)) * 16;
   return (size_t)ring * slot + (size_t)ring * 16; // slots + full/empty bars
 }
+// the z-marching kernel adds 2 x 2 float4 of coefficient staging per
+// consumer thread
+size_t kernelSmem(int kind, int n, int TY, int ring, int threads) {
+  return streamSmem(n, TY, ring) +
+         (kind == 1 ? (size_t)64 * (threads - 32) : 0);
+}
 
 int smCount() {
   static int c = 0;
@@ -368,18 +677,29 @@ int smCount() {
 
 struct Shape {
   int TY, ring, ppt, ctasPerSM;
+  int kind; // 0: stencilStream32, 1: stencilMarch32 (ppt unused)
 };
 
 bool validShape(int n, const Shape &s, int &threads) {
-  if (s.TY < 1 || s.TY > n || s.ring < 8 || (s.ring & (s.ring - 1)) ||
-      !(s.ppt == 1 || s.ppt == 2 || s.ppt == 4))
+  if (s.TY < 1 || s.TY > n || s.ring < 4 || (s.ring & (s.ring - 1)) ||
+      s.ring > 64 || s.ctasPerSM < 1)
     return false;
   if (s.TY + 4 > 256 || n + 4 > 256) return false;
-  const int pts = s.TY * n;
-  // one producer warp + consumer warps covering the band
-  threads = 32 + ((pts + s.ppt - 1) / s.ppt + 31) / 32 * 32;
+  if (s.kind == 1) {
+    // one point per consumer thread
+    threads = 32 + ((s.TY * n) + 31) / 32 * 32;
+    if (threads > kMarchThreads) return false;
+  } else {
+    if (s.kind != 0 || s.ring < 8 || !(s.ppt == 1 || s.ppt == 2 || s.ppt == 4))
+      return false;
+    const int pts = s.TY * n;
+    // one producer warp + consumer warps covering the band
+    threads = 32 + ((pts + s.ppt - 1) / s.ppt + 31) / 32 * 32;
+  }
   if (threads > 512 || threads < 64) return false;
-  if (streamSmem(n, s.TY, s.ring) * s.ctasPerSM > 220 * 1024) return false;
+  if (kernelSmem(s.kind, n, s.TY, s.ring, threads) * s.ctasPerSM >
+      220 * 1024)
+    return false;
   return true;
 }
 
@@ -408,8 +728,9 @@ bool launchStream(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
                             ((long long)(kMaxRuns - 2) * n);
   ctas = std::max(ctas, minCtas);
   ctas = std::min<long long>(ctas, A.total);
-  StreamKernel kern = pickKernel(sh.ppt, n + 4);
-  kern<<<(unsigned)ctas, threads, streamSmem(n, sh.TY, sh.ring), st>>>(map, A);
+  StreamKernel kern = pickKernel(sh.kind, sh.ppt, n + 4);
+  kern<<<(unsigned)ctas, threads,
+         kernelSmem(sh.kind, n, sh.TY, sh.ring, threads), st>>>(map, A);
   return true;
 }
 
@@ -420,7 +741,7 @@ struct TunedShape {
 std::vector<TunedShape> g_tuned;
 
 Shape defaultShape(int n) {
-  Shape s{n, 8, 4, 1};  // ring: a power of two
+  Shape s{n, 8, 4, 1, 0};  // ring: a power of two
   int th;
   while (!validShape(n, s, th) && s.TY > 1) {
     if (s.TY * n > 512 * s.ppt && s.ppt < kPPT) {
@@ -455,35 +776,38 @@ static Shape tune(ncgm_ctx *ctx, int species, int ncols) {
   // NCGM_TUNE_LOG=1 prints every candidate's time to stderr
   const char *lg = std::getenv("NCGM_TUNE_LOG");
   const bool log = lg && lg[0] == '1';
-  for (int TY : rows)
+  auto trial = [&](const Shape &s) {
+    int th;
+    if (!validShape(n, s, th)) return;
+    if (!launchStream(ctx, species, X, Y, ncols, 0.f, ctx->stream, s)) return;
+    cudaEventRecord(ctx->ev0, ctx->stream);
+    for (int r = 0; r < 3; ++r)
+      launchStream(ctx, species, X, Y, ncols, 0.f, ctx->stream, s);
+    cudaEventRecord(ctx->ev1, ctx->stream);
+    if (cudaEventSynchronize(ctx->ev1) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    if (log)
+      std::fprintf(stderr,
+                   "[ncgm tune] n=%d cols=%d kind=%d rows=%d ring=%d ppt=%d "
+                   "ctas/SM=%d: %.1f us\n",
+                   n, ncols, s.kind, s.TY, s.ring, s.ppt, s.ctasPerSM,
+                   1e3f * ms / 3);
+    if (ms < bestMs) {
+      bestMs = ms;
+      best = s;
+    }
+  };
+  for (int TY : rows) {
     for (int ring : {8, 16})
       for (int ppt : {1, 2, 4})
-        for (int cps : {1, 2, 4}) {
-          Shape s{TY, ring, ppt, cps};
-          int th;
-          if (!validShape(n, s, th)) continue;
-          if (!launchStream(ctx, species, X, Y, ncols, 0.f, ctx->stream, s))
-            continue;
-          cudaEventRecord(ctx->ev0, ctx->stream);
-          for (int r = 0; r < 3; ++r)
-            launchStream(ctx, species, X, Y, ncols, 0.f, ctx->stream, s);
-          cudaEventRecord(ctx->ev1, ctx->stream);
-          if (cudaEventSynchronize(ctx->ev1) != cudaSuccess) {
-            cudaGetLastError();
-            continue;
-          }
-          float ms = 0;
-          cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-          if (log)
-            std::fprintf(stderr,
-                         "[ncgm tune] n=%d cols=%d rows=%d ring=%d ppt=%d "
-                         "ctas/SM=%d: %.1f us\n",
-                         n, ncols, TY, ring, ppt, cps, 1e3f * ms / 3);
-          if (ms < bestMs) {
-            bestMs = ms;
-            best = s;
-          }
-        }
+        for (int cps : {1, 2, 4}) trial(Shape{TY, ring, ppt, cps, 0});
+    for (int ring : {4, 8, 16})
+      for (int cps : {1, 2, 4}) trial(Shape{TY, ring, 1, cps, 1});
+  }
   return best;
 }
 
@@ -494,12 +818,12 @@ void applyH32(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
     if (t.ctx == ctx) sh = &t.s;
   if (!sh) {
     g_tuned.push_back({ctx, defaultShape(ctx->n)});
-    // NCGM_STENCIL_SHAPE="rows,ring,ppt,ctasPerSM" fixes the shape (no tuning)
+    // NCGM_STENCIL_SHAPE="rows,ring,ppt,ctasPerSM[,kind]" fixes the shape
     Shape tuned{}, fixed{};
     int th = 0;
     const char *env = std::getenv("NCGM_STENCIL_SHAPE");
-    if (env && std::sscanf(env, "%d,%d,%d,%d", &fixed.TY, &fixed.ring,
-                           &fixed.ppt, &fixed.ctasPerSM) == 4 &&
+    if (env && std::sscanf(env, "%d,%d,%d,%d,%d", &fixed.TY, &fixed.ring,
+                           &fixed.ppt, &fixed.ctasPerSM, &fixed.kind) >= 4 &&
         validShape(ctx->n, fixed, th))
       tuned = fixed;
     else

@@ -64,6 +64,7 @@ struct ncgm_ctx {
   std::vector<std::pair<void *, size_t>> bufs;
   void *buf(int slot, size_t bytes);
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  ncgm_lp *lp = nullptr; // learned preconditioner (not owned)
 };
 
 namespace ncgm {

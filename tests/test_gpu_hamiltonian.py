@@ -42,6 +42,28 @@ def test_fp32_plane_kernel_error_bound(n):
     assert np.abs(Y32 - ref).max() <= FP32_TOL * np.abs(ref).max()
 
 
+# fixed stencil shapes (rows, ring, ppt, CTAs/SM, kind), bypassing the
+# autotuner: kind 0 = plane-streaming kernel, kind 1 = z-marching kernel
+SHAPES = ["3,8,1,1,0", "5,16,4,2,0", "2,4,1,1,1", "8,8,1,2,1", "12,8,1,1,1",
+          "6,4,1,4,1"]
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+@pytest.mark.parametrize("n", [12, 40])
+def test_fp32_fixed_shapes(monkeypatch, shape, n):
+    """Every kernel form and pipeline depth gives the CSR product (the
+    shape is read when a context tunes; shapes invalid for a lattice fall
+    back to the tuner)."""
+    monkeypatch.setenv("NCGM_STENCIL_SHAPE", shape)
+    a = 0.5 * (n - 1) * 0.5
+    ctx, H, R = _pair(n, a, 300 + n, True, True, ncols=6)
+    X = random_block(2 * n ** 3, 6, 3 * n)
+    Y32 = H.apply(X, abi.FP32)
+    ref = R.apply(X)
+    assert np.abs(Y32 - ref).max() <= FP32_TOL * np.abs(ref).max()
+    ctx.close()
+
+
 def test_device_and_host_pointers_agree():
     torch = pytest.importorskip("torch")
     n, a = 10, 3.0
