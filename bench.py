@@ -137,6 +137,64 @@ def _cpu_reference(steps, warmup, a, f, gradf, U, W, X, cols_per_step):
     return byts / dt / 1e9, dt
 
 
+O16_HF = {"functional": "SLy4", "nucleus": {"A": 16, "Z": 8},
+          "box": {"boxSize": 18.0, "axisMeshPoints": 30},
+          "maxIterations": 500, "energyTol": 1e-3}
+
+
+def _hf_wall(with_cpu):
+    """Wall seconds to |dE| < 1 keV (the driver's stop rule, main.cpp:333-337)
+    for the 16O HF ground state (SLy4, 30^3 lattice, box 18 fm, Woods-Saxon
+    guess) in three device forms: plain FP64, mixed (FP32 PCG corrections),
+    and learned + mixed (PCG started from the trained network). Each form
+    runs twice in this process and the second run is timed (the first pays
+    the one-off stencil autotuning and allocations)."""
+    import nuclearcgm_gb300 as ng
+    from nuclearcgm_gb300 import abi, config
+    lp = None
+    wpath = os.path.join(HERE, "nuclearcgm_gb300", "data", "lp_weights.f32")
+    if os.path.exists(wpath):
+        lp = ng.LearnedPreconditioner.pretrained(wpath)
+    forms = [("fp64_gpu", abi.FP64, abi.PRECOND_JACOBI),
+             ("mixed_gpu", abi.FP32, abi.PRECOND_JACOBI)]
+    if lp is not None:
+        forms.append(("learned_mixed_gpu", abi.FP32, abi.PRECOND_LEARNED))
+    out = {"workload": "16O HF ground state, SLy4, 30^3 lattice, box 18 fm, "
+                       "|dE| < 1 keV", "unit": "s"}
+    for name, prec, pc in forms:
+        cfg = config.from_input(O16_HF, precision=prec)
+        cfg.hf_gcg.precond = pc
+        if pc == abi.PRECOND_LEARNED:
+            cfg.lp = lp.h.value
+        for rep in range(2):
+            t0 = time.perf_counter()
+            res, _ = ng.hf_run(cfg)
+            wall = time.perf_counter() - t0
+        out[name + "_s"] = round(wall, 4)
+        out[name + "_iterations"] = res.iterations
+        out[name + "_E_MeV"] = round(res.E_HF, 6)
+    if lp is None:
+        out["learned_mixed_gpu_s"] = None
+        out["learned_note"] = "no trained weights (nuclearcgm_gb300.train_lp)"
+    if with_cpu:
+        from oracle import oracle
+        from nuclearcgm_gb300 import config as cf
+        t = {}
+        for k in (1, 3):
+            c = cf.from_input(dict(O16_HF, maxIterations=k, energyTol=0.0))
+            t0 = time.perf_counter()
+            oracle.hf_run(c)
+            t[k] = time.perf_counter() - t0
+        per_it = (t[3] - t[1]) / 2
+        its = out["fp64_gpu_iterations"]
+        out["cpu_oracle_s_est"] = round(t[1] + per_it * (its - 1), 3)
+        out["cpu_sample"] = ("oracle HF runs of 1 and 3 iterations (%.2f s, "
+                             "%.2f s); estimate = 1-iteration run + %d x "
+                             "per-iteration time" % (t[1], t[3], its - 1))
+        out["cpu_cores"] = os.cpu_count()
+    return out
+
+
 def run_reference(args):
     ws, rank = _dist()
     if rank != 0:
@@ -264,6 +322,9 @@ def run_ours(args):
             traffic = json.load(open(tp)).get("dram_bytes_per_launch")
         except Exception:
             traffic = None
+    hf = None
+    if rank == 0 and not args.no_hf:
+        hf = _hf_wall(not args.no_cpu)
     cpu = None
     if rank == 0 and not args.no_cpu:
         gbs_c, dt_c = _cpu_reference(3, 1, a, f, gradf, U, W, X, 4)
@@ -295,6 +356,7 @@ def run_ours(args):
                          "gbs": round(workloads.hx_bytes(N_LAT, NCOLS, 8) /
                                       (ms64 * 1e-3) / 1e9, 2)},
         "cpu_baseline": cpu,
+        "hf_wall_to_1keV": hf,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -311,6 +373,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true",
                     help="skip the CPU-baseline sample on our arm")
+    ap.add_argument("--no-hf", action="store_true",
+                    help="skip the HF wall-time-to-convergence record")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -257,6 +257,26 @@ typedef struct ncgm_hf_result {
 int ncgm_hf_run(const ncgm_hf_config *cfg, ncgm_hf_result *res, double *spe_n,
                 double *spe_p, double *rho_n, double *rho_p, double *energies);
 
+/* C (p x q) = A^H B for complex column blocks of ctx->N rows (A: N x p,
+ * B: N x q, Eigen layout; host or device buffers): the Gram / projection
+ * products of the GCG (src/solver/solver.cpp:750-777, V.adjoint() * W).
+ * precision NCGM_FP64: FP64 CUDA cores, deterministic reduction;
+ * NCGM_FP32: tensor cores (tcgen05 kind::tf32 with split TF32 operands,
+ * FP32 accumulation over row chunks, FP64 chunk sums; FP32-level error). */
+int ncgm_gram(ncgm_ctx *ctx, const double *A, int p, const double *B, int q,
+              double *C, int precision);
+
+/* Batch of independent HF runs on one GPU (the reference runs the points of
+ * a deformation curve one after another, src/main.cpp:176-185 with
+ * Utilities::curve, src/util/utilities.cpp:71-73). Every configuration runs
+ * on its own host thread, context and stream, at most max_concurrent at a
+ * time (0: all), so the latency-bound launches of the runs overlap. Each
+ * result equals ncgm_hf_run's for that configuration. status (count ints)
+ * and rho_n / rho_p (count pointers to n^3 host doubles) may be NULL. */
+int ncgm_hf_run_batch(const ncgm_hf_config *cfgs, int count,
+                      int max_concurrent, ncgm_hf_result *res, int *status,
+                      double *const *rho_n, double *const *rho_p);
+
 /* ---- learned preconditioner (no reference counterpart) ----------------
  * The reference's GCG correction is Jacobi PCG from d = 0 on
  * (A + shift) d = x lambda - A x (src/solver/solver.cpp:723-745). With

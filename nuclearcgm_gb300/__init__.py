@@ -308,3 +308,36 @@ class LearnedPreconditioner:
     def bind(self, ctx: Context):
         """Network used by ncgm_gcg on ctx with precond = LEARNED."""
         _check(load().ncgm_set_lp(ctx.h, self.h))
+
+    def save(self, path):
+        self.params.astype(np.float32).tofile(path)
+
+    @classmethod
+    def pretrained(cls, path=None):
+        """The network trained by nuclearcgm_gb300.train_lp (data/)."""
+        path = path or os.path.join(HERE, "data", "lp_weights.f32")
+        lp = cls()
+        lp.params = np.fromfile(path, np.float32)
+        return lp
+
+
+def hf_run_batch(cfgs, max_concurrent: int = 0, densities: bool = False):
+    """Independent HF runs (e.g. the points of a deformation curve) on one
+    GPU, each on its own host thread, context and stream
+    (ncgm_hf_run_batch). Returns the list of results and, with
+    densities=True, the lists of neutron and proton densities."""
+    count = len(cfgs)
+    arr = (abi.HFConfig * count)(*cfgs)
+    res = (abi.HFResult * count)()
+    status = np.zeros(count, np.int32)
+    rn = rp = None
+    pn = pp = None
+    if densities:
+        rn = [np.zeros(c.n ** 3) for c in cfgs]
+        rp = [np.zeros(c.n ** 3) for c in cfgs]
+        pn = (C.c_void_p * count)(*[r.ctypes.data for r in rn])
+        pp = (C.c_void_p * count)(*[r.ctypes.data for r in rp])
+    _check(load().ncgm_hf_run_batch(arr, count, int(max_concurrent), res,
+                                    status.ctypes.data, pn, pp))
+    out = list(res)
+    return (out, rn, rp) if densities else out

@@ -19,6 +19,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cmath>
 #include <numeric>
 #include <vector>
@@ -73,14 +74,17 @@ __global__ void axpyCols(double2 *Y, const double2 *X, size_t N, int k,
   }
 }
 
-// per column: |AX_c - L_c X_c|^2 and Re(X_c^H AX_c)
-__global__ void colStats(const double2 *X, const double2 *AX, size_t N,
-                         const double *L, double *res2, double *xax) {
+// per column: partial sums of |AX_c - L_c X_c|^2 and Re(X_c^H AX_c) over
+// the rows of one block (grid: blocks x columns); colStatsFinish adds the
+// partials of each column in a fixed order
+__global__ void colStatsPart(const double2 *X, const double2 *AX, size_t N,
+                             const double *L, double *part, int nb) {
   __shared__ double s0[256], s1[256];
-  const int c = blockIdx.x;
+  const int c = blockIdx.y;
   const double l = L[c];
   double a = 0, b = 0;
-  for (size_t i = threadIdx.x; i < N; i += blockDim.x) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x) {
     double2 x = X[(size_t)c * N + i], y = AX[(size_t)c * N + i];
     double rx = y.x - l * x.x, ry = y.y - l * x.y;
     a += rx * rx + ry * ry;
@@ -97,9 +101,22 @@ __global__ void colStats(const double2 *X, const double2 *AX, size_t N,
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    res2[c] = s0[0];
-    xax[c] = s1[0];
+    part[((size_t)c * nb + blockIdx.x) * 2] = s0[0];
+    part[((size_t)c * nb + blockIdx.x) * 2 + 1] = s1[0];
   }
+}
+
+__global__ void colStatsFinish(const double *part, int nb, double *res2,
+                               double *xax) {
+  const int c = blockIdx.x;
+  if (threadIdx.x != 0) return;
+  double a = 0, b = 0;
+  for (int k = 0; k < nb; ++k) {
+    a += part[((size_t)c * nb + k) * 2];
+    b += part[((size_t)c * nb + k) * 2 + 1];
+  }
+  res2[c] = a;
+  xax[c] = b;
 }
 
 struct Carve {
@@ -126,7 +143,8 @@ double msSince(std::chrono::steady_clock::time_point t0) {
 static int cholQR2(ncgm_ctx *ctx, const double2 *V, int k, double2 *Q,
                    double2 *Q1, double2 *small, double2 *partials,
                    int maxChunks, int *dKeep, int *dIdx, cudaStream_t s,
-                   std::vector<int> *keptOrig = nullptr) {
+                   std::vector<int> *keptOrig = nullptr,
+                   float *tcPart = nullptr) {
   const size_t N = ctx->N;
   double2 *G = small, *R = small + (size_t)k * k, *T = small + 2 * (size_t)k * k,
           *Tk = small + 3 * (size_t)k * k;
@@ -137,7 +155,12 @@ static int cholQR2(ncgm_ctx *ctx, const double2 *V, int k, double2 *Q,
   std::vector<int> orig(k);
   std::iota(orig.begin(), orig.end(), 0);
   for (int pass = 0; pass < 2; ++pass) {
-    gram(src, N, cols, src, N, cols, N, G, cols, partials, maxChunks, s);
+    // mixed form: the first pass's Gram on the tensor cores (FP32-level),
+    // the second in FP64 so the basis is orthonormal to FP64 rounding
+    if (pass == 0 && tcPart)
+      gramTC(src, N, cols, src, N, cols, N, G, cols, tcPart, s);
+    else
+      gram(src, N, cols, src, N, cols, N, G, cols, partials, maxChunks, s);
     cholDrop(G, cols, cols, 1e-24, R, T, dKeep, s);
     if (cudaMemcpyAsync(keep.data(), dKeep, sizeof(int) * cols,
                         cudaMemcpyDeviceToHost, s) != cudaSuccess ||
@@ -177,6 +200,10 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
       1, std::min<size_t>(256, (size_t)8 * 1024 * 1024 / ((size_t)mx * mx)));
   const bool fp32 = prm.precision == NCGM_FP32;
   const bool learned = prm.precond == NCGM_PRECOND_LEARNED;
+  // mixed form: Gram products of the search space on the tensor cores
+  // (NCGM_TC_GRAM=0 keeps them in FP64)
+  const char *tcEnv = std::getenv("NCGM_TC_GRAM");
+  const bool tc = fp32 && !(tcEnv && tcEnv[0] == '0');
   if (learned && !ctx->lp) {
     setError("ncgm_gcg: learned preconditioner requested but no network set "
              "(ncgm_set_lp)");
@@ -193,6 +220,12 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
   need += (size_t)nev * 128 * 5 * sizeof(double) + 64 * 1024;
   char *base = static_cast<char *>(ctx->buf(10, need + 64 * 4096));
   if (!base) return NCGM_ERR_NOMEM;
+  float *tcPart = nullptr;
+  if (tc) {
+    tcPart = static_cast<float *>(ctx->buf(
+        11, sizeof(float) * tcGramPartialFloats(N, vmax, vmax) + 256));
+    if (!tcPart) return NCGM_ERR_NOMEM;
+  }
   Carve ar{base};
   double2 *V = ar.take<double2>(N * vmax), *Q = ar.take<double2>(N * vmax),
           *AV = ar.take<double2>(N * vmax), *Q1 = ar.take<double2>(N * vmax);
@@ -416,8 +449,9 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
         for (auto &c : hs) pcgMax = std::max(pcgMax, c.iters);
         if (learned) {
           std::vector<int> hu(nact);
-          NCGM_CUDA(cudaMemcpy(hu.data(), dUse, sizeof(int) * nact,
-                               cudaMemcpyDeviceToHost));
+          NCGM_CUDA(cudaMemcpyAsync(hu.data(), dUse, sizeof(int) * nact,
+                                    cudaMemcpyDeviceToHost, s));
+          NCGM_CUDA(cudaStreamSynchronize(s));
           for (int u : hu) lpCols += u;
         }
       }
@@ -425,7 +459,7 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
     }
     const int vcols = nconv + nact + pc + nact;
     int m = cholQR2(ctx, V, vcols, Q, Q1, Gs, partials, (int)maxChunks, dKeep,
-                    dIdx, s);
+                    dIdx, s, nullptr, tcPart);
     if (m < 0) return NCGM_ERR_CUDA;
     if (m == 0) {
       setError("ncgm_gcg: search space collapsed");
@@ -434,7 +468,10 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
     lastBasis = m;
     // Rayleigh-Ritz on A_shifted
     applyA(Q, AV, m, shift);
-    gram(Q, N, m, AV, N, m, N, Ap, m, partials, (int)maxChunks, s);
+    if (tc)
+      gramTC(Q, N, m, AV, N, m, N, Ap, m, tcPart, s);
+    else
+      gram(Q, N, m, AV, N, m, N, Ap, m, partials, (int)maxChunks, s);
     heig(Ap, m, m, Cw, Ev, dW, dPerm, dStat, s);
     const int rr = std::min(nev, m);
     gemmVC(Q, N, m, Ev, m, rr, Xn, N, N, 0.0, s);
@@ -445,7 +482,9 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
     std::vector<double> Lnew(rr);
     NCGM_CUDA(cudaStreamSynchronize(s));
     int hstat = 0;
-    cudaMemcpy(&hstat, dStat, sizeof(int), cudaMemcpyDeviceToHost);
+    NCGM_CUDA(cudaMemcpyAsync(&hstat, dStat, sizeof(int),
+                              cudaMemcpyDeviceToHost, s));
+    NCGM_CUDA(cudaStreamSynchronize(s));
     if (hstat != 0) {
       setError("ncgm_gcg: projected eigensolver did not converge");
       return NCGM_ERR_EIG;
@@ -453,7 +492,12 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
     for (int i = 0; i < rr; ++i) Lnew[i] = hw[i] - shift;
     NCGM_CUDA(cudaMemcpyAsync(dL, Lnew.data(), sizeof(double) * rr,
                               cudaMemcpyHostToDevice, s));
-    colStats<<<rr, 256, 0, s>>>(Xn, AXn, N, dL, dRes, dXax);
+    {
+      const int nb = pcgBlocks(N);
+      double *part = reinterpret_cast<double *>(partials);
+      colStatsPart<<<dim3(nb, rr), 256, 0, s>>>(Xn, AXn, N, dL, part, nb);
+      colStatsFinish<<<rr, 32, 0, s>>>(part, nb, dRes, dXax);
+    }
     NCGM_CUDA(cudaMemcpyAsync(hres.data(), dRes, sizeof(double) * rr,
                               cudaMemcpyDeviceToHost, s));
     NCGM_CUDA(cudaMemcpyAsync(hxax.data(), dXax, sizeof(double) * rr,
@@ -529,7 +573,8 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
   NCGM_CUDA(cudaGetLastError());
   if (stats) {
     int live = 0;
-    cudaMemcpy(&live, dLive, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaMemcpyAsync(&live, dLive, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
     stats->iterations = iterations;
     stats->converged = nconv;
     stats->pcg_steps_max = pcgMax;
@@ -609,3 +654,57 @@ extern "C" int ncgm_gcg(ncgm_ctx *ctx, int species, const double *X_init,
     return NCGM_ERR_ARG;
   }
 }
+
+extern "C" int ncgm_gram(ncgm_ctx *ctx, const double *A, int p,
+                         const double *B, int q, double *C, int precision) {
+  if (!ctx || !A || !B || !C || p < 1 || q < 1 || p > 4096 || q > 4096 ||
+      (precision != NCGM_FP64 && precision != NCGM_FP32)) {
+    setError("ncgm_gram: bad argument");
+    return NCGM_ERR_ARG;
+  }
+  const size_t N = ctx->N;
+  cudaStream_t s = ctx->stream;
+  auto stage = [&](const double *h, int cols, int slot) -> const double2 * {
+    if (isDevicePtr(h)) return reinterpret_cast<const double2 *>(h);
+    auto *d = static_cast<double2 *>(ctx->buf(slot, N * cols * sizeof(double2)));
+    if (d && cudaMemcpyAsync(d, h, N * cols * sizeof(double2),
+                             cudaMemcpyHostToDevice, s) != cudaSuccess)
+      return nullptr;
+    return d;
+  };
+  const double2 *dA = stage(A, p, 26), *dB = stage(B, q, 27);
+  if (!dA || !dB) return NCGM_ERR_NOMEM;
+  const bool devOut = isDevicePtr(C);
+  double2 *dC = devOut ? reinterpret_cast<double2 *>(C)
+                       : static_cast<double2 *>(
+                             ctx->buf(28, (size_t)p * q * sizeof(double2)));
+  if (!dC) return NCGM_ERR_NOMEM;
+  if (precision == NCGM_FP32) {
+    float *part = static_cast<float *>(
+        ctx->buf(29, sizeof(float) * tcGramPartialFloats(N, p, q) + 256));
+    if (!part) return NCGM_ERR_NOMEM;
+    gramTC(dA, N, p, dB, N, q, N, dC, p, part, s);
+  } else {
+    const int chunks = gramMaxChunks();
+    auto *part = static_cast<double2 *>(
+        ctx->buf(29, sizeof(double2) * (size_t)chunks * p * q));
+    if (!part) return NCGM_ERR_NOMEM;
+    gram(dA, N, p, dB, N, q, N, dC, p, part, chunks, s);
+  }
+  if (!devOut)
+    NCGM_CUDA(cudaMemcpyAsync(C, dC, (size_t)p * q * sizeof(double2),
+                              cudaMemcpyDeviceToHost, s));
+  NCGM_CUDA(cudaStreamSynchronize(s));
+  NCGM_CUDA(cudaGetLastError());
+  int flag = 0;
+  if (precision == NCGM_FP32) {
+    NCGM_CUDA(cudaMemcpy(&flag, tcGramErrWord(), sizeof(int),
+                         cudaMemcpyDeviceToHost));
+    if (flag) {
+      setError("ncgm_gram: tensor-core kernel wait timed out");
+      return NCGM_ERR_TIMEOUT;
+    }
+  }
+  return NCGM_OK;
+}
+

@@ -15,6 +15,8 @@
 #include "ncgm_internal.cuh"
 
 #include <algorithm>
+#include <atomic>
+#include <thread>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -868,7 +870,9 @@ void quadDef(Run &R, double &beta, double &gamma) {
   // output only: beta2 and gamma from the total density
   const int nblk = 120;
   int kinds[2] = {6, 3};
-  cudaMemcpy(R.ismall, kinds, sizeof(kinds), cudaMemcpyHostToDevice);
+  cudaMemcpyAsync(R.ismall, kinds, sizeof(kinds), cudaMemcpyHostToDevice,
+                  R.s);
+  cudaStreamSynchronize(R.s); // kinds is a stack array
   constraintQ<<<nblk, 256, 0, R.s>>>(R.rho[0], R.rho[1], R.n, R.a, R.h,
                                      R.ismall, 2, R.small);
   std::vector<double> part(2 * nblk);
@@ -1115,8 +1119,13 @@ int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
   res.t_pairing_s = R.tPair;
   if (spe_n) std::copy(R.sp[0].e.begin(), R.sp[0].e.end(), spe_n);
   if (spe_p) std::copy(R.sp[1].e.begin(), R.sp[1].e.end(), spe_p);
-  if (rho_n) cudaMemcpy(rho_n, R.rho[0], sizeof(double) * R.ns, cudaMemcpyDeviceToHost);
-  if (rho_p) cudaMemcpy(rho_p, R.rho[1], sizeof(double) * R.ns, cudaMemcpyDeviceToHost);
+  if (rho_n)
+    NCGM_CUDA(cudaMemcpyAsync(rho_n, R.rho[0], sizeof(double) * R.ns,
+                              cudaMemcpyDeviceToHost, R.s));
+  if (rho_p)
+    NCGM_CUDA(cudaMemcpyAsync(rho_p, R.rho[1], sizeof(double) * R.ns,
+                              cudaMemcpyDeviceToHost, R.s));
+  NCGM_TRY(sync(R));
   res.wall_s = now() - tStart;
   return NCGM_OK;
 }
@@ -1218,3 +1227,51 @@ extern "C" int ncgm_poisson(ncgm_ctx *ctx, const double *rhoP, int Z,
     return NCGM_ERR_ARG;
   }
 }
+
+// Batch of independent runs (constraint points of a deformation curve, or
+// different nuclei) on one GPU: every configuration runs the full HF loop on
+// its own host thread, context and non-blocking stream, so the small,
+// latency-bound launches of the different runs overlap on the device. Each
+// run is bit-for-bit the run ncgm_hf_run gives for that configuration.
+extern "C" int ncgm_hf_run_batch(const ncgm_hf_config *cfgs, int count,
+                                 int max_concurrent, ncgm_hf_result *res,
+                                 int *status, double *const *rho_n,
+                                 double *const *rho_p) {
+  if (!cfgs || !res || count < 1) {
+    setError("ncgm_hf_run_batch: bad argument");
+    return NCGM_ERR_ARG;
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    setError("ncgm_hf_run_batch: no CUDA device");
+    return NCGM_ERR_CUDA;
+  }
+  const int width =
+      max_concurrent > 0 ? std::min(max_concurrent, count) : count;
+  std::vector<int> st(count, NCGM_OK);
+  std::vector<std::string> err(count);
+  std::atomic<int> next{0};
+  auto worker = [&]() {
+    cudaSetDevice(dev);
+    for (int i = next++; i < count; i = next++) {
+      st[i] = ncgm_hf_run(&cfgs[i], &res[i], nullptr, nullptr,
+                          rho_n ? rho_n[i] : nullptr,
+                          rho_p ? rho_p[i] : nullptr, nullptr);
+      if (st[i] != NCGM_OK) err[i] = ncgm_last_error();
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 0; t < width; ++t) pool.emplace_back(worker);
+  for (auto &t : pool) t.join();
+  int first = NCGM_OK;
+  for (int i = 0; i < count; ++i) {
+    if (status) status[i] = st[i];
+    if (st[i] != NCGM_OK && first == NCGM_OK) {
+      first = st[i];
+      setError("ncgm_hf_run_batch: configuration " + std::to_string(i) +
+               ": " + err[i]);
+    }
+  }
+  return first;
+}
+

@@ -187,8 +187,14 @@ __global__ void cholDropKernel(const double2 *G, int ldg, int m,
 // m/2 disjoint (p,q) pairs at once, m-1 rounds per sweep) on a Hermitian
 // m x m matrix whose lower triangle is read. A, Vm: m x m workspaces;
 // w: eigenvalues ascending; Vm: eigenvectors in the same order.
-__global__ void heigKernel(const double2 *Ain, int lda, int m, double2 *A,
-                           double2 *Vm, double *w, int *perm, int *status) {
+__global__ void heigKernel(const double2 *Ain, int lda, int m, double2 *Ag,
+                           double2 *Vg, double *w, int *perm, int *status,
+                           int useSmem) {
+  // working copies of A and V in shared memory when they fit (m <= 64),
+  // else in the global work buffers
+  extern __shared__ double2 hsm[];
+  double2 *A = useSmem ? hsm : Ag;
+  double2 *Vm = useSmem ? hsm + (size_t)m * m : Vg;
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int e = tid; e < m * m; e += nt) {
     int i = e % m, j = e / m;
@@ -206,7 +212,7 @@ __global__ void heigKernel(const double2 *Ain, int lda, int m, double2 *A,
   __shared__ int P[256], Q[256];
   __shared__ double C[256], S[256];
   __shared__ double2 E[256];
-  __shared__ double red[256];
+  __shared__ double red[512]; // blockDim.x <= 512
   __syncthreads();
   double fro = 0;
   {
@@ -336,7 +342,7 @@ __global__ void heigKernel(const double2 *Ain, int lda, int m, double2 *A,
     A[e] = Vm[(size_t)perm[c] * m + r];
   }
   __syncthreads();
-  for (int e = tid; e < m * m; e += nt) Vm[e] = A[e];
+  for (int e = tid; e < m * m; e += nt) Vg[e] = A[e];
 }
 
 } // namespace
@@ -370,13 +376,13 @@ void gemmVC(const double2 *V, size_t ldv, int m, const double2 *Cm, int ldc,
     return;
   }
   size_t smem = (size_t)m * k * sizeof(double2);
-  static bool attr = false;
-  if (!attr) {
+  static const bool attr = [] {
     cudaFuncSetAttribute(gemmVCKernel,
                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                          200 * 1024);
-    attr = true;
-  }
+    return true;
+  }();
+  (void)attr;
   dim3 grid((unsigned)((N + 127) / 128), (k + 7) / 8);
   gemmVCKernel<<<grid, 128, smem, s>>>(V, ldv, m, Cm, ldc, k, Y, ldy, N, beta);
 }
@@ -389,7 +395,16 @@ void cholDrop(const double2 *G, int ldg, int m, double dropTol, double2 *R,
 void heig(const double2 *A, int lda, int m, double2 *work, double2 *V,
           double *w, int *perm, int *status, cudaStream_t s) {
   // the round-robin tables hold up to 256 pairs (m <= 512)
-  heigKernel<<<1, 256, 0, s>>>(A, lda, m, work, V, w, perm, status);
+  static const bool attr = [] {
+    cudaFuncSetAttribute(heigKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         2 * 64 * 64 * (int)sizeof(double2));
+    return true;
+  }();
+  (void)attr;
+  const bool sm = m <= 64;
+  const size_t smem = sm ? 2 * (size_t)m * m * sizeof(double2) : 0;
+  heigKernel<<<1, 512, smem, s>>>(A, lda, m, work, V, w, perm, status,
+                                  sm ? 1 : 0);
 }
 
 } // namespace ncgm

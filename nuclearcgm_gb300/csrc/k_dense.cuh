@@ -11,6 +11,14 @@ void gram(const double2 *A, size_t lda, int p, const double2 *B, size_t ldb,
           int q, size_t N, double2 *C, int ldc, double2 *partials,
           int maxChunks, cudaStream_t s);
 int gramMaxChunks();
+// C = A^H B on the tensor cores (tcgen05 kind::tf32, split TF32 products,
+// FP32 accumulation over row chunks, FP64 chunk sums; k_tcgram.cu). part:
+// tcGramPartialFloats(N, p, q) floats.
+void gramTC(const double2 *A, size_t lda, int p, const double2 *B, size_t ldb,
+            int q, size_t N, double2 *C, int ldc, float *part,
+            cudaStream_t s);
+size_t tcGramPartialFloats(size_t N, int p, int q);
+int *tcGramErrWord();
 // Y = V C + beta Y (V: N x m, C: m x k with m*k*16 bytes <= 200 KB).
 void gemmVC(const double2 *V, size_t ldv, int m, const double2 *C, int ldc,
             int k, double2 *Y, size_t ldy, size_t N, double beta,

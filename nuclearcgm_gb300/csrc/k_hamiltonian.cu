@@ -147,11 +147,13 @@ __global__ void cvt32to64(const float2 *in, double2 *out, size_t count) {
 }
 
 int *errWordImpl() {
-  static int *d = nullptr;
-  if (!d) {
-    cudaMalloc(&d, sizeof(int));
-    cudaMemset(d, 0, sizeof(int));
-  }
+  // thread-safe one-time allocation (concurrent contexts on host threads)
+  static int *d = [] {
+    int *p = nullptr;
+    if (cudaMalloc(&p, sizeof(int)) == cudaSuccess)
+      cudaMemset(p, 0, sizeof(int));
+    return p;
+  }();
   return d;
 }
 

@@ -5,7 +5,7 @@
 // correction form that is (A + shift) d = r, r = x lambda - A x, w = x + d.
 // Here a small 3-D convolutional network maps r (one real component at a
 // time, scaled to unit RMS) together with the local fields (U + shift and
-// the effective-mass field f) to an estimate d0 of d. The PCG then starts
+// the kinetic coefficient f / h^2) to an estimate d0 of d. The PCG then starts
 // from alpha d0 instead of 0, alpha the step along d0 that minimises the CG
 // energy (so the start is never worse than 0 in the A-norm the PCG
 // minimises); a column with alpha <= 0 starts from 0 as before. The
@@ -34,6 +34,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <vector>
 
 namespace ncgm {
@@ -43,7 +44,9 @@ bool isDevicePtr(const void *p);
 namespace {
 
 constexpr float kU = 50.f;   // MeV: scale of U + shift at the input
-constexpr float kF = 20.7f;  // MeV fm^2: scale of f at the input
+// MeV: scale of f / h^2 at the input (20.7 MeV fm^2 at h = 0.5 fm), so the
+// network sees the kinetic scale of the lattice it runs on
+constexpr float kK = 82.8f;
 constexpr float kE = 10.f;   // MeV: d is predicted as d kE / rms(r)
 constexpr int kNL = 8;
 
@@ -377,7 +380,8 @@ __global__ void residualRmsKernel(const double2 *__restrict__ X,
 }
 
 // network inputs of instance b = 4 j + c: r_c / rms, (U + UC + shift) / kU,
-// f / kF (U + UC = c0 - 7.5 c1 and f = c1 h^2 from the coefficient table)
+// (f / h^2) / kK (U + UC = c0 - 7.5 c1 and f / h^2 = c1 from the
+// coefficient table)
 __global__ void packInputKernel(const double2 *__restrict__ X,
                                 const double2 *__restrict__ AX,
                                 const double *__restrict__ lam,
@@ -399,7 +403,7 @@ __global__ void packInputKernel(const double2 *__restrict__ X,
     dst[p] = s > 0.f ? (float)(r / s) : 0.f;
     const double c0 = coef[8 * p], c1 = coef[8 * p + 1];
     dst[ns + p] = (float)((c0 - 7.5 * c1 + shift) / kU);
-    dst[2 * ns + p] = (float)(c1 * h2 / kF);
+    dst[2 * ns + p] = (float)(c1 / kK);
   }
 }
 
@@ -505,6 +509,7 @@ struct ncgm_lp {
   float *dLoss = nullptr;
   int *dIdx = nullptr;
   int idxCap = 0;
+  std::mutex mu; // one user at a time (batched runs may share a network)
 };
 
 namespace ncgm {
@@ -582,13 +587,13 @@ void launchConv(const float *in, int Cin, int D, int B,
                 int layerCout, cudaStream_t s) {
   const int V = D * D * D;
   const size_t smem = (size_t)Cin * K * K * K * COT * sizeof(float);
-  static bool attr = false;
-  if (!attr) {
+  static const bool attr = [] {
     cudaFuncSetAttribute(convKernel<K, COT>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                          100 * 1024);
-    attr = true;
-  }
+    return true;
+  }();
+  (void)attr;
   dim3 grid((V + 127) / 128, (Cout + COT - 1) / COT, B);
   convKernel<K, COT><<<grid, 128, smem, s>>>(in, Cin, D, Wq, bias, Cout, out,
                                              relu ? 1 : 0, transposed ? 1 : 0,
@@ -786,6 +791,7 @@ int lpInitialCorrection(ncgm_lp *lp, ncgm_ctx *ctx, int species,
     setError("learned preconditioner: no network bound to the context");
     return NCGM_ERR_ARG;
   }
+  std::lock_guard<std::mutex> lock(lp->mu);
   const int n = ctx->n;
   const size_t ns = ctx->ns, N = ctx->N;
   const int B = 4 * ncols;
@@ -998,6 +1004,7 @@ int ncgm_lp_collect(ncgm_lp *lp, ncgm_ctx *ctx, int species, const double *X,
     return NCGM_ERR_ARG;
   }
   if (!onLpDevice(lp)) return NCGM_ERR_ARG;
+  std::lock_guard<std::mutex> lock(lp->mu);
   cudaStream_t s = ctx->stream;
   const size_t N = ctx->N, ns = ctx->ns;
   // device copies of X and the exact-correction workspace

@@ -25,6 +25,8 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
+#include <string>
 #include <cstdlib>
 #include <vector>
 
@@ -111,6 +113,92 @@ __device__ __forceinline__ bool mbarWaitSleep(uint64_t *bar, uint32_t phase,
     if (done) return true;
   }
   return false;
+}
+
+// ---- packed FP32 pair arithmetic (f32x2: one instruction, two lanes) ----
+using f2x = unsigned long long;
+__device__ __forceinline__ f2x pk(float a, float b) {
+  f2x r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float2 upk(f2x v) {
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+  return r;
+}
+__device__ __forceinline__ f2x add2(f2x a, f2x b) {
+  f2x r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2x sub2(f2x a, f2x b) {
+  f2x r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2x mul2(f2x a, f2x b) {
+  f2x r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c) {
+  f2x r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+__device__ __forceinline__ f2x bc(float a) { return pk(a, a); }
+
+// pointH (stencil_core.cuh) with each spin component held as one (re, im)
+// pair: the kinetic, derivative and gradient terms are real coefficients
+// times pairs; the spin-orbit matrix is split as A + iB (A, B real), so
+// (A + iB) D = A D + i (B D) and only one i-rotation per spin is needed.
+__device__ __forceinline__ float4 pointH2(const float4 ca, const float4 cb,
+                                          float shift, float4 v, float4 xp1,
+                                          float4 xm1, float4 xp2, float4 xm2,
+                                          float4 yp1, float4 ym1, float4 yp2,
+                                          float4 ym2, float4 zp1, float4 zm1,
+                                          float4 zp2, float4 zm2) {
+  const f2x D = bc(ca.x + shift), NF = bc(-ca.y);
+  const f2x GX = bc(ca.z), GY = bc(ca.w), GZ = bc(cb.x);
+  const f2x WX = bc(cb.y), WY = bc(cb.z), WZ = bc(cb.w);
+  const f2x NWX = bc(-cb.y), NWY = bc(-cb.z), NWZ = bc(-cb.w);
+  const f2x C43 = bc(4.0f / 3.0f), NC112 = bc(-1.0f / 12.0f), EIGHT = bc(8.f);
+  f2x o[2], Dx[2], Dy[2], Dz[2];
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    auto A = [s](float4 q) { return s ? pk(q.z, q.w) : pk(q.x, q.y); };
+    const f2x a_xp1 = A(xp1), a_xm1 = A(xm1), a_xp2 = A(xp2), a_xm2 = A(xm2);
+    const f2x a_yp1 = A(yp1), a_ym1 = A(ym1), a_yp2 = A(yp2), a_ym2 = A(ym2);
+    const f2x a_zp1 = A(zp1), a_zm1 = A(zm1), a_zp2 = A(zp2), a_zm2 = A(zm2);
+    f2x s1 = add2(add2(add2(a_xp1, a_xm1), add2(a_yp1, a_ym1)),
+                  add2(a_zp1, a_zm1));
+    f2x s2 = add2(add2(add2(a_xp2, a_xm2), add2(a_yp2, a_ym2)),
+                  add2(a_zp2, a_zm2));
+    f2x t = fma2(C43, s1, mul2(NC112, s2));
+    f2x os = fma2(NF, t, mul2(D, A(v)));
+    Dx[s] = fma2(EIGHT, sub2(a_xp1, a_xm1), sub2(a_xm2, a_xp2));
+    Dy[s] = fma2(EIGHT, sub2(a_yp1, a_ym1), sub2(a_ym2, a_yp2));
+    Dz[s] = fma2(EIGHT, sub2(a_zp1, a_zm1), sub2(a_zm2, a_zp2));
+    os = fma2(GX, Dx[s], os);
+    os = fma2(GY, Dy[s], os);
+    o[s] = fma2(GZ, Dz[s], os);
+  }
+  // spin-orbit: real parts (A) into o, imaginary parts (B) into u, o += i u
+  o[0] = fma2(NWZ, Dx[1], o[0]);
+  o[0] = fma2(WX, Dz[1], o[0]);
+  f2x u0 = mul2(WY, Dx[0]);
+  u0 = fma2(NWX, Dy[0], u0);
+  u0 = fma2(WZ, Dy[1], u0);
+  u0 = fma2(NWY, Dz[1], u0);
+  o[1] = fma2(WZ, Dx[0], o[1]);
+  o[1] = fma2(NWX, Dz[0], o[1]);
+  f2x u1 = mul2(NWY, Dx[1]);
+  u1 = fma2(WZ, Dy[0], u1);
+  u1 = fma2(WX, Dy[1], u1);
+  u1 = fma2(NWY, Dz[0], u1);
+  const float2 p0 = upk(o[0]), p1 = upk(o[1]), q0 = upk(u0), q1 = upk(u1);
+  return make_float4(p0.x - q0.y, p0.y + q0.x, p1.x - q1.y, p1.y + q1.x);
 }
 
 // Warp-specialised form. Warp 0 is the producer: one lane issues the TMA
@@ -256,14 +344,10 @@ __global__ void __launch_bounds__(512, 1)
       for (int t = 0; t < PPT; ++t)
         if (qv[t] < tyn) {
           const int l = lr[t];
-          float c[8] = {ca[t].x, ca[t].y, ca[t].z, ca[t].w,
-                        cbv[t].x, cbv[t].y, cbv[t].z, cbv[t].w};
-          auto S = [](float4 v) { return Spinor<float>{v.x, v.y, v.z, v.w}; };
-          Spinor<float> o = pointH<float>(
-              c, A.shift, S(pc[l]), S(pc[l + 1]), S(pc[l - 1]), S(pc[l + 2]),
-              S(pc[l - 2]), S(pc[l + W]), S(pc[l - W]), S(pc[l + 2 * W]),
-              S(pc[l - 2 * W]), S(pp1[l]), S(pm1[l]), S(pp2[l]), S(pm2[l]));
-          Yc[pbase + qv[t]] = make_float4(o.r0, o.i0, o.r1, o.i1);
+          Yc[pbase + qv[t]] = pointH2(
+              ca[t], cbv[t], A.shift, pc[l], pc[l + 1], pc[l - 1], pc[l + 2],
+              pc[l - 2], pc[l + W], pc[l - W], pc[l + 2 * W], pc[l - 2 * W],
+              pp1[l], pm1[l], pp2[l], pm2[l]);
         }
       // release the planes this warp no longer needs: seq s0, or all five at
       // the end of the run
@@ -274,92 +358,6 @@ __global__ void __launch_bounds__(512, 1)
       }
     }
   }
-}
-
-// ---- packed FP32 pair arithmetic (f32x2: one instruction, two lanes) ----
-using f2x = unsigned long long;
-__device__ __forceinline__ f2x pk(float a, float b) {
-  f2x r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-  return r;
-}
-__device__ __forceinline__ float2 upk(f2x v) {
-  float2 r;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
-  return r;
-}
-__device__ __forceinline__ f2x add2(f2x a, f2x b) {
-  f2x r;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ f2x sub2(f2x a, f2x b) {
-  f2x r;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ f2x mul2(f2x a, f2x b) {
-  f2x r;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c) {
-  f2x r;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-  return r;
-}
-__device__ __forceinline__ f2x bc(float a) { return pk(a, a); }
-
-// pointH (stencil_core.cuh) with each spin component held as one (re, im)
-// pair: the kinetic, derivative and gradient terms are real coefficients
-// times pairs; the spin-orbit matrix is split as A + iB (A, B real), so
-// (A + iB) D = A D + i (B D) and only one i-rotation per spin is needed.
-__device__ __forceinline__ float4 pointH2(const float4 ca, const float4 cb,
-                                          float shift, float4 v, float4 xp1,
-                                          float4 xm1, float4 xp2, float4 xm2,
-                                          float4 yp1, float4 ym1, float4 yp2,
-                                          float4 ym2, float4 zp1, float4 zm1,
-                                          float4 zp2, float4 zm2) {
-  const f2x D = bc(ca.x + shift), NF = bc(-ca.y);
-  const f2x GX = bc(ca.z), GY = bc(ca.w), GZ = bc(cb.x);
-  const f2x WX = bc(cb.y), WY = bc(cb.z), WZ = bc(cb.w);
-  const f2x NWX = bc(-cb.y), NWY = bc(-cb.z), NWZ = bc(-cb.w);
-  const f2x C43 = bc(4.0f / 3.0f), NC112 = bc(-1.0f / 12.0f), EIGHT = bc(8.f);
-  f2x o[2], Dx[2], Dy[2], Dz[2];
-#pragma unroll
-  for (int s = 0; s < 2; ++s) {
-    auto A = [s](float4 q) { return s ? pk(q.z, q.w) : pk(q.x, q.y); };
-    const f2x a_xp1 = A(xp1), a_xm1 = A(xm1), a_xp2 = A(xp2), a_xm2 = A(xm2);
-    const f2x a_yp1 = A(yp1), a_ym1 = A(ym1), a_yp2 = A(yp2), a_ym2 = A(ym2);
-    const f2x a_zp1 = A(zp1), a_zm1 = A(zm1), a_zp2 = A(zp2), a_zm2 = A(zm2);
-    f2x s1 = add2(add2(add2(a_xp1, a_xm1), add2(a_yp1, a_ym1)),
-                  add2(a_zp1, a_zm1));
-    f2x s2 = add2(add2(add2(a_xp2, a_xm2), add2(a_yp2, a_ym2)),
-                  add2(a_zp2, a_zm2));
-    f2x t = fma2(C43, s1, mul2(NC112, s2));
-    f2x os = fma2(NF, t, mul2(D, A(v)));
-    Dx[s] = fma2(EIGHT, sub2(a_xp1, a_xm1), sub2(a_xm2, a_xp2));
-    Dy[s] = fma2(EIGHT, sub2(a_yp1, a_ym1), sub2(a_ym2, a_yp2));
-    Dz[s] = fma2(EIGHT, sub2(a_zp1, a_zm1), sub2(a_zm2, a_zp2));
-    os = fma2(GX, Dx[s], os);
-    os = fma2(GY, Dy[s], os);
-    o[s] = fma2(GZ, Dz[s], os);
-  }
-  // spin-orbit: real parts (A) into o, imaginary parts (B) into u, o += i u
-  o[0] = fma2(NWZ, Dx[1], o[0]);
-  o[0] = fma2(WX, Dz[1], o[0]);
-  f2x u0 = mul2(WY, Dx[0]);
-  u0 = fma2(NWX, Dy[0], u0);
-  u0 = fma2(WZ, Dy[1], u0);
-  u0 = fma2(NWY, Dz[1], u0);
-  o[1] = fma2(WZ, Dx[0], o[1]);
-  o[1] = fma2(NWX, Dz[0], o[1]);
-  f2x u1 = mul2(NWY, Dx[1]);
-  u1 = fma2(WZ, Dy[0], u1);
-  u1 = fma2(WX, Dy[1], u1);
-  u1 = fma2(NWY, Dz[0], u1);
-  const float2 p0 = upk(o[0]), p1 = upk(o[1]), q0 = upk(u0), q1 = upk(u1);
-  return make_float4(p0.x - q0.y, p0.y + q0.x, p1.x - q1.y, p1.y + q1.x);
 }
 
 // z-marching form. Same producer and plane sequence as stencilStream32, but
@@ -590,16 +588,16 @@ StreamKernel pickMarch(int W) {
 }
 // kind 0: stencilStream32 with `ppt` points per thread; kind 1: z-marching
 StreamKernel pickKernel(int kind, int ppt, int W) {
-  static bool attr = false;
-  if (!attr) {
+  static const bool attr = [] {
     for (int w : kWidths) {
       cudaFuncSetAttribute(pickW<1>(w), cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
       cudaFuncSetAttribute(pickW<2>(w), cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
       cudaFuncSetAttribute(pickW<4>(w), cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
       cudaFuncSetAttribute(pickMarch(w), cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     }
-    attr = true;
-  }
+    return true;
+  }();
+  (void)attr;
   if (kind == 1) return pickMarch(W);
   if (ppt == 1) return pickW<1>(W);
   if (ppt == 2) return pickW<2>(W);
@@ -607,15 +605,16 @@ StreamKernel pickKernel(int kind, int ppt, int W) {
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encodeFn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    PFN_cuTensorMapEncodeTiled_v12000 f = nullptr;
     cudaDriverEntryPointQueryResult q;
     void *p = nullptr;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
                                          cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  }
+      f = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    return f;
+  }();
   return fn;
 }
 
@@ -625,9 +624,11 @@ struct MapEntry {
   CUtensorMap map;
 };
 std::vector<MapEntry> g_maps;
+std::mutex g_mapsMutex; // contexts may run on several host threads
 
 // 5-D map of X: dims (4 floats, i, j, k, col), box (4, n+4, TY+4, 1, 1).
 bool tensorMapFor(const void *X, int n, int ncols, int TY, CUtensorMap *out) {
+  std::lock_guard<std::mutex> lock(g_mapsMutex);
   for (auto &e : g_maps)
     if (e.ptr == X && e.n == n && e.ncols == ncols && e.TY == TY) {
       *out = e.map;
@@ -665,13 +666,12 @@ size_t kernelSmem(int kind, int n, int TY, int ring, int threads) {
 }
 
 int smCount() {
-  static int c = 0;
-  if (!c) {
-    int dev = 0;
+  static const int c = [] {
+    int dev = 0, v = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev);
-    if (c <= 0) c = 1;
-  }
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 1;
+  }();
   return c;
 }
 
@@ -734,11 +734,15 @@ bool launchStream(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
   return true;
 }
 
+// Tuned launch shapes, one per lattice size (and shape override string):
+// contexts on the same lattice share the first context's measurement.
 struct TunedShape {
-  ncgm_ctx *ctx;
+  int n;
+  std::string env;
   Shape s;
 };
 std::vector<TunedShape> g_tuned;
+std::mutex g_tunedMutex;
 
 Shape defaultShape(int n) {
   Shape s{n, 8, 4, 1, 0};  // ring: a power of two
@@ -813,37 +817,33 @@ static Shape tune(ncgm_ctx *ctx, int species, int ncols) {
 
 void applyH32(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
               int ncols, float shift, cudaStream_t s) {
-  Shape *sh = nullptr;
-  for (auto &t : g_tuned)
-    if (t.ctx == ctx) sh = &t.s;
-  if (!sh) {
-    g_tuned.push_back({ctx, defaultShape(ctx->n)});
-    // NCGM_STENCIL_SHAPE="rows,ring,ppt,ctasPerSM[,kind]" fixes the shape
-    Shape tuned{}, fixed{};
-    int th = 0;
-    const char *env = std::getenv("NCGM_STENCIL_SHAPE");
-    if (env && std::sscanf(env, "%d,%d,%d,%d,%d", &fixed.TY, &fixed.ring,
-                           &fixed.ppt, &fixed.ctasPerSM, &fixed.kind) >= 4 &&
-        validShape(ctx->n, fixed, th))
-      tuned = fixed;
-    else
-      tuned = tune(ctx, species, ncols);
+  // NCGM_STENCIL_SHAPE="rows,ring,ppt,ctasPerSM[,kind]" fixes the shape
+  const char *envp = std::getenv("NCGM_STENCIL_SHAPE");
+  const std::string env = envp ? envp : "";
+  Shape sh{};
+  {
+    std::lock_guard<std::mutex> lock(g_tunedMutex);
+    bool found = false;
     for (auto &t : g_tuned)
-      if (t.ctx == ctx) {
-        t.s = tuned;
-        sh = &t.s;
+      if (t.n == ctx->n && t.env == env) {
+        sh = t.s;
+        found = true;
       }
-  }
-  if (!launchStream(ctx, species, X, Y, ncols, shift, s, *sh))
-    setError("FP32 stencil: launch shape or tensor map unavailable");
-}
-
-void forgetStencilShape(ncgm_ctx *ctx) {
-  for (size_t i = 0; i < g_tuned.size(); ++i)
-    if (g_tuned[i].ctx == ctx) {
-      g_tuned.erase(g_tuned.begin() + i);
-      return;
+    if (!found) {
+      Shape fixed{};
+      int th = 0;
+      if (!env.empty() &&
+          std::sscanf(env.c_str(), "%d,%d,%d,%d,%d", &fixed.TY, &fixed.ring,
+                      &fixed.ppt, &fixed.ctasPerSM, &fixed.kind) >= 4 &&
+          validShape(ctx->n, fixed, th))
+        sh = fixed;
+      else
+        sh = tune(ctx, species, ncols);
+      g_tuned.push_back({ctx->n, env, sh});
     }
+  }
+  if (!launchStream(ctx, species, X, Y, ncols, shift, s, sh))
+    setError("FP32 stencil: launch shape or tensor map unavailable");
 }
 
 } // namespace ncgm

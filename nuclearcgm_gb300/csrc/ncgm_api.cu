@@ -130,7 +130,6 @@ int ncgm_create(ncgm_ctx **out, int n, double a, int max_cols, int flags) {
 int ncgm_destroy(ncgm_ctx *ctx) {
   if (!ctx) return NCGM_OK;
   cudaStreamSynchronize(ctx->stream);
-  forgetStencilShape(ctx);
   for (auto &b : ctx->bufs)
     if (b.first) cudaFree(b.first);
   for (auto &s : ctx->sp) {

@@ -81,8 +81,6 @@ void applyH64(ncgm_ctx *ctx, int species, const double2 *X, double2 *Y,
               int ncols, double shift, cudaStream_t s);
 void applyH32(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
               int ncols, float shift, cudaStream_t s);
-// Drops the FP32 stencil launch shape tuned for a context (on destroy).
-void forgetStencilShape(ncgm_ctx *ctx);
 // Non-zero when a stencil's bounded wait gave up since the last reset.
 int stencilErrorFlag();
 

@@ -11,7 +11,7 @@ are checked against finite differences on the CPU.
 
 Network (per instance: one real component of one residual column):
   input x: 3 channels on the n^3 lattice (residual r/s, (U+shift)/50,
-  f/20.7); levels D0 = n, D(l+1) = (Dl + 1) // 2.
+  (f/h^2)/82.8); levels D0 = n, D(l+1) = (Dl + 1) // 2.
     e0 = relu(conv3(x;  W0 3->16))            D0
     e1 = relu(conv3(pool(e0); W1 16->16))     D1
     e2 = relu(conv3(pool(e1); W2 16->32))     D2

@@ -166,3 +166,31 @@ def test_o16_bcs_fixed_point():
     assert abs(rg.lambda_n - ro.lambda_n) < 1e-4
     assert np.abs(og["spe_n"] - oo["spe_n"]).max() < 1e-4
     assert np.abs(og["rho_n"] - oo["rho_n"]).max() < 1e-6
+
+
+def test_o16_hfb_fixed_point():
+    """HFB (iteration_data.cpp:605-850: kappa field, Delta matrix, 2M x 2M
+    quasiparticle problem, lambda bisection, natural orbitals) with the
+    same basis rule as the BCS test; the oracle settles to ~1e-6 MeV per
+    iteration by 200 iterations."""
+    data = {"functional": "SKMstar", "nucleus": {"A": 16, "Z": 8},
+            "box": {"boxSize": 16.5, "axisMeshPoints": 12},
+            "pairing": {"type": "HFB", "HFbasisSize": 14, "V0": 800.0,
+                        "window": 5.0},
+            "maxIterations": 200, "energyTol": 1e-8}
+    _, rg, og, ro, oo = _run_both(data, cg_tol=FP_CG_TOL)
+    print("HFB: E_HF %.6f / %.6f, Epair_n %.6f / %.6f, lambda_n %.6f / %.6f"
+          % (rg.E_HF, ro.E_HF, rg.E_pair_n, ro.E_pair_n, rg.lambda_n,
+             ro.lambda_n))
+    assert rg.last_dE < 1e-4 and ro.last_dE < 1e-4
+    assert abs(rg.E_int - ro.E_int) < E_TOL
+    # E_HF is not compared: HFEnergy adds the BCS quasiparticle sums
+    # (iteration_data.cpp:212-224, bcsN.qpEnergies), which the HFB branch
+    # stops updating after iteration startHFBIter - 1, so E_HF keeps the
+    # levels of that early iteration, where the two runs' degenerate-basis
+    # choices (TROrder reorders the vectors but not the energies) differ.
+    assert abs(rg.E_pair_n - ro.E_pair_n) < E_TOL
+    assert abs(rg.E_pair_p - ro.E_pair_p) < E_TOL
+    assert abs(rg.lambda_n - ro.lambda_n) < 1e-4
+    assert np.abs(og["spe_n"] - oo["spe_n"]).max() < 1e-4
+    assert np.abs(og["rho_n"] - oo["rho_n"]).max() < 1e-6

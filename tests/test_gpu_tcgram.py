@@ -1,0 +1,50 @@
+"""Tensor-core Gram products (tcgen05 kind::tf32, split TF32 operands) of
+the mixed-precision GCG against the FP64 Gram and numpy."""
+import numpy as np
+import pytest
+
+import nuclearcgm_gb300 as ng
+from nuclearcgm_gb300 import abi, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _gram(ctx, A, B, precision):
+    import ctypes as C
+    A = np.asfortranarray(A, np.complex128)
+    B = np.asfortranarray(B, np.complex128)
+    Cm = np.zeros((A.shape[1], B.shape[1]), np.complex128, order="F")
+    ng._check(ng.load().ncgm_gram(ctx.h, A.ctypes.data, A.shape[1],
+                                  B.ctypes.data, B.shape[1], Cm.ctypes.data,
+                                  precision))
+    return Cm
+
+
+@pytest.mark.parametrize("n,p,q", [(12, 5, 7), (16, 24, 24), (30, 32, 32),
+                                   (20, 70, 40), (24, 3, 100)])
+def test_tensor_core_gram(n, p, q):
+    N = 2 * n ** 3
+    ctx = ng.Context(ng.Grid(n, 0.5 * (n - 1) * 0.6), 4)
+    rng = np.random.default_rng(n + p + q)
+    A = workloads.orthonormal_block(N, p, seed=n + p)
+    B = (rng.normal(size=(N, q)) + 1j * rng.normal(size=(N, q))) * 0.01
+    ref = A.conj().T @ B
+    g64 = _gram(ctx, A, B, abi.FP64)
+    g32 = _gram(ctx, A, B, abi.FP32)
+    scale = np.abs(ref).max()
+    assert np.abs(g64 - ref).max() <= 1e-13 * scale
+    err = np.abs(g32 - ref).max() / scale
+    print("n=%d p=%d q=%d: tensor-core Gram max error %.2e (relative)" % (
+        n, p, q, err))
+    assert err <= 2e-6
+    ctx.close()
+
+
+def test_tensor_core_gram_orthonormal_block():
+    """A^H A of an orthonormal block: the identity to FP32-level error."""
+    n, p = 24, 48
+    ctx = ng.Context(ng.Grid(n, 7.0), 4)
+    A = workloads.orthonormal_block(2 * n ** 3, p, seed=5)
+    g = _gram(ctx, A, A, abi.FP32)
+    assert np.abs(g - np.eye(p)).max() <= 1e-6
+    ctx.close()
