@@ -195,6 +195,38 @@ def _hf_wall(with_cpu):
     return out
 
 
+def _gcg_step(H, X):
+    """One GCG iteration (reference parameters: 80 PCG steps, cgTol 1e-5) on
+    the 40^3 x 64 workload in the plain FP64 form, the FP32-correction form
+    and the FP32 + tensor-core Gram form, from a block first brought near
+    the eigenpairs (12 FP64 iterations from the seeded orthonormal block);
+    eigenvalue differences against the FP64 step."""
+    from nuclearcgm_gb300 import abi
+    out = {"workload": "one GCG iteration, 40^3 lattice, 64 spinors, "
+                       "80 PCG steps max, cgTol 1e-5, from 12 FP64 "
+                       "iterations of the seeded block", "unit": "ms"}
+    warm = abi.GcgParams(max_iter=12, tol=1e-6, cg_steps=80, cg_tol=1e-5,
+                         shift=0, ordering=1, precision=abi.FP64, precond=0)
+    X = H.gcg(X, 64, None, warm)[0]
+    lam = {}
+    for name, prec in (("fp64", abi.FP64), ("fp32", abi.FP32),
+                       ("fp32_tc", abi.FP32_TC)):
+        p = abi.GcgParams(max_iter=1, tol=1e-6, cg_steps=80, cg_tol=1e-5,
+                          shift=0, ordering=1, precision=prec, precond=0)
+        H.gcg(X, 64, None, p)
+        t = []
+        for _ in range(3):
+            _, lam[name], st = H.gcg(X, 64, None, p)
+            t.append(st.ms_total)
+        out[name + "_ms"] = round(min(t), 3)
+        out[name + "_pcg_ms"] = round(st.ms_pcg, 3)
+    import numpy as np
+    for name in ("fp32", "fp32_tc"):
+        out[name + "_max_dlambda_MeV"] = float(np.abs(lam[name] -
+                                                      lam["fp64"]).max())
+    return out
+
+
 def run_reference(args):
     ws, rank = _dist()
     if rank != 0:
@@ -322,8 +354,9 @@ def run_ours(args):
             traffic = json.load(open(tp)).get("dram_bytes_per_launch")
         except Exception:
             traffic = None
-    hf = None
+    hf = gstep = None
     if rank == 0 and not args.no_hf:
+        gstep = _gcg_step(H, X)
         hf = _hf_wall(not args.no_cpu)
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -357,6 +390,7 @@ def run_ours(args):
                                       (ms64 * 1e-3) / 1e9, 2)},
         "cpu_baseline": cpu,
         "hf_wall_to_1keV": hf,
+        "gcg_step": gstep,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -34,6 +34,8 @@ extern "C" {
 
 #define NCGM_FP64 0         /* Hamiltonian apply in FP64 */
 #define NCGM_FP32 1         /* Hamiltonian apply in FP32 (inputs rounded) */
+#define NCGM_FP32_TC 2      /* GCG only: FP32 corrections and tensor-core
+                               Gram products (FP32-level, ~2e-6 relative) */
 
 #define NCGM_NEUTRON 0
 #define NCGM_PROTON 1
@@ -70,7 +72,8 @@ typedef struct ncgm_gcg_params {
   double cg_tol;   /* relative PCG tolerance */
   double shift;    /* initial shift (reference passes 0) */
   int ordering;    /* NCGM_ORDER_* */
-  int precision;   /* precision of the PCG correction applies: NCGM_FP64/FP32 */
+  int precision;   /* NCGM_FP64; NCGM_FP32: FP32 PCG corrections; NCGM_FP32_TC:
+                      also the search-space Gram products on tensor cores */
   int precond;     /* NCGM_PRECOND_*: 1 needs a network (ncgm_set_lp) */
 } ncgm_gcg_params;
 

@@ -78,7 +78,7 @@ NCGM_OK = 0
 STATUS = {0: "NCGM_OK", 1: "NCGM_ERR_ARG", 2: "NCGM_ERR_CUDA",
           3: "NCGM_ERR_NAN", 4: "NCGM_ERR_RANK", 5: "NCGM_ERR_TIMEOUT",
           6: "NCGM_ERR_EIG", 7: "NCGM_ERR_NOMEM"}
-FP64, FP32 = 0, 1
+FP64, FP32, FP32_TC = 0, 1, 2
 PRECOND_JACOBI, PRECOND_LEARNED = 0, 1
 NEUTRON, PROTON = 0, 1
 ORDER_MATCH_PREVIOUS, ORDER_ASCENDING = 0, 1

@@ -198,12 +198,11 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
   const int mx = std::max(vmax, 4);
   const size_t maxChunks = std::max<size_t>(
       1, std::min<size_t>(256, (size_t)8 * 1024 * 1024 / ((size_t)mx * mx)));
-  const bool fp32 = prm.precision == NCGM_FP32;
+  const bool fp32 =
+      prm.precision == NCGM_FP32 || prm.precision == NCGM_FP32_TC;
   const bool learned = prm.precond == NCGM_PRECOND_LEARNED;
-  // mixed form: Gram products of the search space on the tensor cores
-  // (NCGM_TC_GRAM=0 keeps them in FP64)
-  const char *tcEnv = std::getenv("NCGM_TC_GRAM");
-  const bool tc = fp32 && !(tcEnv && tcEnv[0] == '0');
+  // tensor-core Gram products of the search space (FP32-level accuracy)
+  const bool tc = prm.precision == NCGM_FP32_TC;
   if (learned && !ctx->lp) {
     setError("ncgm_gcg: learned preconditioner requested but no network set "
              "(ncgm_set_lp)");

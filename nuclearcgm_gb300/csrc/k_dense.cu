@@ -375,7 +375,6 @@ void gemmVC(const double2 *V, size_t ldv, int m, const double2 *Cm, int ldc,
       cudaMemsetAsync(Y + (size_t)j * ldy, 0, N * sizeof(double2), s);
     return;
   }
-  size_t smem = (size_t)m * k * sizeof(double2);
   static const bool attr = [] {
     cudaFuncSetAttribute(gemmVCKernel,
                          cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -383,8 +382,18 @@ void gemmVC(const double2 *V, size_t ldv, int m, const double2 *Cm, int ldc,
     return true;
   }();
   (void)attr;
-  dim3 grid((unsigned)((N + 127) / 128), (k + 7) / 8);
-  gemmVCKernel<<<grid, 128, smem, s>>>(V, ldv, m, Cm, ldc, k, Y, ldy, N, beta);
+  // C is staged in shared memory: blocks of kt columns with m * kt * 16
+  // bytes <= 200 KB (kt a multiple of 8)
+  int kt = (int)((200 * 1024) / ((size_t)m * sizeof(double2)));
+  kt = std::max(8, kt / 8 * 8);
+  for (int j0 = 0; j0 < k; j0 += kt) {
+    const int kb = std::min(kt, k - j0);
+    const size_t smem = (size_t)m * kb * sizeof(double2);
+    dim3 grid((unsigned)((N + 127) / 128), (kb + 7) / 8);
+    gemmVCKernel<<<grid, 128, smem, s>>>(V, ldv, m, Cm + (size_t)j0 * ldc,
+                                         ldc, kb, Y + (size_t)j0 * ldy, ldy, N,
+                                         beta);
+  }
 }
 
 void cholDrop(const double2 *G, int ldg, int m, double dropTol, double2 *R,

@@ -19,7 +19,8 @@ void gramTC(const double2 *A, size_t lda, int p, const double2 *B, size_t ldb,
             cudaStream_t s);
 size_t tcGramPartialFloats(size_t N, int p, int q);
 int *tcGramErrWord();
-// Y = V C + beta Y (V: N x m, C: m x k with m*k*16 bytes <= 200 KB).
+// Y = V C + beta Y (V: N x m with m <= 1600, C: m x k; C is staged in
+// shared memory in blocks of columns).
 void gemmVC(const double2 *V, size_t ldv, int m, const double2 *C, int ldc,
             int k, double2 *Y, size_t ldy, size_t N, double beta,
             cudaStream_t s);

@@ -88,6 +88,7 @@ struct StreamArgs {
   long long total; // ncols * nbands * n output band-planes
   float shift;
   int *err;
+  int cpa; // stencilStream32: coefficients prefetched one plane ahead
 };
 
 struct Run {
@@ -301,24 +302,64 @@ __global__ void __launch_bounds__(512, 1)
     qv[t] = q;
     lr[t] = (q == 0x7fffffff) ? 0 : ((q / n) + 2) * W + (q % n) + 2;
   }
-  int waited = -1;
+  // with A.cpa: per-thread coefficient staging (two planes x PPT points x
+  // 2 float4) after the ring; the next plane's coefficients are copied with
+  // cp.async while the current plane is computed
+  float4 *stage = reinterpret_cast<float4 *>(
+      smem_raw + (size_t)A.ring * slotElems * 16u + (size_t)A.ring * 16u);
+  auto stg = [&](int buf, int t, int h) {
+    return stage + ((buf * PPT + t) * 2 + h) * nct + ct;
+  };
+  auto prefetch = [&](unsigned pb, int tyn, int buf) {
+#pragma unroll
+    for (int t = 0; t < PPT; ++t)
+      if (qv[t] < tyn) {
+        const float4 *c2 = A.coef + 2 * (size_t)(pb + qv[t]);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                         smemAddr(stg(buf, t, 0))),
+                     "l"(c2)
+                     : "memory");
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                         smemAddr(stg(buf, t, 1))),
+                     "l"(c2 + 1)
+                     : "memory");
+      }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  int waited = -1, sc = 0;
   for (int r = 0; r < NR; ++r) {
     const Run R = runs[r];
     const int col = R.cb / A.nbands, band = R.cb % A.nbands;
     const int y0 = band * A.TY;
     const int tyn = min(A.TY, n - y0) * n;
     float4 *Yc = A.Y + (size_t)col * A.ns;
+    if (A.cpa)
+      prefetch((unsigned)R.ka * (unsigned)(n * n) + (unsigned)(y0 * n), tyn,
+               sc & 1);
     for (int k = R.ka; k < R.kb; ++k) {
       const int s0 = R.base + (k - R.ka);
       const unsigned pbase = (unsigned)k * (unsigned)(n * n) + (unsigned)(y0 * n);
       float4 ca[PPT], cbv[PPT];
+      if (A.cpa) {
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        const int cur = sc & 1;
 #pragma unroll
-      for (int t = 0; t < PPT; ++t)
-        if (qv[t] < tyn) {
-          const float4 *c2 = A.coef + 2 * (size_t)(pbase + qv[t]);
-          ca[t] = __ldg(c2);
-          cbv[t] = __ldg(c2 + 1);
-        }
+        for (int t = 0; t < PPT; ++t)
+          if (qv[t] < tyn) {
+            ca[t] = *stg(cur, t, 0);
+            cbv[t] = *stg(cur, t, 1);
+          }
+        if (k + 1 < R.kb) prefetch(pbase + (unsigned)(n * n), tyn, cur ^ 1);
+        ++sc;
+      } else {
+#pragma unroll
+        for (int t = 0; t < PPT; ++t)
+          if (qv[t] < tyn) {
+            const float4 *c2 = A.coef + 2 * (size_t)(pbase + qv[t]);
+            ca[t] = __ldg(c2);
+            cbv[t] = __ldg(c2 + 1);
+          }
+      }
       bool ok = true;
       while (waited < s0 + 4) {
         const int s = waited + 1;
@@ -358,6 +399,7 @@ __global__ void __launch_bounds__(512, 1)
       }
     }
   }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
 
 // z-marching form. Same producer and plane sequence as stencilStream32, but
@@ -658,11 +700,14 @@ size_t streamSmem(int n, int TY, int ring) {
   size_t slot = (((size_t)(TY + 4) * (n + 4) + 7) & ~size_t(7)) * 16;
   return (size_t)ring * slot + (size_t)ring * 16; // slots + full/empty bars
 }
-// the z-marching kernel adds 2 x 2 float4 of coefficient staging per
-// consumer thread
-size_t kernelSmem(int kind, int n, int TY, int ring, int threads) {
-  return streamSmem(n, TY, ring) +
-         (kind == 1 ? (size_t)64 * (threads - 32) : 0);
+// coefficient staging per consumer thread: the z-marching kernel 2 x 2
+// float4, the streaming kernel with prefetch 2 x ppt x 2 float4
+size_t kernelSmem(int kind, int n, int TY, int ring, int threads, int ppt,
+                  int cpa) {
+  size_t st = 0;
+  if (kind == 1) st = (size_t)64 * (threads - 32);
+  else if (cpa) st = (size_t)64 * ppt * (threads - 32);
+  return streamSmem(n, TY, ring) + st;
 }
 
 int smCount() {
@@ -678,6 +723,7 @@ int smCount() {
 struct Shape {
   int TY, ring, ppt, ctasPerSM;
   int kind; // 0: stencilStream32, 1: stencilMarch32 (ppt unused)
+  int cpa;  // kind 0: coefficients prefetched with cp.async
 };
 
 bool validShape(int n, const Shape &s, int &threads) {
@@ -697,7 +743,8 @@ bool validShape(int n, const Shape &s, int &threads) {
     threads = 32 + ((pts + s.ppt - 1) / s.ppt + 31) / 32 * 32;
   }
   if (threads > 512 || threads < 64) return false;
-  if (kernelSmem(s.kind, n, s.TY, s.ring, threads) * s.ctasPerSM >
+  if (kernelSmem(s.kind, n, s.TY, s.ring, threads, s.ppt, s.cpa) *
+          s.ctasPerSM >
       220 * 1024)
     return false;
   return true;
@@ -722,6 +769,7 @@ bool launchStream(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
   A.total = (long long)ncols * A.nbands * n;
   A.shift = shift;
   A.err = stencilErrWord();
+  A.cpa = sh.kind == 0 ? sh.cpa : 0;
   // enough CTAs that no CTA holds more than kMaxRuns runs
   long long ctas = (long long)smCount() * sh.ctasPerSM;
   const long long minCtas = (A.total + (long long)(kMaxRuns - 2) * n - 1) /
@@ -730,7 +778,8 @@ bool launchStream(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
   ctas = std::min<long long>(ctas, A.total);
   StreamKernel kern = pickKernel(sh.kind, sh.ppt, n + 4);
   kern<<<(unsigned)ctas, threads,
-         kernelSmem(sh.kind, n, sh.TY, sh.ring, threads), st>>>(map, A);
+         kernelSmem(sh.kind, n, sh.TY, sh.ring, threads, sh.ppt, sh.cpa),
+         st>>>(map, A);
   return true;
 }
 
@@ -745,7 +794,7 @@ std::vector<TunedShape> g_tuned;
 std::mutex g_tunedMutex;
 
 Shape defaultShape(int n) {
-  Shape s{n, 8, 4, 1, 0};  // ring: a power of two
+  Shape s{n, 8, 4, 1, 0, 0};  // ring: a power of two
   int th;
   while (!validShape(n, s, th) && s.TY > 1) {
     if (s.TY * n > 512 * s.ppt && s.ppt < kPPT) {
@@ -797,8 +846,8 @@ static Shape tune(ncgm_ctx *ctx, int species, int ncols) {
     if (log)
       std::fprintf(stderr,
                    "[ncgm tune] n=%d cols=%d kind=%d rows=%d ring=%d ppt=%d "
-                   "ctas/SM=%d: %.1f us\n",
-                   n, ncols, s.kind, s.TY, s.ring, s.ppt, s.ctasPerSM,
+                   "ctas/SM=%d cpa=%d: %.1f us\n",
+                   n, ncols, s.kind, s.TY, s.ring, s.ppt, s.ctasPerSM, s.cpa,
                    1e3f * ms / 3);
     if (ms < bestMs) {
       bestMs = ms;
@@ -808,16 +857,17 @@ static Shape tune(ncgm_ctx *ctx, int species, int ncols) {
   for (int TY : rows) {
     for (int ring : {8, 16})
       for (int ppt : {1, 2, 4})
-        for (int cps : {1, 2, 4}) trial(Shape{TY, ring, ppt, cps, 0});
+        for (int cps : {1, 2, 4})
+          for (int cpa : {0, 1}) trial(Shape{TY, ring, ppt, cps, 0, cpa});
     for (int ring : {4, 8, 16})
-      for (int cps : {1, 2, 4}) trial(Shape{TY, ring, 1, cps, 1});
+      for (int cps : {1, 2, 4}) trial(Shape{TY, ring, 1, cps, 1, 0});
   }
   return best;
 }
 
 void applyH32(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
               int ncols, float shift, cudaStream_t s) {
-  // NCGM_STENCIL_SHAPE="rows,ring,ppt,ctasPerSM[,kind]" fixes the shape
+  // NCGM_STENCIL_SHAPE="rows,ring,ppt,ctasPerSM[,kind[,cpa]]" fixes the shape
   const char *envp = std::getenv("NCGM_STENCIL_SHAPE");
   const std::string env = envp ? envp : "";
   Shape sh{};
@@ -833,8 +883,9 @@ void applyH32(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
       Shape fixed{};
       int th = 0;
       if (!env.empty() &&
-          std::sscanf(env.c_str(), "%d,%d,%d,%d,%d", &fixed.TY, &fixed.ring,
-                      &fixed.ppt, &fixed.ctasPerSM, &fixed.kind) >= 4 &&
+          std::sscanf(env.c_str(), "%d,%d,%d,%d,%d,%d", &fixed.TY,
+                      &fixed.ring, &fixed.ppt, &fixed.ctasPerSM, &fixed.kind,
+                      &fixed.cpa) >= 4 &&
           validShape(ctx->n, fixed, th))
         sh = fixed;
       else

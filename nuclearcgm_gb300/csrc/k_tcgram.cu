@@ -12,12 +12,13 @@
 // mixed-precision form accepts for its Gram products; the projected
 // eigenproblem and the Cholesky factorisation stay in FP64.
 //
-// One CTA of 4 warps computes one 128 x 128 tile of D over one chunk of rows:
+// One CTA of 8 warps computes one 128 x 128 tile of D over one chunk of rows:
 // all threads stage 32-row slabs of both operands into shared memory
 // (double-buffered, core-matrix layout without swizzle), one thread issues
 // the tcgen05.mma instructions and commits them to an mbarrier, and after
-// the last slab the four warps read the accumulator out of TMEM
-// (tcgen05.ld 32x32b). Every wait is bounded; on a timeout the CTA records
+// the last slab the warps read the accumulator out of TMEM (tcgen05.ld
+// 32x32b; a warp may read only its quarter of the TMEM lanes, so warps w and
+// w + 4 split the columns of lanes 32 (w % 4) ..). Every wait is bounded; on a timeout the CTA records
 // an error, waits (bounded) for its own MMAs and frees its TMEM.
 #include "ncgm_internal.cuh"
 
@@ -93,7 +94,9 @@ __device__ __forceinline__ float stacked(const double2 *X, size_t ld, int p,
   return 0.f;
 }
 
-__global__ void __launch_bounds__(128, 1)
+constexpr int kThreads = 256; // 8 warps: staging by all, epilogue split
+
+__global__ void __launch_bounds__(kThreads, 1)
     tcGramKernel(const double2 *__restrict__ A, size_t lda, int p,
                  const double2 *__restrict__ B, size_t ldb, int q, size_t N,
                  int rowsPerChunk, float *__restrict__ part, int *err) {
@@ -138,16 +141,26 @@ __global__ void __launch_bounds__(128, 1)
     unsigned char *buf = sm + b * kBufBytes;
     // a warp stages one 8 x 4 core matrix per step: lane = (row & 7, k & 3),
     // so its 32 stores fill 128 contiguous bytes (no bank conflicts) and
-    // every 4 lanes read 4 consecutive rows of one column
+    // every 4 lanes read 4 consecutive rows of one column; all the slab's
+    // loads of a thread are issued before any is used
+    constexpr int kPer = (kTile / 8) * (kSlab / 4) / (kThreads / 32);
     const int r8 = lane >> 2, k4 = lane & 3;
-    for (int g = warp; g < (kTile / 8) * (kSlab / 4); g += 4) {
+    float va[kPer], vb[kPer];
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+      const int g = warp + (kThreads / 32) * i;
       const int row = (g >> 3) * 8 + r8, k = (g & 7) * 4 + k4;
       const size_t r = r0 + (size_t)s * kSlab + k;
       const bool rv = r < r1;
-      const float a = rv ? stacked(A, lda, p, mt * kTile + row, r) : 0.f;
-      const float bb = rv ? stacked(B, ldb, q, nt * kTile + row, r) : 0.f;
-      const float ah = tf32(a), al = tf32(a - ah);
-      const float bh = tf32(bb), bl = tf32(bb - bh);
+      va[i] = rv ? stacked(A, lda, p, mt * kTile + row, r) : 0.f;
+      vb[i] = rv ? stacked(B, ldb, q, nt * kTile + row, r) : 0.f;
+    }
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+      const int g = warp + (kThreads / 32) * i;
+      const int row = (g >> 3) * 8 + r8, k = (g & 7) * 4 + k4;
+      const float ah = tf32(va[i]), al = tf32(va[i] - ah);
+      const float bh = tf32(vb[i]), bl = tf32(vb[i] - bh);
       const uint32_t o = tileOff(row, k);
       *reinterpret_cast<float *>(buf + o) = ah;
       *reinterpret_cast<float *>(buf + kTileBytes + o) = al;
@@ -194,11 +207,14 @@ __global__ void __launch_bounds__(128, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (ok && nslab > 0) {
     // (every thread of the CTA takes this branch together)
-    // epilogue: warp w holds D rows 32w .. 32w + 31 (TMEM lanes)
-    const int row = mt * kTile + warp * 32 + lane;
-    for (int c0 = 0; c0 < kTile; c0 += 16) {
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (D rows), warps
+    // 0-3 the first 64 columns and warps 4-7 the last 64
+    const int lw = warp & 3;
+    const int row = mt * kTile + lw * 32 + lane;
+    const int cBeg = (warp >> 2) * (kTile / 2);
+    for (int c0 = cBeg; c0 < cBeg + kTile / 2; c0 += 16) {
       uint32_t v[16];
-      const uint32_t ta = taddr + ((uint32_t)(warp * 32) << 16) + c0;
+      const uint32_t ta = taddr + ((uint32_t)(lw * 32) << 16) + c0;
       asm volatile(
           "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, "
           "%6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
@@ -286,8 +302,8 @@ void gramTC(const double2 *A, size_t lda, int p, const double2 *B, size_t ldb,
   const int rows = tcGramChunkRows(N, p, q);
   const int chunks = (int)((N + rows - 1) / rows);
   dim3 grid((2 * p + kTile - 1) / kTile, (2 * q + kTile - 1) / kTile, chunks);
-  tcGramKernel<<<grid, 128, kSmemBytes, s>>>(A, lda, p, B, ldb, q, N, rows,
-                                             part, tcGramErrWord());
+  tcGramKernel<<<grid, kThreads, kSmemBytes, s>>>(A, lda, p, B, ldb, q, N,
+                                                  rows, part, tcGramErrWord());
   tcGramReduce<<<(p * q + 127) / 128, 128, 0, s>>>(part, chunks, p, q, C,
                                                    ldc);
 }

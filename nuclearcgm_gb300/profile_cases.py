@@ -1,0 +1,56 @@
+"""Small, fixed workloads for profiling single kernels of the library
+(the commands in profiles/*.md run these).
+
+  python -m nuclearcgm_gb300.profile_cases tcgram      # ncgm_gram, 128 000 x 96
+  python -m nuclearcgm_gb300.profile_cases hf_o16      # 4 HF iterations, 16O 30^3
+  python -m nuclearcgm_gb300.profile_cases gcg_step64  # one GCG step, 40^3 x 64
+"""
+import sys
+
+import numpy as np
+
+from . import Context, Grid, Hamiltonian, _check, abi, config, hf_run, load
+from . import workloads
+
+
+def tcgram():
+    """C = A^H A for an orthonormal 2*40^3 x 96 block, FP64 then twice on
+    the tensor cores."""
+    n, p = 40, 96
+    ctx = Context(Grid(n, 9.75), 4)
+    A = workloads.orthonormal_block(2 * n ** 3, p, seed=5)
+    C = np.zeros((p, p), np.complex128, order="F")
+    for prec in (abi.FP64, abi.FP32, abi.FP32):
+        _check(load().ncgm_gram(ctx.h, A.ctypes.data, p, A.ctypes.data, p,
+                                C.ctypes.data, prec))
+    print("max |A^H A - I| = %.2e" % np.abs(C - np.eye(p)).max())
+    ctx.close()
+
+
+def hf_o16(precision=abi.FP64):
+    """Four HF iterations of 16O (SLy4, box 18 fm, 30^3)."""
+    data = {"functional": "SLy4", "nucleus": {"A": 16, "Z": 8},
+            "box": {"boxSize": 18.0, "axisMeshPoints": 30},
+            "maxIterations": 4, "energyTol": 0.0}
+    res, _ = hf_run(config.from_input(data, precision=precision))
+    print("iterations %d wall %.3f s (gcg %.3f, poisson %.3f)" % (
+        res.iterations, res.wall_s, res.t_gcg_s, res.t_poisson_s))
+
+
+def gcg_step64(precision=abi.FP64):
+    """One GCG iteration on the 40^3 x 64 benchmark workload."""
+    a, f, gradf, U, W = workloads.fields(40, 0.5)
+    ctx = Context(Grid(40, a), 64)
+    H = Hamiltonian(ctx, abi.NEUTRON).set_fields(f, gradf.T, U, W.T)
+    X = workloads.orthonormal_block(2 * 40 ** 3, 64, seed=1)
+    p = abi.GcgParams(max_iter=1, tol=1e-6, cg_steps=80, cg_tol=1e-5,
+                      shift=0, ordering=1, precision=precision, precond=0)
+    _, _, st = H.gcg(X, 64, None, p)
+    print("GCG step %.1f ms (PCG %.1f ms)" % (st.ms_total, st.ms_pcg))
+    ctx.close()
+
+
+CASES = {"tcgram": tcgram, "hf_o16": hf_o16, "gcg_step64": gcg_step64}
+
+if __name__ == "__main__":
+    CASES[sys.argv[1] if len(sys.argv) > 1 else "tcgram"]()

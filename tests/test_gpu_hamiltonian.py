@@ -42,10 +42,11 @@ def test_fp32_plane_kernel_error_bound(n):
     assert np.abs(Y32 - ref).max() <= FP32_TOL * np.abs(ref).max()
 
 
-# fixed stencil shapes (rows, ring, ppt, CTAs/SM, kind), bypassing the
-# autotuner: kind 0 = plane-streaming kernel, kind 1 = z-marching kernel
-SHAPES = ["3,8,1,1,0", "5,16,4,2,0", "2,4,1,1,1", "8,8,1,2,1", "12,8,1,1,1",
-          "6,4,1,4,1"]
+# fixed stencil shapes (rows, ring, ppt, CTAs/SM, kind, coefficient
+# prefetch), bypassing the autotuner: kind 0 = plane-streaming kernel,
+# kind 1 = z-marching kernel
+SHAPES = ["3,8,1,1,0", "5,16,4,2,0", "10,8,2,1,0,1", "5,16,4,2,0,1",
+          "2,4,1,1,1", "8,8,1,2,1", "12,8,1,1,1", "6,4,1,4,1"]
 
 
 @pytest.mark.parametrize("shape", SHAPES)
