@@ -119,6 +119,12 @@ __global__ void colStatsFinish(const double *part, int nb, double *res2,
   xax[c] = b;
 }
 
+__global__ void extractDiag(const double *coef, size_t ns, double *d) {
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < ns;
+       p += (size_t)gridDim.x * blockDim.x)
+    d[p] = coef[8 * p];
+}
+
 struct Carve {
   char *p;
   size_t off = 0;
@@ -187,6 +193,15 @@ static int cholQR2(ncgm_ctx *ctx, const double2 *V, int k, double2 *Q,
   return cols;
 }
 
+double *jacobiDiagonal(ncgm_ctx *ctx, int species, cudaStream_t s) {
+  double *d = static_cast<double *>(
+      ctx->buf(12 + species, ctx->ns * sizeof(double)));
+  if (!d) return nullptr;
+  extractDiag<<<(unsigned)std::min<size_t>(1024, (ctx->ns + 255) / 256), 256,
+                0, s>>>(ctx->sp[species].coef64, ctx->ns, d);
+  return d;
+}
+
 int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
            const double2 *ConjDir, int pcols, int nev,
            const ncgm_gcg_params &prm, double2 *Xout, double *lamOut,
@@ -248,6 +263,7 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
   double *pp1 = ar.take<double>((size_t)nev * 128 * 3),
          *pp2 = ar.take<double>((size_t)nev * 128 * 2);
   int *dLive = ar.take<int>(1), *dNdone = ar.take<int>(1);
+  unsigned *dArrive = ar.take<unsigned>(2 * (size_t)nev);
   double2 *Gs = small, *Cw = small + 4 * (size_t)mx * mx,
           *Ev = small + 5 * (size_t)mx * mx, *Ap = small + 6 * (size_t)mx * mx;
 
@@ -258,6 +274,8 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
     applyH64(ctx, species, X, Y, cols, sh, s);
   };
   NCGM_CUDA(cudaMemsetAsync(dLive, 0, sizeof(int), s));
+  const double *dDiag = jacobiDiagonal(ctx, species, s);
+  if (!dDiag) return NCGM_ERR_NOMEM;
 
   // X = X_init.leftCols(nev), orthonormalised (solver.cpp:669,677)
   NCGM_CUDA(cudaMemcpyAsync(V, Xinit, N * (size_t)nev * sizeof(double2),
@@ -363,7 +381,8 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
         pl.D0 = pD0;
         pl.useNet = dUse;
         pl.lamShift = dLs;
-        pl.coef = ctx->sp[species].coef64;
+        pl.coef = dDiag;
+        pl.arrive = dArrive;
         pl.shift = shift;
         pl.tol = prm.cg_tol;
         pl.maxSteps = prm.cg_steps;
@@ -390,7 +409,8 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
         pl.P = pP;
         pl.AP = pAP;
         pl.lamShift = dLs;
-        pl.coef = ctx->sp[species].coef64;
+        pl.coef = dDiag;
+        pl.arrive = dArrive;
         pl.shift = shift;
         pl.tol = prm.cg_tol;
         pl.maxSteps = prm.cg_steps;
@@ -424,7 +444,8 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
           pl.useNet = dUse;
         }
         pl.lamShift = dLs;
-        pl.coef = ctx->sp[species].coef64;
+        pl.coef = dDiag;
+        pl.arrive = dArrive;
         pl.shift = shift;
         pl.tol = prm.cg_tol;
         pl.maxSteps = prm.cg_steps;

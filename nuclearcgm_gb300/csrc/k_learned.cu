@@ -1019,8 +1019,8 @@ int ncgm_lp_collect(ncgm_lp *lp, ncgm_ctx *ctx, int species, const double *X,
   double *dLam = dLs + ncols;
   PcgCol *st = reinterpret_cast<PcgCol *>(dLam + ncols);
   const int nblk = pcgBlocks(N);
-  double *pp1 = static_cast<double *>(
-      ctx->buf(31, sizeof(double) * ((size_t)ncols * nblk * 5 + 64)));
+  double *pp1 = static_cast<double *>(ctx->buf(
+      31, sizeof(double) * ((size_t)ncols * nblk * 5 + 64 + ncols)));
   // (live and the finished-column counter follow the partial sums)
   if (!pp1) return NCGM_ERR_NOMEM;
   double *pp2 = pp1 + (size_t)ncols * nblk * 3;
@@ -1050,7 +1050,9 @@ int ncgm_lp_collect(ncgm_lp *lp, ncgm_ctx *ctx, int species, const double *X,
   pl.P = Pp;
   pl.AP = AP;
   pl.lamShift = dLs;
-  pl.coef = ctx->sp[species].coef64;
+  pl.coef = jacobiDiagonal(ctx, species, s);
+  pl.arrive = reinterpret_cast<unsigned *>(live + 2);
+  if (!pl.coef) return NCGM_ERR_NOMEM;
   pl.shift = shift;
   pl.tol = cg_tol;
   pl.maxSteps = cg_steps;

@@ -34,10 +34,28 @@ __device__ double blockSum(double v, double *sh) {
   return r;
 }
 
-// inverse Jacobi diagonal from the FP64 coefficient table: diag = c0 + shift
-__device__ inline double invDiag(const double *coef, size_t p, double shift) {
-  double d = coef[8 * p] + shift;
+// inverse Jacobi diagonal: diag = c0 + shift, c0 = U + UC + 7.5 f / h^2
+// (the diagonal of H, one double per lattice point)
+__device__ inline double invDiag(const double *c0, size_t p, double shift) {
+  double d = c0[p] + shift;
   return d != 0.0 ? 1.0 / d : 1.0;
+}
+
+// Last-block test of a per-column reduction: every block has written its
+// partial before it arrives; the block that arrives last sees all of them
+// and resets the counter for the next use.
+__device__ inline bool lastArrival(unsigned *counter, int nblk) {
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned prev = atomicAdd(counter, 1u);
+    last = (prev == (unsigned)nblk - 1);
+    if (last) *counter = 0;
+  }
+  __syncthreads();
+  if (last) __threadfence();
+  return last;
 }
 
 // r = b - T, b = x (lam+shift), z = Minv r, p = z, w = x; partials |b|^2,
@@ -260,7 +278,8 @@ __global__ void pcgInitFinish(PcgCol *st, const double *partials, int nblk,
 template <class T>
 __global__ void pcgDotKernel(const typename C2<T>::type *P,
                              const typename C2<T>::type *AP, size_t N,
-                             const PcgCol *st, double *partials, int nblk) {
+                             PcgCol *st, double *partials, int nblk,
+                             unsigned *arrive) {
   __shared__ double sh[kThreads];
   const int col = blockIdx.y;
   if (st[col].done) return;
@@ -274,43 +293,41 @@ __global__ void pcgDotKernel(const typename C2<T>::type *P,
     im += (double)p.x * a.y - (double)p.y * a.x;
   }
   double s0 = blockSum(re, sh), s1 = blockSum(im, sh);
+  double *pp = partials + (size_t)col * nblk * 3;
   if (threadIdx.x == 0) {
-    double *pp = partials + (size_t)col * nblk * 3;
     pp[blockIdx.x] = s0;
     pp[nblk + blockIdx.x] = s1;
   }
+  // the last block sums the partials in block order: alpha = absNew / p^H Ap
+  if (lastArrival(&arrive[col], nblk) && threadIdx.x == 0) {
+    double r = 0, m = 0;
+    for (int b = 0; b < nblk; ++b) {
+      r += ((volatile double *)pp)[b];
+      m += ((volatile double *)pp)[nblk + b];
+    }
+    const double den = r * r + m * m;
+    const double a = st[col].absNew;
+    st[col].alphaR = a * r / den;
+    st[col].alphaI = -a * m / den;
+  }
 }
 
-// alpha = absNew / (p^H Ap); w += alpha p; r -= alpha Ap; z = Minv r;
-// partials |r|^2 and Re(r^H z) (stored after the p^H Ap partials).
+// w += alpha p; r -= alpha Ap; z = Minv r; partials |r|^2 and Re(r^H z);
+// the last block to finish a column takes the stopping decision and the
+// next beta (the column's finish step)
 template <class T>
 __global__ void pcgUpdateKernel(typename C2<T>::type *Wv,
                                 typename C2<T>::type *R,
                                 typename C2<T>::type *Z,
                                 const typename C2<T>::type *P,
                                 const typename C2<T>::type *AP, size_t N,
-                                const PcgCol *st, const double *coef,
-                                double shift, double *partials,
-                                double *partials2, int nblk) {
+                                PcgCol *st, const double *diag, double shift,
+                                double *partials2, int nblk, unsigned *arrive,
+                                int *live, int *ndone) {
   __shared__ double sh[kThreads];
-  __shared__ double ar, ai;
   const int col = blockIdx.y;
   if (st[col].done) return;
-  if (threadIdx.x == 0) {
-    const double *pp = partials + (size_t)col * nblk * 3;
-    double re = 0, im = 0;
-    for (int b = 0; b < nblk; ++b) {
-      re += pp[b];
-      im += pp[nblk + b];
-    }
-    // alpha = absNew / (re + i im)
-    double den = re * re + im * im;
-    double a = st[col].absNew;
-    ar = a * re / den;
-    ai = -a * im / den;
-  }
-  __syncthreads();
-  const double alr = ar, ali = ai;
+  const double alr = st[col].alphaR, ali = st[col].alphaI;
   double rr = 0, rz = 0;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
        i += (size_t)gridDim.x * blockDim.x) {
@@ -324,7 +341,7 @@ __global__ void pcgUpdateKernel(typename C2<T>::type *Wv,
     double wy = (double)w.y + (alr * py + ali * px);
     double rx = (double)r.x - (alr * ax - ali * ay);
     double ry = (double)r.y - (alr * ay + ali * ax);
-    double m = invDiag(coef, i / 2, shift);
+    double m = invDiag(diag, i / 2, shift);
     double zx = m * rx, zy = m * ry;
     Wv[o] = {(T)wx, (T)wy};
     R[o] = {(T)rx, (T)ry};
@@ -333,36 +350,30 @@ __global__ void pcgUpdateKernel(typename C2<T>::type *Wv,
     rz += rx * zx + ry * zy;
   }
   double s0 = blockSum(rr, sh), s1 = blockSum(rz, sh);
+  double *pp = partials2 + (size_t)col * nblk * 2;
   if (threadIdx.x == 0) {
-    double *pp = partials2 + (size_t)col * nblk * 2;
     pp[blockIdx.x] = s0;
     pp[nblk + blockIdx.x] = s1;
   }
-}
-
-__global__ void pcgFinishKernel(PcgCol *st, const double *partials2, int nblk,
-                                int *live, int *ndone) {
-  const int col = blockIdx.x;
-  if (threadIdx.x != 0) return;
-  PcgCol c = st[col];
-  if (c.done) return;
-  const double *pp = partials2 + (size_t)col * nblk * 2;
-  double rr = 0, rz = 0;
-  for (int b = 0; b < nblk; ++b) {
-    rr += pp[b];
-    rz += pp[nblk + b];
+  if (lastArrival(&arrive[col], nblk) && threadIdx.x == 0) {
+    double tr = 0, tz = 0;
+    for (int b = 0; b < nblk; ++b) {
+      tr += ((volatile double *)pp)[b];
+      tz += ((volatile double *)pp)[nblk + b];
+    }
+    PcgCol c = st[col];
+    if (tr < c.thr) {
+      c.done = 1;
+      if (ndone) atomicAdd(ndone, 1);
+    } else {
+      c.absOld = c.absNew;
+      c.absNew = tz;
+      c.beta = c.absNew / c.absOld;
+      c.iters += 1;
+      atomicAdd(live, 1);
+    }
+    st[col] = c;
   }
-  if (rr < c.thr) {
-    c.done = 1;
-    if (ndone) atomicAdd(ndone, 1);
-  } else {
-    c.absOld = c.absNew;
-    c.absNew = rz;
-    c.beta = c.absNew / c.absOld;
-    c.iters += 1;
-    atomicAdd(live, 1);
-  }
-  st[col] = c;
 }
 
 template <class T>
@@ -461,6 +472,7 @@ void pcgRun(const PcgPlan<T> &pl, cudaStream_t s) {
         pl.partials, nblk);
   }
   if (pl.ndone) cudaMemsetAsync(pl.ndone, 0, sizeof(int), s);
+  cudaMemsetAsync(pl.arrive, 0, 2 * sizeof(unsigned) * pl.ncols, s);
   pcgInitFinish<<<pl.ncols, 32, 0, s>>>(pl.st, pl.partials, nblk, pl.tol,
                                         pl.ndone);
   // Early exit: after the init and after every step the count of finished
@@ -486,14 +498,12 @@ void pcgRun(const PcgPlan<T> &pl, cudaStream_t s) {
     pl.apply(pl.P, pl.N, pl.AP, pl.ncols, pl.shift, s);
     pcgDotKernel<T><<<grid, kThreads, 0, s>>>(
         reinterpret_cast<const V *>(pl.P), reinterpret_cast<const V *>(pl.AP),
-        pl.N, pl.st, pl.partials, nblk);
+        pl.N, pl.st, pl.partials, nblk, pl.arrive);
     pcgUpdateKernel<T><<<grid, kThreads, 0, s>>>(
         reinterpret_cast<V *>(pl.W), reinterpret_cast<V *>(pl.R),
         reinterpret_cast<V *>(pl.Z), reinterpret_cast<const V *>(pl.P),
         reinterpret_cast<const V *>(pl.AP), pl.N, pl.st, pl.coef, pl.shift,
-        pl.partials, pl.partials2, nblk);
-    pcgFinishKernel<<<pl.ncols, 32, 0, s>>>(pl.st, pl.partials2, nblk,
-                                            pl.live, pl.ndone);
+        pl.partials2, nblk, pl.arrive + pl.ncols, pl.live, pl.ndone);
     pcgPKernel<T><<<grid, kThreads, 0, s>>>(
         reinterpret_cast<V *>(pl.P), reinterpret_cast<const V *>(pl.Z), pl.N,
         pl.st);

@@ -1,5 +1,7 @@
 // Batched Jacobi-PCG (see k_pcg.cu).
 #pragma once
+#include "ncgm_internal.cuh"
+
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -9,6 +11,7 @@ namespace ncgm {
 
 struct PcgCol {
   double absNew, absOld, beta, thr, rhsNorm2;
+  double alphaR, alphaI; // step of the current iteration (dot kernel)
   int iters, done, zero, pad;
 };
 
@@ -21,13 +24,16 @@ template <class T> struct PcgPlan {
   size_t ldx = 0;
   void *W = nullptr, *R = nullptr, *Z = nullptr, *P = nullptr, *AP = nullptr;
   const double *lamShift = nullptr; // lambda_k + shift per column (device)
-  const double *coef = nullptr;     // FP64 coefficient table (diagonal)
+  const double *coef = nullptr;     // Jacobi diagonal c0 per point (n^3)
   double shift = 0, tol = 0;
   int maxSteps = 0;
   PcgCol *st = nullptr;
   double *partials = nullptr, *partials2 = nullptr; // ncols*128*3, ncols*128*2
   int *live = nullptr; // count of column-iterations (stats)
   int *ndone = nullptr; // device counter of finished columns: early exit
+  // per-column arrival counters of the fused reductions (2 x ncols, zeroed
+  // by pcgRun)
+  unsigned *arrive = nullptr;
   // correction form: when AX64 is set the plan solves for d = w - x from the
   // FP64 residual x lam - A x; X64 = x, W64 receives w = x + d (FP64)
   const double2 *X64 = nullptr, *AX64 = nullptr;
@@ -43,6 +49,9 @@ template <class T> struct PcgPlan {
 };
 
 int pcgBlocks(size_t N);
+// The Jacobi diagonal c0 = U + UC + 7.5 f / h^2 of a species' current
+// coefficient table, one double per lattice point, in a context buffer.
+double *jacobiDiagonal(ncgm_ctx *ctx, int species, cudaStream_t s);
 template <class T> void pcgRun(const PcgPlan<T> &plan, cudaStream_t s);
 
 } // namespace ncgm
