@@ -156,7 +156,8 @@ def _hf_wall(with_cpu):
     if os.path.exists(wpath):
         lp = ng.LearnedPreconditioner.pretrained(wpath)
     forms = [("fp64_gpu", abi.FP64, abi.PRECOND_JACOBI),
-             ("mixed_gpu", abi.FP32, abi.PRECOND_JACOBI)]
+             ("mixed_gpu", abi.FP32, abi.PRECOND_JACOBI),
+             ("mixed_tc_gpu", abi.FP32_TC, abi.PRECOND_JACOBI)]
     if lp is not None:
         forms.append(("learned_mixed_gpu", abi.FP32, abi.PRECOND_LEARNED))
     out = {"workload": "16O HF ground state, SLy4, 30^3 lattice, box 18 fm, "
@@ -222,8 +223,10 @@ def _gcg_step(H, X):
         out[name + "_pcg_ms"] = round(st.ms_pcg, 3)
     import numpy as np
     for name in ("fp32", "fp32_tc"):
-        out[name + "_max_dlambda_MeV"] = float(np.abs(lam[name] -
-                                                      lam["fp64"]).max())
+        d = np.abs(lam[name] - lam["fp64"])
+        out[name + "_max_dlambda_MeV"] = float(d.max())
+        # the lowest half of the block (converged furthest) separately
+        out[name + "_max_dlambda_low32_MeV"] = float(d[:32].max())
     return out
 
 

@@ -34,8 +34,9 @@ extern "C" {
 
 #define NCGM_FP64 0         /* Hamiltonian apply in FP64 */
 #define NCGM_FP32 1         /* Hamiltonian apply in FP32 (inputs rounded) */
-#define NCGM_FP32_TC 2      /* GCG only: FP32 corrections and tensor-core
-                               Gram products (FP32-level, ~2e-6 relative) */
+#define NCGM_FP32_TC 2      /* GCG: FP32 corrections and tensor-core Gram
+                               products split into exact BF16 digits
+                               (~1e-13 relative) */
 
 #define NCGM_NEUTRON 0
 #define NCGM_PROTON 1
@@ -73,7 +74,8 @@ typedef struct ncgm_gcg_params {
   double shift;    /* initial shift (reference passes 0) */
   int ordering;    /* NCGM_ORDER_* */
   int precision;   /* NCGM_FP64; NCGM_FP32: FP32 PCG corrections; NCGM_FP32_TC:
-                      also the search-space Gram products on tensor cores */
+                      also the search-space Gram products on the tensor
+                      cores (exact-digit form, ~1e-13 relative) */
   int precond;     /* NCGM_PRECOND_*: 1 needs a network (ncgm_set_lp) */
 } ncgm_gcg_params;
 
@@ -265,7 +267,10 @@ int ncgm_hf_run(const ncgm_hf_config *cfg, ncgm_hf_result *res, double *spe_n,
  * products of the GCG (src/solver/solver.cpp:750-777, V.adjoint() * W).
  * precision NCGM_FP64: FP64 CUDA cores, deterministic reduction;
  * NCGM_FP32: tensor cores (tcgen05 kind::tf32 with split TF32 operands,
- * FP32 accumulation over row chunks, FP64 chunk sums; FP32-level error). */
+ * FP32 accumulation over row chunks, FP64 chunk sums; ~2e-6 relative);
+ * NCGM_FP32_TC: tensor cores (tcgen05 kind::f16, values split into six
+ * 7-bit integer digits held exactly in BF16, exact FP32 sums per digit
+ * level, FP64 combination; ~1e-13 relative). */
 int ncgm_gram(ncgm_ctx *ctx, const double *A, int p, const double *B, int q,
               double *C, int precision);
 

@@ -164,7 +164,8 @@ static int cholQR2(ncgm_ctx *ctx, const double2 *V, int k, double2 *Q,
     // mixed form: the first pass's Gram on the tensor cores (FP32-level),
     // the second in FP64 so the basis is orthonormal to FP64 rounding
     if (pass == 0 && tcPart)
-      gramTC(src, N, cols, src, N, cols, N, G, cols, tcPart, s);
+      gramTCExact(src, N, cols, src, N, cols, N, G, cols,
+                  reinterpret_cast<double *>(tcPart), s);
     else
       gram(src, N, cols, src, N, cols, N, G, cols, partials, maxChunks, s);
     cholDrop(G, cols, cols, 1e-24, R, T, dKeep, s);
@@ -237,7 +238,7 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
   float *tcPart = nullptr;
   if (tc) {
     tcPart = static_cast<float *>(ctx->buf(
-        11, sizeof(float) * tcGramPartialFloats(N, vmax, vmax) + 256));
+        11, sizeof(double) * exactGramScratchDoubles(N, vmax, vmax) + 256));
     if (!tcPart) return NCGM_ERR_NOMEM;
   }
   Carve ar{base};
@@ -443,6 +444,9 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
           pl.D0 = pD0;
           pl.useNet = dUse;
         }
+        // with tensor-core Grams the search space takes the correction d
+        // itself (same span as w = x + d, but not nearly dependent on x)
+        pl.onlyCorrection = tc;
         pl.lamShift = dLs;
         pl.coef = dDiag;
         pl.arrive = dArrive;
@@ -489,7 +493,8 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
     // Rayleigh-Ritz on A_shifted
     applyA(Q, AV, m, shift);
     if (tc)
-      gramTC(Q, N, m, AV, N, m, N, Ap, m, tcPart, s);
+      gramTCExact(Q, N, m, AV, N, m, N, Ap, m,
+                  reinterpret_cast<double *>(tcPart), s);
     else
       gram(Q, N, m, AV, N, m, N, Ap, m, partials, (int)maxChunks, s);
     heig(Ap, m, m, Cw, Ev, dW, dPerm, dStat, s);
@@ -678,7 +683,8 @@ extern "C" int ncgm_gcg(ncgm_ctx *ctx, int species, const double *X_init,
 extern "C" int ncgm_gram(ncgm_ctx *ctx, const double *A, int p,
                          const double *B, int q, double *C, int precision) {
   if (!ctx || !A || !B || !C || p < 1 || q < 1 || p > 4096 || q > 4096 ||
-      (precision != NCGM_FP64 && precision != NCGM_FP32)) {
+      (precision != NCGM_FP64 && precision != NCGM_FP32 &&
+       precision != NCGM_FP32_TC)) {
     setError("ncgm_gram: bad argument");
     return NCGM_ERR_ARG;
   }
@@ -704,6 +710,11 @@ extern "C" int ncgm_gram(ncgm_ctx *ctx, const double *A, int p,
         ctx->buf(29, sizeof(float) * tcGramPartialFloats(N, p, q) + 256));
     if (!part) return NCGM_ERR_NOMEM;
     gramTC(dA, N, p, dB, N, q, N, dC, p, part, s);
+  } else if (precision == NCGM_FP32_TC) {
+    double *part = static_cast<double *>(
+        ctx->buf(29, sizeof(double) * exactGramScratchDoubles(N, p, q) + 256));
+    if (!part) return NCGM_ERR_NOMEM;
+    gramTCExact(dA, N, p, dB, N, q, N, dC, p, part, s);
   } else {
     const int chunks = gramMaxChunks();
     auto *part = static_cast<double2 *>(
@@ -717,9 +728,11 @@ extern "C" int ncgm_gram(ncgm_ctx *ctx, const double *A, int p,
   NCGM_CUDA(cudaStreamSynchronize(s));
   NCGM_CUDA(cudaGetLastError());
   int flag = 0;
-  if (precision == NCGM_FP32) {
-    NCGM_CUDA(cudaMemcpy(&flag, tcGramErrWord(), sizeof(int),
-                         cudaMemcpyDeviceToHost));
+  if (precision != NCGM_FP64) {
+    NCGM_CUDA(cudaMemcpy(&flag,
+                         precision == NCGM_FP32 ? tcGramErrWord()
+                                                : exactGramErrWord(),
+                         sizeof(int), cudaMemcpyDeviceToHost));
     if (flag) {
       setError("ncgm_gram: tensor-core kernel wait timed out");
       return NCGM_ERR_TIMEOUT;

@@ -19,6 +19,14 @@ void gramTC(const double2 *A, size_t lda, int p, const double2 *B, size_t ldb,
             cudaStream_t s);
 size_t tcGramPartialFloats(size_t N, int p, int q);
 int *tcGramErrWord();
+// C = A^H B on the tensor cores to ~1e-13 relative: error-free splitting into
+// BF16 integer digits, exact FP32 level sums, FP64 combination
+// (k_tcgram_exact.cu). scratch: exactGramScratchDoubles(N, p, q) doubles.
+void gramTCExact(const double2 *A, size_t lda, int p, const double2 *B,
+                 size_t ldb, int q, size_t N, double2 *C, int ldc,
+                 double *scratch, cudaStream_t s);
+size_t exactGramScratchDoubles(size_t N, int p, int q);
+int *exactGramErrWord();
 // Y = V C + beta Y (V: N x m with m <= 1600, C: m x k; C is staged in
 // shared memory in blocks of columns).
 void gemmVC(const double2 *V, size_t ldv, int m, const double2 *C, int ldc,

@@ -10,6 +10,7 @@
 #include "k_pcg.cuh"
 
 #include <cfloat>
+#include <cstdlib>
 #include <vector>
 
 namespace ncgm {
@@ -237,14 +238,14 @@ __global__ void pcgInitNetKernel(const double2 *X64, const double2 *AX64,
 template <class T>
 __global__ void pcgCombineKernel(const double2 *X64,
                                  const typename C2<T>::type *Dv, double2 *W64,
-                                 size_t N, const PcgCol *st) {
+                                 size_t N, const PcgCol *st, int onlyD) {
   const int col = blockIdx.y;
   const bool zero = st[col].zero;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
        i += (size_t)gridDim.x * blockDim.x) {
     size_t o = (size_t)col * N + i;
     auto d = Dv[o];
-    double2 x = X64[o];
+    double2 x = onlyD ? make_double2(0.0, 0.0) : X64[o];
     W64[o] = zero ? make_double2(0.0, 0.0)
                   : make_double2(x.x + (double)d.x, x.y + (double)d.y);
   }
@@ -488,13 +489,7 @@ void pcgRun(const PcgPlan<T> &pl, cudaStream_t s) {
     cudaEventRecord(poll->ev[slot % kPollEvents], s);
   };
   mark(0);
-  for (int it = 0; it < pl.maxSteps; ++it) {
-    if (poll && it + 1 - kLag >= 0 && it + 1 - kLag < kPollSlots) {
-      const int slot = it + 1 - kLag;
-      if (cudaEventSynchronize(poll->ev[slot % kPollEvents]) == cudaSuccess &&
-          poll->host[slot] >= pl.ncols)
-        break;
-    }
+  auto step = [&]() {
     pl.apply(pl.P, pl.N, pl.AP, pl.ncols, pl.shift, s);
     pcgDotKernel<T><<<grid, kThreads, 0, s>>>(
         reinterpret_cast<const V *>(pl.P), reinterpret_cast<const V *>(pl.AP),
@@ -507,11 +502,49 @@ void pcgRun(const PcgPlan<T> &pl, cudaStream_t s) {
     pcgPKernel<T><<<grid, kThreads, 0, s>>>(
         reinterpret_cast<V *>(pl.P), reinterpret_cast<const V *>(pl.Z), pl.N,
         pl.st);
+  };
+  // One step is the same four launches with the same arguments every time:
+  // after a first direct step (which also settles the stencil's tuned
+  // shape), it is captured once into a CUDA graph and replayed, one graph
+  // launch per step. NCGM_PCG_GRAPH=0 keeps direct launches.
+  const char *genv = std::getenv("NCGM_PCG_GRAPH");
+  const bool useGraph = !(genv && genv[0] == '0');
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool graphFailed = false;
+  for (int it = 0; it < pl.maxSteps; ++it) {
+    if (poll && it + 1 - kLag >= 0 && it + 1 - kLag < kPollSlots) {
+      const int slot = it + 1 - kLag;
+      if (cudaEventSynchronize(poll->ev[slot % kPollEvents]) == cudaSuccess &&
+          poll->host[slot] >= pl.ncols)
+        break;
+    }
+    if (useGraph && it > 0 && !exec && !graphFailed) {
+      if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) ==
+          cudaSuccess) {
+        step();
+        if (cudaStreamEndCapture(s, &graph) != cudaSuccess ||
+            cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
+          graphFailed = true;
+          exec = nullptr;
+        }
+      } else {
+        graphFailed = true;
+      }
+      cudaGetLastError();
+    }
+    if (exec)
+      cudaGraphLaunch(exec, s);
+    else
+      step();
     if (it + 1 < kPollSlots) mark(it + 1);
   }
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
   if (pl.AX64)
     pcgCombineKernel<T><<<grid, kThreads, 0, s>>>(
-        pl.X64, reinterpret_cast<const V *>(pl.W), pl.W64, pl.N, pl.st);
+        pl.X64, reinterpret_cast<const V *>(pl.W), pl.W64, pl.N, pl.st,
+        pl.onlyCorrection ? 1 : 0);
   else
     pcgZeroKernel<T><<<grid, kThreads, 0, s>>>(reinterpret_cast<V *>(pl.W),
                                                pl.N, pl.st);

@@ -43,6 +43,10 @@ template <class T> struct PcgPlan {
   // when alpha <= 0 (useNet[col] records the choice, device, may be null)
   const void *D0 = nullptr;
   int *useNet = nullptr;
+  // correction form: W64 receives d instead of x + d (span(x, x + d) =
+  // span(x, d); used when the search space is orthonormalised from a Gram
+  // product with FP32-level resolution of near-dependent columns)
+  bool onlyCorrection = false;
   // Y = (A + shift) X on device buffers (ld of X given, Y stride N)
   std::function<void(const void *, size_t, void *, int, double, cudaStream_t)>
       apply;

@@ -209,8 +209,12 @@ __device__ __forceinline__ float4 pointH2(const float4 ca, const float4 cb,
 // planes it no longer needs with one arrive per warp. No CTA-wide barrier
 // in the loop. PPT: points per consumer thread; WFIX: padded row width
 // n + 4 fixed at compile time (0: runtime), making +-W offsets immediates.
+// block-size limit per variant: the 1- and 2-point forms fit in 102
+// registers, so up to 640 threads (20 warps) per SM; the 4-point form 512
+constexpr int streamMaxThreads(int ppt) { return ppt == 4 ? 512 : 640; }
+
 template <int PPT, int WFIX>
-__global__ void __launch_bounds__(512, 1)
+__global__ void __launch_bounds__(streamMaxThreads(PPT), 1)
     stencilStream32(const __grid_constant__ CUtensorMap map, StreamArgs A) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ Run runs[kMaxRuns];
@@ -741,8 +745,9 @@ bool validShape(int n, const Shape &s, int &threads) {
     const int pts = s.TY * n;
     // one producer warp + consumer warps covering the band
     threads = 32 + ((pts + s.ppt - 1) / s.ppt + 31) / 32 * 32;
+    if (threads > streamMaxThreads(s.ppt)) return false;
   }
-  if (threads > 512 || threads < 64) return false;
+  if (threads < 64) return false;
   if (kernelSmem(s.kind, n, s.TY, s.ring, threads, s.ppt, s.cpa) *
           s.ctasPerSM >
       220 * 1024)
@@ -854,6 +859,13 @@ static Shape tune(ncgm_ctx *ctx, int species, int ncols) {
       best = s;
     }
   };
+  // plus, per points-per-thread, the tallest band one block can cover
+  for (int ppt : {1, 2, 4}) {
+    const int ty = ((streamMaxThreads(ppt) - 32) * ppt) / n;
+    if (ty >= 1 && ty < n &&
+        std::find(rows.begin(), rows.end(), ty) == rows.end())
+      rows.push_back(ty);
+  }
   for (int TY : rows) {
     for (int ring : {8, 16})
       for (int ppt : {1, 2, 4})

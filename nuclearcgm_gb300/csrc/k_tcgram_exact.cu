@@ -1,0 +1,396 @@
+// FP64-accurate Gram products on the tensor cores: C = A^H B for complex FP64
+// blocks A (N x p), B (N x q), with the error-free splitting of Ozaki, Ogita,
+// Oishi and Rump (Numer. Algorithms 59, 2012) mapped onto tcgen05 BF16 MMAs.
+//
+// As in k_tcgram.cu the complex product is one real product of the stacked
+// blocks S = [Re A | Im A] (N x 2p) and T = [Re B | Im B] (N x 2q). Every
+// column c of S and T is scaled by a power of two 2^-e_c that brings its
+// entries into [-1, 1] (e_c from the column's max-abs, exact), and each
+// scaled value is written as a sum of kDig signed 7-bit integer digits,
+//   x 2^-e = sum_t a_t 2^(-7t),  |a_1| <= 128, |a_t| <= 64 (t > 1),
+// all exactly representable in BF16. A product of two digits is an integer
+// below 2^14; the MMAs of one "level" l = t + u (pairs with the same scale
+// 2^(-7l)) accumulate in FP32 tensor memory over 256 rows, so every partial
+// sum is an integer below 2^24 and the FP32 accumulation is exact. After each
+// 256-row block the levels are combined in FP64 (shared-memory accumulators),
+// and the CTA's FP64 partial is summed with the other row chunks in a fixed
+// order. Levels above kDig + 1 are dropped: the truncation error is ~2^(-7
+// kDig) of the column max per element (kDig = 6: ~2e-13 relative).
+//
+// Tile: M = 128 rows of S^T, N = 64 columns of T; 8 warps stage 32-row slabs
+// (double-buffered, K-major core matrices, no swizzle), one thread issues the
+// MMAs (instruction K = 16, 2 per slab per digit pair) and commits them, and
+// after every 8 slabs the warps fold the level accumulators (tcgen05.ld) into
+// FP64. Every wait is bounded.
+#include "ncgm_internal.cuh"
+
+#include <cuda_bf16.h>
+
+namespace ncgm {
+
+namespace {
+
+constexpr int kDig = 6;                  // digits per value
+constexpr int kM = 128, kN = 64;         // D tile
+constexpr int kSlab = 32;                // K rows per stage (2 MMAs of K 16)
+constexpr int kFold = 8;                 // slabs per exact accumulation block
+constexpr int kThr = 256;
+constexpr int kABytes = kM * kSlab * 2;  // one digit plane of A: 8 KB
+constexpr int kBBytes = kN * kSlab * 2;  // one digit plane of B: 4 KB
+constexpr int kBuf = kDig * (kABytes + kBBytes); // 72 KB
+constexpr int kAccBytes = kM * kN * 8;           // FP64 tile: 64 KB
+constexpr int kSmem = 2 * kBuf + kAccBytes + 64;
+constexpr uint32_t kLBO = 128, kSBO = 512;       // 8 rows x 16 B cores; K 32
+constexpr uint32_t kTmemCols = 512; // kDig levels x kN = 384 -> 512
+
+__device__ __forceinline__ uint32_t sAddr(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ uint64_t smemDesc(uint32_t addr) {
+  uint64_t d = (uint64_t)((addr >> 4) & 0x3FFF);
+  d |= (uint64_t)((kLBO >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((kSBO >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+// D FP32, A/B BF16, K-major, M = 128, N = 64
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) |
+                            ((uint32_t)(kN >> 3) << 17) |
+                            ((uint32_t)(kM >> 4) << 24);
+
+// byte offset of element (row, k) in a K-major tile with 32 BF16 per row:
+// core matrices of 8 rows x 8 elements (16 B); 4 cores along K
+__device__ __forceinline__ uint32_t off16(int row, int k) {
+  return (uint32_t)(row >> 3) * kSBO + (uint32_t)(k >> 3) * kLBO +
+         (uint32_t)(row & 7) * 16u + (uint32_t)(k & 7) * 2u;
+}
+
+__device__ __forceinline__ bool waitBar(uint64_t *bar, uint32_t phase) {
+  for (uint32_t it = 0; it < (1u << 20); ++it) {
+    uint32_t done;
+    asm volatile("{\n .reg .pred p;\n"
+                 " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+                 " selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(done)
+                 : "r"(sAddr(bar)), "r"(phase), "r"(1000u)
+                 : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ double stackedD(const double2 *X, size_t ld, int p,
+                                           int c, size_t r) {
+  if (c < p) return X[(size_t)c * ld + r].x;
+  if (c < 2 * p) return X[(size_t)(c - p) * ld + r].y;
+  return 0.0;
+}
+
+// digits of a scaled value: w = round(x 2^(42-e)), |w| < 2^42, written as
+// sum_t a_t 2^(42-7t) with |a_1| <= 128 and |a_t| <= 64, by integer rounding
+// divisions (exact; the digits are integers, exact in BF16)
+__device__ __forceinline__ void digits(long long w, float d[kDig]) {
+#pragma unroll
+  for (int t = 0; t < kDig - 1; ++t) {
+    const int sh = 35 - 7 * t;
+    const long long a = (w + (1ll << (sh - 1))) >> sh;
+    d[t] = (float)a;
+    w -= a << sh;
+  }
+  d[kDig - 1] = (float)w;
+}
+
+// w = round(x 2^(42 - e)) for |x| < 2^e, from the bits of x with integer
+// operations only (round half away from zero; the FP64 pipe is slow)
+__device__ __forceinline__ long long scaledInt(double x, int e) {
+  const long long bits = __double_as_longlong(x);
+  const int ex = (int)((bits >> 52) & 0x7FF);
+  if (ex == 0) return 0; // zero or subnormal: below 2^-1022
+  const long long mant = (bits & 0xFFFFFFFFFFFFFll) | (1ll << 52);
+  // x = mant 2^(ex - 1075); the result is mant 2^(ex - 1033 - e), where the
+  // shift is <= -11 since |x| < 2^e
+  const int sh = 1033 + e - ex;
+  if (sh >= 63) return 0;
+  const long long w = (mant + (1ll << (sh - 1))) >> sh;
+  return bits < 0 ? -w : w;
+}
+
+// per column of the stacked block X (N x 2p): the power of two sc[c] = 2^e
+// above its max-abs, and its exponent ex[c] = e (one block per column)
+__global__ void colMaxKernel(const double2 *X, size_t ld, int p, size_t N,
+                             double *mx, int *exq) {
+  __shared__ double sh[256];
+  const int c = blockIdx.x;
+  double m = 0;
+  for (size_t r = threadIdx.x; r < N; r += blockDim.x)
+    m = fmax(m, fabs(stackedD(X, ld, p, c, r)));
+  sh[threadIdx.x] = m;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    int e = 0;
+    if (sh[0] > 0) frexp(sh[0], &e); // sh[0] < 2^e
+    mx[c] = ldexp(1.0, e);           // column scale: entries / mx in (-1, 1)
+    exq[c] = e;
+  }
+}
+
+__global__ void __launch_bounds__(kThr, 1)
+    exactGramKernel(const double2 *__restrict__ A, size_t lda, int p,
+                    const double2 *__restrict__ B, size_t ldb, int q, size_t N,
+                    const double *__restrict__ scA,
+                    const int *__restrict__ eA,
+                    const double *__restrict__ scB,
+                    const int *__restrict__ eB, int rowsPerChunk,
+                    double *__restrict__ part, int *err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  double *acc = reinterpret_cast<double *>(sm + 2 * kBuf);
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + 2 * kBuf + kAccBytes);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int mt = blockIdx.x, nt = blockIdx.y, chunk = blockIdx.z;
+  const size_t r0 = (size_t)chunk * rowsPerChunk;
+  const size_t r1 = (r0 + (size_t)rowsPerChunk < N) ? r0 + rowsPerChunk : N;
+  const int nslab = (int)((r1 - r0 + kSlab - 1) / kSlab);
+
+  if (warp == 0) {
+    asm volatile(
+        "tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::
+            "r"(sAddr(tslot)),
+        "r"(kTmemCols)
+        : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;"
+                 ::
+                     : "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sAddr(&mbar[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sAddr(&mbar[1])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (int e = tid; e < kM * kN; e += kThr) acc[e] = 0.0;
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t taddr = *tslot;
+  bool ok = true;
+  __shared__ int nCommitted;
+  int committed = 0;
+
+  for (int s = 0; s < nslab && ok; ++s) {
+    const int b = s & 1;
+    if (s >= 2 && !waitBar(&mbar[b], ((s - 2) >> 1) & 1)) ok = false;
+    if (!__syncthreads_and(ok)) {
+      ok = false;
+      break;
+    }
+    unsigned char *buf = sm + b * kBuf;
+    // stage the digit planes: A rows (kM) then B rows (kN); a warp writes
+    // one 8 x 8 core matrix per step (lane = row & 7, k pair)
+    const int r8 = lane >> 2, k2 = (lane & 3) * 2;
+    for (int g = warp; g < (kM / 8) * (kSlab / 8) + (kN / 8) * (kSlab / 8);
+         g += kThr / 32) {
+      const bool isA = g < (kM / 8) * (kSlab / 8);
+      const int gg = isA ? g : g - (kM / 8) * (kSlab / 8);
+      const int row = (gg >> 2) * 8 + r8, k = (gg & 3) * 8 + k2;
+      float d0[kDig], d1[kDig];
+      for (int h = 0; h < 2; ++h) {
+        const size_t r = r0 + (size_t)s * kSlab + k + h;
+        long long w = 0;
+        if (r < r1) {
+          if (isA) {
+            const int c = mt * kM + row;
+            if (c < 2 * p) w = scaledInt(stackedD(A, lda, p, c, r), eA[c]);
+          } else {
+            const int c = nt * kN + row;
+            if (c < 2 * q) w = scaledInt(stackedD(B, ldb, q, c, r), eB[c]);
+          }
+        }
+        digits(w, h ? d1 : d0);
+      }
+      const uint32_t o = off16(row, k);
+      for (int t = 0; t < kDig; ++t) {
+        unsigned char *plane =
+            isA ? buf + t * kABytes
+                : buf + kDig * kABytes + t * kBBytes;
+        __nv_bfloat162 v2 = __floats2bfloat162_rn(d0[t], d1[t]);
+        *reinterpret_cast<__nv_bfloat162 *>(plane + o) = v2;
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t base = sAddr(buf);
+      const bool first = (s % kFold) == 0;
+      for (int ks = 0; ks < kSlab / 16; ++ks) {
+        const uint32_t kofs = ks * 2 * kLBO; // 16 K = 2 core matrices
+        for (int t = 0; t < kDig; ++t)
+          for (int u = 0; u + t < kDig; ++u) {
+            const int lev = t + u; // level index 0 .. kDig-1
+            const uint64_t ad = smemDesc(base + t * kABytes + kofs);
+            const uint64_t bd =
+                smemDesc(base + kDig * kABytes + u * kBBytes + kofs);
+            // the first MMA of each level in a fold block overwrites (in this
+            // loop order a level's first pair is (0, lev))
+            const uint32_t accum = (first && ks == 0 && t == 0) ? 0u : 1u;
+            const uint32_t td = taddr + (uint32_t)(lev * kN);
+            asm volatile("{\n .reg .pred pa;\n setp.ne.b32 pa, %4, 0;\n"
+                         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, "
+                         "%3, pa;\n}\n" ::"r"(td),
+                         "l"(ad), "l"(bd), "r"(kIdesc), "r"(accum)
+                         : "memory");
+          }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::"
+                   "cluster.b64 [%0];" ::"r"(sAddr(&mbar[b]))
+                   : "memory");
+      committed = s + 1;
+    }
+    // fold the exact level sums into FP64 at the end of each block
+    if ((s % kFold) == kFold - 1 || s == nslab - 1) {
+      if (!waitBar(&mbar[b], (s >> 1) & 1)) ok = false;
+      if (!__syncthreads_and(ok)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int lw = warp & 3, row = lw * 32 + lane;
+      const int cBeg = (warp >> 2) * (kN / 2);
+      for (int c0 = cBeg; c0 < cBeg + kN / 2; c0 += 16) {
+        // the level sums are integers below 2^24: combine them exactly in
+        // 64-bit integers (sum_l L_l 2^(7 (kDig-1-l)) < 2^60), then one
+        // conversion to FP64 per element
+        long long sum[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) sum[j] = 0;
+        for (int lev = 0; lev < kDig; ++lev) {
+          uint32_t v[16];
+          const uint32_t ta =
+              taddr + ((uint32_t)(lw * 32) << 16) + (uint32_t)(lev * kN + c0);
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, "
+              "%5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+              : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]),
+                "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]),
+                "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                "=r"(v[14]), "=r"(v[15])
+              : "r"(ta));
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int j = 0; j < 16; ++j)
+            sum[j] = sum[j] * 128 + (long long)__float2int_rn(
+                                         __uint_as_float(v[j]));
+        }
+        // sum = sum_l L_l 2^(7 (kDig-1-l)); value = sum 2^(-7 (kDig+1))
+        const double w = ldexp(1.0, -7 * (kDig + 1));
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          acc[row * kN + c0 + j] += (double)sum[j] * w;
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+    }
+  }
+  if (tid == 0) nCommitted = committed;
+  __syncthreads();
+  if (!ok && nCommitted > 0) {
+    const int last = nCommitted - 1;
+    waitBar(&mbar[last & 1], (last >> 1) & 1);
+  }
+  ok = __syncthreads_and(ok);
+  if (ok) {
+    for (int e = tid; e < kM * kN; e += kThr) {
+      const int row = e / kN, col = e % kN;
+      const int gr = mt * kM + row, gc = nt * kN + col;
+      if (gr < 2 * p && gc < 2 * q)
+        part[((size_t)chunk * 2 * p + gr) * (2 * q) + gc] =
+            acc[e] * scA[gr] * scB[gc];
+    }
+  } else if (tid == 0) {
+    atomicExch(err, 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(
+                     taddr),
+                 "r"(kTmemCols)
+                 : "memory");
+}
+
+__global__ void exactGramReduce(const double *__restrict__ part, int chunks,
+                                int p, int q, double2 *__restrict__ C,
+                                int ldc) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= p * q) return;
+  const int i = e % p, j = e / p;
+  const size_t W = 2 * (size_t)q, H = 2 * (size_t)p;
+  double re = 0, im = 0;
+  for (int ch = 0; ch < chunks; ++ch) {
+    const double *P = part + (size_t)ch * H * W;
+    re += P[(size_t)i * W + j] + P[(size_t)(p + i) * W + q + j];
+    im += P[(size_t)i * W + q + j] - P[(size_t)(p + i) * W + j];
+  }
+  C[(size_t)j * ldc + i] = make_double2(re, im);
+}
+
+int chunkRows(size_t N, int p, int q) {
+  const int tiles = ((2 * p + kM - 1) / kM) * ((2 * q + kN - 1) / kN);
+  size_t rows = (N * tiles + 303) / 304;
+  const size_t blk = (size_t)kSlab * kFold;
+  rows = ((rows + blk - 1) / blk) * blk;
+  if (rows < blk) rows = blk;
+  return (int)rows;
+}
+
+} // namespace
+
+size_t exactGramScratchDoubles(size_t N, int p, int q) {
+  const size_t rows = chunkRows(N, p, q);
+  const size_t chunks = (N + rows - 1) / rows;
+  return chunks * 4 * (size_t)p * q + 4 * (size_t)(p + q) + 8;
+} // (column scales 2(p+q) doubles, exponents 2(p+q) ints, partials)
+
+int *exactGramErrWord() {
+  static int *d = [] {
+    int *x = nullptr;
+    if (cudaMalloc(&x, sizeof(int)) == cudaSuccess)
+      cudaMemset(x, 0, sizeof(int));
+    return x;
+  }();
+  return d;
+}
+
+// C = A^H B on the tensor cores to ~1e-13 relative (see the file comment);
+// scratch holds exactGramScratchDoubles(N, p, q) doubles.
+void gramTCExact(const double2 *A, size_t lda, int p, const double2 *B,
+                 size_t ldb, int q, size_t N, double2 *C, int ldc,
+                 double *scratch, cudaStream_t s) {
+  if (p == 0 || q == 0 || N == 0) return;
+  static const bool attr = [] {
+    cudaFuncSetAttribute(exactGramKernel,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
+    return true;
+  }();
+  (void)attr;
+  double *scA = scratch, *scB = scA + 2 * (size_t)p;
+  int *eA = reinterpret_cast<int *>(scB + 2 * (size_t)q);
+  int *eB = eA + 2 * (size_t)p;
+  double *part = scB + 4 * (size_t)q + 2 * (size_t)p + 8;
+  colMaxKernel<<<2 * p, 256, 0, s>>>(A, lda, p, N, scA, eA);
+  colMaxKernel<<<2 * q, 256, 0, s>>>(B, ldb, q, N, scB, eB);
+  const int rows = chunkRows(N, p, q);
+  const int chunks = (int)((N + rows - 1) / rows);
+  dim3 grid((2 * p + kM - 1) / kM, (2 * q + kN - 1) / kN, chunks);
+  exactGramKernel<<<grid, kThr, kSmem, s>>>(A, lda, p, B, ldb, q, N, scA, eA,
+                                            scB, eB, rows, part,
+                                            exactGramErrWord());
+  exactGramReduce<<<(p * q + 127) / 128, 128, 0, s>>>(part, chunks, p, q, C,
+                                                      ldc);
+}
+
+} // namespace ncgm

@@ -14,13 +14,13 @@ from . import workloads
 
 
 def tcgram():
-    """C = A^H A for an orthonormal 2*40^3 x 96 block, FP64 then twice on
-    the tensor cores."""
+    """C = A^H A for an orthonormal 2*40^3 x 96 block: FP64, then the
+    TF32-split and the exact-digit tensor-core forms."""
     n, p = 40, 96
     ctx = Context(Grid(n, 9.75), 4)
     A = workloads.orthonormal_block(2 * n ** 3, p, seed=5)
     C = np.zeros((p, p), np.complex128, order="F")
-    for prec in (abi.FP64, abi.FP32, abi.FP32):
+    for prec in (abi.FP64, abi.FP32, abi.FP32_TC):
         _check(load().ncgm_gram(ctx.h, A.ctypes.data, p, A.ctypes.data, p,
                                 C.ctypes.data, prec))
     print("max |A^H A - I| = %.2e" % np.abs(C - np.eye(p)).max())

@@ -115,6 +115,14 @@ def test_o16_hf_mixed_precision_fixed_point():
     _fixed_point(rg, og, ro, oo, translation=True)
 
 
+def test_o16_hf_mixed_tensor_core_fixed_point():
+    """FP32 PCG corrections plus the exact-digit tensor-core Gram products
+    (NCGM_FP32_TC): the same fixed point."""
+    _, rg, og, ro, oo = _run_both(O16, precision=abi.FP32_TC,
+                                  cg_tol=FP_CG_TOL)
+    _fixed_point(rg, og, ro, oo, translation=True)
+
+
 def test_n_equals_z_without_coulomb_fixed_point():
     data = {"functional": "SKMstar", "nucleus": {"A": 16, "Z": 8},
             "box": {"boxSize": 16.5, "axisMeshPoints": 12},

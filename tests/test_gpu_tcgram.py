@@ -48,3 +48,23 @@ def test_tensor_core_gram_orthonormal_block():
     g = _gram(ctx, A, A, abi.FP32)
     assert np.abs(g - np.eye(p)).max() <= 2e-5
     ctx.close()
+
+
+@pytest.mark.parametrize("n,p,q", [(12, 5, 7), (16, 24, 24), (30, 32, 32),
+                                   (20, 70, 40), (24, 3, 100)])
+def test_exact_digit_gram(n, p, q):
+    """The exact-digit tensor-core form (NCGM_FP32_TC): FP64-level error."""
+    N = 2 * n ** 3
+    ctx = ng.Context(ng.Grid(n, 0.5 * (n - 1) * 0.6), 4)
+    rng = np.random.default_rng(7 * n + p + q)
+    A = workloads.orthonormal_block(N, p, seed=n + 2 * p)
+    B = (rng.normal(size=(N, q)) + 1j * rng.normal(size=(N, q))) * 0.01
+    B[:, 0] *= 1e-6  # a column far below the others: per-column scaling
+    ref = A.conj().T @ B
+    g = _gram(ctx, A, B, abi.FP32_TC)
+    err = np.abs(g - ref).max() / np.abs(ref).max()
+    col0 = np.abs(g[:, 0] - ref[:, 0]).max() / np.abs(ref[:, 0]).max()
+    print("n=%d p=%d q=%d: exact-digit Gram max error %.2e (column 0: %.2e)"
+          % (n, p, q, err, col0))
+    assert err <= 5e-12 and col0 <= 5e-12
+    ctx.close()
