@@ -142,6 +142,45 @@ O16_HF = {"functional": "SLy4", "nucleus": {"A": 16, "Z": 8},
           "maxIterations": 500, "energyTol": 1e-3}
 
 
+CA40_HF = {"functional": "SLy4", "nucleus": {"A": 40, "Z": 20},
+           "box": {"boxSize": 20.0, "axisMeshPoints": 36},
+           "maxIterations": 500, "energyTol": 1e-3}
+
+
+def _hf_wall_ca40():
+    """The learned-preconditioner evaluation nucleus: 40Ca, SLy4, 36^3
+    lattice, box 20 fm, 20 orbitals per isospin, to |dE| < 1 keV, in the
+    plain FP64, mixed, mixed + tensor-core and learned + mixed forms (second
+    of two runs each)."""
+    import nuclearcgm_gb300 as ng
+    from nuclearcgm_gb300 import abi, config
+    lp = None
+    wpath = os.path.join(HERE, "nuclearcgm_gb300", "data", "lp_weights.f32")
+    if os.path.exists(wpath):
+        lp = ng.LearnedPreconditioner.pretrained(wpath)
+    out = {"workload": "40Ca HF ground state, SLy4, 36^3 lattice, box 20 fm, "
+                       "|dE| < 1 keV", "unit": "s"}
+    forms = [("fp64_gpu", abi.FP64, abi.PRECOND_JACOBI),
+             ("mixed_gpu", abi.FP32, abi.PRECOND_JACOBI),
+             ("mixed_tc_gpu", abi.FP32_TC, abi.PRECOND_JACOBI)]
+    if lp is not None:
+        forms.append(("learned_mixed_gpu", abi.FP32, abi.PRECOND_LEARNED))
+    for name, prec, pc in forms:
+        cfg = config.from_input(CA40_HF, precision=prec)
+        cfg.hf_gcg.precond = pc
+        if pc == abi.PRECOND_LEARNED:
+            cfg.lp = lp.h.value
+        for rep in range(2):
+            t0 = time.perf_counter()
+            res, _ = ng.hf_run(cfg)
+            wall = time.perf_counter() - t0
+        out[name + "_s"] = round(wall, 4)
+        out[name + "_iterations"] = res.iterations
+        out[name + "_E_MeV"] = round(res.E_HF, 6)
+        out[name + "_gcg_s"] = round(res.t_gcg_s, 4)
+    return out
+
+
 def _hf_wall(with_cpu):
     """Wall seconds to |dE| < 1 keV (the driver's stop rule, main.cpp:333-337)
     for the 16O HF ground state (SLy4, 30^3 lattice, box 18 fm, Woods-Saxon
@@ -357,10 +396,11 @@ def run_ours(args):
             traffic = json.load(open(tp)).get("dram_bytes_per_launch")
         except Exception:
             traffic = None
-    hf = gstep = None
+    hf = gstep = hf_ca = None
     if rank == 0 and not args.no_hf:
         gstep = _gcg_step(H, X)
         hf = _hf_wall(not args.no_cpu)
+        hf_ca = _hf_wall_ca40()
     cpu = None
     if rank == 0 and not args.no_cpu:
         gbs_c, dt_c = _cpu_reference(3, 1, a, f, gradf, U, W, X, 4)
@@ -393,6 +433,7 @@ def run_ours(args):
                                       (ms64 * 1e-3) / 1e9, 2)},
         "cpu_baseline": cpu,
         "hf_wall_to_1keV": hf,
+        "hf_wall_to_1keV_ca40": hf_ca,
         "gcg_step": gstep,
     }
     if rank == 0:

@@ -444,9 +444,11 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
           pl.D0 = pD0;
           pl.useNet = dUse;
         }
-        // with tensor-core Grams the search space takes the correction d
-        // itself (same span as w = x + d, but not nearly dependent on x)
-        pl.onlyCorrection = tc;
+        // the search space takes the correction d itself: the same span as
+        // w = x + d, but not nearly dependent on x, so the orthonormalisation
+        // keeps d's direction to full precision (with w = x + d it would
+        // lose the digits of d that FP32 rounding already made noisy)
+        pl.onlyCorrection = true;
         pl.lamShift = dLs;
         pl.coef = dDiag;
         pl.arrive = dArrive;

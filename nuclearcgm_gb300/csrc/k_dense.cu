@@ -190,11 +190,11 @@ __global__ void cholDropKernel(const double2 *G, int ldg, int m,
 __global__ void heigKernel(const double2 *Ain, int lda, int m, double2 *Ag,
                            double2 *Vg, double *w, int *perm, int *status,
                            int useSmem) {
-  // working copies of A and V in shared memory when they fit (m <= 64),
-  // else in the global work buffers
+  // working copies in shared memory when they fit: useSmem 2 = A and V
+  // (m <= 81), 1 = A only (m <= 114), 0 = both in the global work buffers
   extern __shared__ double2 hsm[];
   double2 *A = useSmem ? hsm : Ag;
-  double2 *Vm = useSmem ? hsm + (size_t)m * m : Vg;
+  double2 *Vm = useSmem == 2 ? hsm + (size_t)m * m : Vg;
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int e = tid; e < m * m; e += nt) {
     int i = e % m, j = e / m;
@@ -404,16 +404,21 @@ void cholDrop(const double2 *G, int ldg, int m, double dropTol, double2 *R,
 void heig(const double2 *A, int lda, int m, double2 *work, double2 *V,
           double *w, int *perm, int *status, cudaStream_t s) {
   // the round-robin tables hold up to 256 pairs (m <= 512)
+  constexpr size_t kMaxDyn = 210 * 1024; // + 14 KB static <= 227 KB
   static const bool attr = [] {
     cudaFuncSetAttribute(heigKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         2 * 64 * 64 * (int)sizeof(double2));
+                         (int)kMaxDyn);
     return true;
   }();
   (void)attr;
-  const bool sm = m <= 64;
-  const size_t smem = sm ? 2 * (size_t)m * m * sizeof(double2) : 0;
-  heigKernel<<<1, 512, smem, s>>>(A, lda, m, work, V, w, perm, status,
-                                  sm ? 1 : 0);
+  const size_t mat = (size_t)m * m * sizeof(double2);
+  const int sm = 2 * mat <= kMaxDyn ? 2 : (mat <= kMaxDyn ? 1 : 0);
+  const size_t smem = sm == 2 ? 2 * mat : (sm == 1 ? mat : 0);
+  // a round updates m x m/2 elements between barriers: small problems run
+  // with fewer warps, so each of the ~4 barriers per round is cheaper
+  const int threads = m <= 32 ? 128 : (m <= 48 ? 256 : 512);
+  heigKernel<<<1, threads, smem, s>>>(A, lda, m, work, V, w, perm, status,
+                                      sm);
 }
 
 } // namespace ncgm

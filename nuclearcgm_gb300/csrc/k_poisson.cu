@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -305,14 +306,44 @@ int poissonSolve(const PoissonArgs &P, cudaStream_t s, int *iterations) {
   double hs[8];
   double best = 1e300;
   int sinceBest = 0;
-  for (; it < maxit;) {
-    for (int b = 0; b < 16; ++b, ++it) {
+  // a block of 16 CG iterations (64 launches with fixed arguments) is
+  // captured once per solve into a CUDA graph and replayed; the host checks
+  // convergence between blocks. NCGM_POISSON_GRAPH=0 keeps direct launches.
+  auto block = [&]() {
+    for (int b = 0; b < 16; ++b) {
       negLapKernel<<<nblk, 256, 0, s>>>(p, Ap, n, P.h, part2);
       cgUpdateKernel<<<nblk, 256, 0, s>>>(P.U, r, p, Ap, ns, part2, nblk, sc,
                                           part);
       cgDirKernel<<<nblk, 256, 0, s>>>(p, r, ns, part, nblk, sc, tol2);
       cgCommit<<<1, 32, 0, s>>>(sc);
     }
+  };
+  const char *genv = std::getenv("NCGM_POISSON_GRAPH");
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  if (!(genv && genv[0] == '0') &&
+      cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) ==
+          cudaSuccess) {
+    block();
+    if (cudaStreamEndCapture(s, &graph) != cudaSuccess ||
+        cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess)
+      exec = nullptr;
+    cudaGetLastError();
+  }
+  struct GraphGuard {
+    cudaGraph_t &g;
+    cudaGraphExec_t &e;
+    ~GraphGuard() {
+      if (e) cudaGraphExecDestroy(e);
+      if (g) cudaGraphDestroy(g);
+    }
+  } guard{graph, exec};
+  for (; it < maxit;) {
+    if (exec)
+      cudaGraphLaunch(exec, s);
+    else
+      block();
+    it += 16;
     cudaMemcpyAsync(hs, sc, sizeof(double) * 8, cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return NCGM_ERR_CUDA;
     if (!std::isfinite(hs[0])) return NCGM_ERR_NAN;
