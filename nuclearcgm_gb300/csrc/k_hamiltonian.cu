@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(256)
 __global__ void buildCoefKernel(const double *f, const double *gf,
                                 const double *U, const double *W,
                                 const double *UC, size_t ns, double h,
-                                double *c64, float *c32) {
+                                double *c64, float *c32, float *c32s) {
   size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (p >= ns) return;
   const double hh = h * h, i12h = 1.0 / (12.0 * h);
@@ -89,6 +89,7 @@ __global__ void buildCoefKernel(const double *f, const double *gf,
   for (int q = 0; q < 8; ++q) {
     c64[8 * p + q] = c[q];
     c32[8 * p + q] = (float)c[q];
+    c32s[(q < 4 ? 4 * p : 4 * (ns + p) - 4) + q] = (float)c[q];
   }
 }
 
@@ -177,9 +178,10 @@ int buildCoefficients(ncgm_ctx *ctx, int species, const double *f,
   if (!F.coef64) {
     NCGM_CUDA(cudaMalloc(&F.coef64, ctx->ns * 8 * sizeof(double)));
     NCGM_CUDA(cudaMalloc(&F.coef32, ctx->ns * 8 * sizeof(float)));
+    NCGM_CUDA(cudaMalloc(&F.coef32s, ctx->ns * 8 * sizeof(float)));
   }
   buildCoefKernel<<<(unsigned)((ctx->ns + 255) / 256), 256, 0, ctx->stream>>>(
-      f, gradf, U, W, UC, ctx->ns, ctx->h, F.coef64, F.coef32);
+      f, gradf, U, W, UC, ctx->ns, ctx->h, F.coef64, F.coef32, F.coef32s);
   NCGM_CUDA(cudaGetLastError());
   F.ready = true;
   return NCGM_OK;

@@ -18,7 +18,7 @@
 //  * mbarrier waits are bounded: on timeout the CTA records an error flag,
 //    drains its own copies (bounded) and returns.
 #include "ncgm_internal.cuh"
-#include "stencil_core.cuh"
+#include "stencil32.cuh"
 
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -36,171 +36,7 @@ int *stencilErrWord();
 
 namespace {
 
-constexpr int kPPT = 4;       // max owned points per thread
-constexpr int kMaxRuns = 48;  // (column, band) runs per CTA
-
-__device__ __forceinline__ uint32_t smemAddr(const void *p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbarInit(uint64_t *bar, int count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(bar)),
-               "r"(count));
-}
-__device__ __forceinline__ void mbarExpectTx(uint64_t *bar, uint32_t bytes) {
-  asm volatile(
-      "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
-          smemAddr(bar)),
-      "r"(bytes)
-      : "memory");
-}
-__device__ __forceinline__ bool mbarWait(uint64_t *bar, uint32_t phase,
-                                         uint32_t limit) {
-  for (uint32_t it = 0; it < limit; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n"
-        " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(smemAddr(bar)), "r"(phase)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
-__device__ __forceinline__ void tmaTile5(void *dst, const CUtensorMap *map,
-                                         int c1, int c2, int c3, int c4,
-                                         uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::"
-      "complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(
-          smemAddr(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(c1), "r"(c2), "r"(c3),
-      "r"(c4), "r"(smemAddr(bar))
-      : "memory");
-}
-
-struct StreamArgs {
-  float4 *Y;
-  const float4 *coef;
-  int n, TY, nbands, ring, ppt;
-  size_t ns;
-  long long total; // ncols * nbands * n output band-planes
-  float shift;
-  int *err;
-  int cpa; // stencilStream32: coefficients prefetched one plane ahead
-};
-
-struct Run {
-  int cb, ka, kb, base;
-};
-
-__device__ __forceinline__ void mbarArrive(uint64_t *bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smemAddr(bar))
-               : "memory");
-}
-// bounded wait that lets the warp sleep between polls (suspend-time hint)
-__device__ __forceinline__ bool mbarWaitSleep(uint64_t *bar, uint32_t phase,
-                                              uint32_t limit) {
-  for (uint32_t it = 0; it < limit; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n"
-        " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
-        " selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(smemAddr(bar)), "r"(phase), "r"(1000u)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
-
-// ---- packed FP32 pair arithmetic (f32x2: one instruction, two lanes) ----
-using f2x = unsigned long long;
-__device__ __forceinline__ f2x pk(float a, float b) {
-  f2x r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-  return r;
-}
-__device__ __forceinline__ float2 upk(f2x v) {
-  float2 r;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
-  return r;
-}
-__device__ __forceinline__ f2x add2(f2x a, f2x b) {
-  f2x r;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ f2x sub2(f2x a, f2x b) {
-  f2x r;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ f2x mul2(f2x a, f2x b) {
-  f2x r;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c) {
-  f2x r;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-  return r;
-}
-__device__ __forceinline__ f2x bc(float a) { return pk(a, a); }
-
-// pointH (stencil_core.cuh) with each spin component held as one (re, im)
-// pair: the kinetic, derivative and gradient terms are real coefficients
-// times pairs; the spin-orbit matrix is split as A + iB (A, B real), so
-// (A + iB) D = A D + i (B D) and only one i-rotation per spin is needed.
-__device__ __forceinline__ float4 pointH2(const float4 ca, const float4 cb,
-                                          float shift, float4 v, float4 xp1,
-                                          float4 xm1, float4 xp2, float4 xm2,
-                                          float4 yp1, float4 ym1, float4 yp2,
-                                          float4 ym2, float4 zp1, float4 zm1,
-                                          float4 zp2, float4 zm2) {
-  const f2x D = bc(ca.x + shift), NF = bc(-ca.y);
-  const f2x GX = bc(ca.z), GY = bc(ca.w), GZ = bc(cb.x);
-  const f2x WX = bc(cb.y), WY = bc(cb.z), WZ = bc(cb.w);
-  const f2x NWX = bc(-cb.y), NWY = bc(-cb.z), NWZ = bc(-cb.w);
-  const f2x C43 = bc(4.0f / 3.0f), NC112 = bc(-1.0f / 12.0f), EIGHT = bc(8.f);
-  f2x o[2], Dx[2], Dy[2], Dz[2];
-#pragma unroll
-  for (int s = 0; s < 2; ++s) {
-    auto A = [s](float4 q) { return s ? pk(q.z, q.w) : pk(q.x, q.y); };
-    const f2x a_xp1 = A(xp1), a_xm1 = A(xm1), a_xp2 = A(xp2), a_xm2 = A(xm2);
-    const f2x a_yp1 = A(yp1), a_ym1 = A(ym1), a_yp2 = A(yp2), a_ym2 = A(ym2);
-    const f2x a_zp1 = A(zp1), a_zm1 = A(zm1), a_zp2 = A(zp2), a_zm2 = A(zm2);
-    f2x s1 = add2(add2(add2(a_xp1, a_xm1), add2(a_yp1, a_ym1)),
-                  add2(a_zp1, a_zm1));
-    f2x s2 = add2(add2(add2(a_xp2, a_xm2), add2(a_yp2, a_ym2)),
-                  add2(a_zp2, a_zm2));
-    f2x t = fma2(C43, s1, mul2(NC112, s2));
-    f2x os = fma2(NF, t, mul2(D, A(v)));
-    Dx[s] = fma2(EIGHT, sub2(a_xp1, a_xm1), sub2(a_xm2, a_xp2));
-    Dy[s] = fma2(EIGHT, sub2(a_yp1, a_ym1), sub2(a_ym2, a_yp2));
-    Dz[s] = fma2(EIGHT, sub2(a_zp1, a_zm1), sub2(a_zm2, a_zp2));
-    os = fma2(GX, Dx[s], os);
-    os = fma2(GY, Dy[s], os);
-    o[s] = fma2(GZ, Dz[s], os);
-  }
-  // spin-orbit: real parts (A) into o, imaginary parts (B) into u, o += i u
-  o[0] = fma2(NWZ, Dx[1], o[0]);
-  o[0] = fma2(WX, Dz[1], o[0]);
-  f2x u0 = mul2(WY, Dx[0]);
-  u0 = fma2(NWX, Dy[0], u0);
-  u0 = fma2(WZ, Dy[1], u0);
-  u0 = fma2(NWY, Dz[1], u0);
-  o[1] = fma2(WZ, Dx[0], o[1]);
-  o[1] = fma2(NWX, Dz[0], o[1]);
-  f2x u1 = mul2(NWY, Dx[1]);
-  u1 = fma2(WZ, Dy[0], u1);
-  u1 = fma2(WX, Dy[1], u1);
-  u1 = fma2(NWY, Dz[0], u1);
-  const float2 p0 = upk(o[0]), p1 = upk(o[1]), q0 = upk(u0), q1 = upk(u1);
-  return make_float4(p0.x - q0.y, p0.y + q0.x, p1.x - q1.y, p1.y + q1.x);
-}
+using namespace s32;
 
 // Warp-specialised form. Warp 0 is the producer: one lane issues the TMA
 // loads of the CTA's plane sequence, waiting on the slot's `empty` barrier
@@ -276,7 +112,8 @@ __global__ void __launch_bounds__(streamMaxThreads(PPT), 1)
         const Run &R = runs[pr];
         const int col = R.cb / A.nbands, band = R.cb % A.nbands;
         mbarExpectTx(&full[slot], boxBytes);
-        tmaTile5(ring + (size_t)slot * slotElems, &map, -2, band * A.TY - 2,
+        tmaBand(ring + (size_t)slot * slotElems, &map, A.flat, -2,
+                band * A.TY - 2,
                  pz, col, &full[slot]);
         issued = s + 1;
         if (++pz >= R.kb + 2 && pr + 1 < NR) {
@@ -480,7 +317,8 @@ __global__ void __launch_bounds__(kMarchThreads, 1)
         const Run &R = runs[pr];
         const int col = R.cb / A.nbands, band = R.cb % A.nbands;
         mbarExpectTx(&full[slot], boxBytes);
-        tmaTile5(ring + (size_t)slot * slotElems, &map, -2, band * A.TY - 2,
+        tmaBand(ring + (size_t)slot * slotElems, &map, A.flat, -2,
+                band * A.TY - 2,
                  pz, col, &full[slot]);
         issued = s + 1;
         if (++pz >= R.kb + 2 && pr + 1 < NR) {
@@ -666,38 +504,69 @@ PFN_cuTensorMapEncodeTiled_v12000 encodeFn() {
 
 struct MapEntry {
   const void *ptr;
-  int n, ncols, TY;
+  int n, d4, boxW, boxRows, boxD4;
+  bool flat;
   CUtensorMap map;
 };
 std::vector<MapEntry> g_maps;
 std::mutex g_mapsMutex; // contexts may run on several host threads
 
-// 5-D map of X: dims (4 floats, i, j, k, col), box (4, n+4, TY+4, 1, 1).
-bool tensorMapFor(const void *X, int n, int ncols, int TY, CUtensorMap *out) {
+} // namespace
+
+bool tensorMapX(const void *base, int n, int d4, int boxW, int boxRows,
+                int boxD4, bool &flat, CUtensorMap *out) {
   std::lock_guard<std::mutex> lock(g_mapsMutex);
   for (auto &e : g_maps)
-    if (e.ptr == X && e.n == n && e.ncols == ncols && e.TY == TY) {
+    if (e.ptr == base && e.n == n && e.d4 == d4 && e.boxW == boxW &&
+        e.boxRows == boxRows && e.boxD4 == boxD4) {
+      flat = e.flat;
       *out = e.map;
       return true;
     }
   auto fn = encodeFn();
   if (!fn) return false;
-  cuuint64_t dims[5] = {4, (cuuint64_t)n, (cuuint64_t)n, (cuuint64_t)n,
-                        (cuuint64_t)ncols};
-  cuuint64_t strides[4] = {16, (cuuint64_t)16 * n, (cuuint64_t)16 * n * n,
-                           (cuuint64_t)16 * n * n * n};
-  cuuint32_t box[5] = {4, (cuuint32_t)(n + 4), (cuuint32_t)(TY + 4), 1, 1};
+  const bool fl = 4 * boxW <= 256;
+  const cuuint64_t nn = (cuuint64_t)n;
+  cuuint64_t dims5[5] = {4, nn, nn, nn, (cuuint64_t)d4};
+  cuuint64_t dims4[4] = {4 * nn, nn, nn, (cuuint64_t)d4};
+  cuuint64_t str5[4] = {16, 16 * nn, 16 * nn * nn, 16 * nn * nn * nn};
+  cuuint64_t str4[3] = {16 * nn, 16 * nn * nn, 16 * nn * nn * nn};
+  cuuint32_t box5[5] = {4, (cuuint32_t)boxW, (cuuint32_t)boxRows, 1,
+                        (cuuint32_t)boxD4};
+  cuuint32_t box4[4] = {(cuuint32_t)(4 * boxW), (cuuint32_t)boxRows, 1,
+                        (cuuint32_t)boxD4};
   cuuint32_t es[5] = {1, 1, 1, 1, 1};
   CUtensorMap m;
-  CUresult r = fn(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, const_cast<void *>(X),
-                  dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+  CUresult r = fn(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, fl ? 4 : 5,
+                  const_cast<void *>(base), fl ? dims4 : dims5,
+                  fl ? str4 : str5, fl ? box4 : box5, es,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return false;
   if (g_maps.size() > 64) g_maps.erase(g_maps.begin());
-  g_maps.push_back({X, n, ncols, TY, m});
+  g_maps.push_back({base, n, d4, boxW, boxRows, boxD4, fl, m});
+  flat = fl;
   *out = m;
   return true;
+}
+
+int smCount() {
+  static const int c = [] {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 1;
+  }();
+  return c;
+}
+
+namespace {
+
+// map of X with one (n+4) x (TY+4) band box of one column
+bool tensorMapFor(const void *X, int n, int ncols, int TY, bool &flat,
+                  CUtensorMap *out) {
+  return tensorMapX(X, n, ncols, n + 4, TY + 4, 1, flat, out);
 }
 
 size_t streamSmem(int n, int TY, int ring) {
@@ -714,23 +583,19 @@ size_t kernelSmem(int kind, int n, int TY, int ring, int threads, int ppt,
   return streamSmem(n, TY, ring) + st;
 }
 
-int smCount() {
-  static const int c = [] {
-    int dev = 0, v = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-    return v > 0 ? v : 1;
-  }();
-  return c;
-}
-
 struct Shape {
   int TY, ring, ppt, ctasPerSM;
-  int kind; // 0: stencilStream32, 1: stencilMarch32 (ppt unused)
-  int cpa;  // kind 0: coefficients prefetched with cp.async
+  int kind; // 0: stencilStream32, 1: stencilMarch32 (ppt unused),
+            // 2: stencilStage32 (ppt = rows per thread)
+  int cpa;  // kind 0: coefficients prefetched with cp.async;
+            // kind 2: coefficient ring depth
+  int nc;   // kind 2: columns per X box
 };
 
 bool validShape(int n, const Shape &s, int &threads) {
+  if (s.kind == 2)
+    return validStage(n, s.TY, s.ring, s.cpa, s.ppt, s.nc, s.ctasPerSM,
+                      threads);
   if (s.TY < 1 || s.TY > n || s.ring < 4 || (s.ring & (s.ring - 1)) ||
       s.ring > 64 || s.ctasPerSM < 1)
     return false;
@@ -760,8 +625,12 @@ bool launchStream(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
   const int n = ctx->n;
   int threads = 0;
   if (!validShape(n, sh, threads)) return false;
+  if (sh.kind == 2)
+    return launchStage(ctx, species, X, Y, ncols, shift, st, sh.TY, sh.ring,
+                       sh.cpa, sh.ppt, sh.nc, sh.ctasPerSM);
   CUtensorMap map;
-  if (!tensorMapFor(X, n, ncols, sh.TY, &map)) return false;
+  bool flat = false;
+  if (!tensorMapFor(X, n, ncols, sh.TY, flat, &map)) return false;
   StreamArgs A;
   A.Y = reinterpret_cast<float4 *>(Y);
   A.coef = reinterpret_cast<const float4 *>(ctx->sp[species].coef32);
@@ -775,6 +644,7 @@ bool launchStream(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
   A.shift = shift;
   A.err = stencilErrWord();
   A.cpa = sh.kind == 0 ? sh.cpa : 0;
+  A.flat = flat ? 1 : 0;
   // enough CTAs that no CTA holds more than kMaxRuns runs
   long long ctas = (long long)smCount() * sh.ctasPerSM;
   const long long minCtas = (A.total + (long long)(kMaxRuns - 2) * n - 1) /
@@ -799,7 +669,7 @@ std::vector<TunedShape> g_tuned;
 std::mutex g_tunedMutex;
 
 Shape defaultShape(int n) {
-  Shape s{n, 8, 4, 1, 0, 0};  // ring: a power of two
+  Shape s{n, 8, 4, 1, 0, 0, 1};  // ring: a power of two
   int th;
   while (!validShape(n, s, th) && s.TY > 1) {
     if (s.TY * n > 512 * s.ppt && s.ppt < kPPT) {
@@ -851,9 +721,9 @@ static Shape tune(ncgm_ctx *ctx, int species, int ncols) {
     if (log)
       std::fprintf(stderr,
                    "[ncgm tune] n=%d cols=%d kind=%d rows=%d ring=%d ppt=%d "
-                   "ctas/SM=%d cpa=%d: %.1f us\n",
+                   "ctas/SM=%d cpa=%d nc=%d: %.1f us\n",
                    n, ncols, s.kind, s.TY, s.ring, s.ppt, s.ctasPerSM, s.cpa,
-                   1e3f * ms / 3);
+                   s.nc, 1e3f * ms / 3);
     if (ms < bestMs) {
       bestMs = ms;
       best = s;
@@ -870,16 +740,27 @@ static Shape tune(ncgm_ctx *ctx, int species, int ncols) {
     for (int ring : {8, 16})
       for (int ppt : {1, 2, 4})
         for (int cps : {1, 2, 4})
-          for (int cpa : {0, 1}) trial(Shape{TY, ring, ppt, cps, 0, cpa});
+          for (int cpa : {0, 1}) trial(Shape{TY, ring, ppt, cps, 0, cpa, 1});
     for (int ring : {4, 8, 16})
-      for (int cps : {1, 2, 4}) trial(Shape{TY, ring, 1, cps, 1, 0});
+      for (int cps : {1, 2, 4}) trial(Shape{TY, ring, 1, cps, 1, 0, 1});
   }
+  // staged-coefficient kernel: band rows a multiple of the rows per thread
+  std::vector<int> srows;
+  for (int TY = 2; TY <= std::min(n, 40); TY += 2) srows.push_back(TY);
+  for (int TY : srows)
+    for (int yr : {1, 2, 4})
+      for (int nc : {1, 2})
+        for (int ring : {8, 16})
+          for (int cring : {2, 4, 8})
+            for (int cps : {1, 2})
+              trial(Shape{TY, ring, yr, cps, 2, cring, nc});
   return best;
 }
 
 void applyH32(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
               int ncols, float shift, cudaStream_t s) {
-  // NCGM_STENCIL_SHAPE="rows,ring,ppt,ctasPerSM[,kind[,cpa]]" fixes the shape
+  // NCGM_STENCIL_SHAPE="rows,ring,ppt,ctasPerSM[,kind[,cpa[,nc]]]" fixes the
+  // shape
   const char *envp = std::getenv("NCGM_STENCIL_SHAPE");
   const std::string env = envp ? envp : "";
   Shape sh{};
@@ -893,11 +774,12 @@ void applyH32(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
       }
     if (!found) {
       Shape fixed{};
+      fixed.nc = 1;
       int th = 0;
       if (!env.empty() &&
-          std::sscanf(env.c_str(), "%d,%d,%d,%d,%d,%d", &fixed.TY,
+          std::sscanf(env.c_str(), "%d,%d,%d,%d,%d,%d,%d", &fixed.TY,
                       &fixed.ring, &fixed.ppt, &fixed.ctasPerSM, &fixed.kind,
-                      &fixed.cpa) >= 4 &&
+                      &fixed.cpa, &fixed.nc) >= 4 &&
           validShape(ctx->n, fixed, th))
         sh = fixed;
       else

@@ -135,6 +135,7 @@ int ncgm_destroy(ncgm_ctx *ctx) {
   for (auto &s : ctx->sp) {
     if (s.coef64) cudaFree(s.coef64);
     if (s.coef32) cudaFree(s.coef32);
+    if (s.coef32s) cudaFree(s.coef32s);
   }
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);

@@ -40,6 +40,7 @@ void setError(const std::string &msg);
 struct SpeciesFields {
   double *coef64 = nullptr; // ns x 8
   float *coef32 = nullptr;  // ns x 8
+  float *coef32s = nullptr; // 2 x ns x 4: lo halves of all points, then hi
   bool ready = false;
 };
 

@@ -42,11 +42,14 @@ def test_fp32_plane_kernel_error_bound(n):
     assert np.abs(Y32 - ref).max() <= FP32_TOL * np.abs(ref).max()
 
 
-# fixed stencil shapes (rows, ring, ppt, CTAs/SM, kind, coefficient
-# prefetch), bypassing the autotuner: kind 0 = plane-streaming kernel,
-# kind 1 = z-marching kernel
+# fixed stencil shapes (rows, ring, ppt, CTAs/SM, kind, cpa, nc), bypassing
+# the autotuner: kind 0 = plane-streaming kernel (cpa: coefficient
+# prefetch), kind 1 = z-marching kernel, kind 2 = staged-coefficient kernel
+# (ppt: rows per thread, cpa: coefficient ring depth, nc: columns per box)
 SHAPES = ["3,8,1,1,0", "5,16,4,2,0", "10,8,2,1,0,1", "5,16,4,2,0,1",
-          "2,4,1,1,1", "8,8,1,2,1", "12,8,1,1,1", "6,4,1,4,1"]
+          "2,4,1,1,1", "8,8,1,2,1", "12,8,1,1,1", "6,4,1,4,1",
+          "12,8,2,1,2,2,1", "10,8,1,1,2,4,2", "8,8,4,1,2,2,1",
+          "6,8,2,1,2,4,2", "4,8,4,2,2,2,1", "2,8,1,1,2,2,2"]
 
 
 @pytest.mark.parametrize("shape", SHAPES)
@@ -54,11 +57,12 @@ SHAPES = ["3,8,1,1,0", "5,16,4,2,0", "10,8,2,1,0,1", "5,16,4,2,0,1",
 def test_fp32_fixed_shapes(monkeypatch, shape, n):
     """Every kernel form and pipeline depth gives the CSR product (the
     shape is read when a context tunes; shapes invalid for a lattice fall
-    back to the tuner)."""
+    back to the tuner). Five columns: the two-column boxes end on a
+    half-empty box."""
     monkeypatch.setenv("NCGM_STENCIL_SHAPE", shape)
     a = 0.5 * (n - 1) * 0.5
     ctx, H, R = _pair(n, a, 300 + n, True, True, ncols=6)
-    X = random_block(2 * n ** 3, 6, 3 * n)
+    X = random_block(2 * n ** 3, 5, 3 * n)
     Y32 = H.apply(X, abi.FP32)
     ref = R.apply(X)
     assert np.abs(Y32 - ref).max() <= FP32_TOL * np.abs(ref).max()
