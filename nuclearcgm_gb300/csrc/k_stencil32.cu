@@ -204,7 +204,8 @@ __global__ void __launch_bounds__(streamMaxThreads(PPT), 1)
       bool ok = true;
       while (waited < s0 + 4) {
         const int s = waited + 1;
-        if (!mbarWaitSleep(&full[s & rmask], (s >> rlog) & 1u, kLimit)) {
+        if (!mbarWaitBackoff(&full[s & rmask], (s >> rlog) & 1u, kLimit,
+                             kPollNs)) {
           ok = false;
           break;
         }
@@ -365,7 +366,8 @@ __global__ void __launch_bounds__(kMarchThreads, 1)
   auto waitTo = [&](int upto) {
     while (waited < upto) {
       const int s = waited + 1;
-      if (!mbarWaitSleep(&full[s & rmask], (s >> rlog) & 1u, kLimit))
+      if (!mbarWaitBackoff(&full[s & rmask], (s >> rlog) & 1u, kLimit,
+                           kPollNs))
         return false;
       waited = s;
     }

@@ -203,13 +203,15 @@ __global__ void __launch_bounds__(stageMaxThreads(YR, NC), 1)
       bool ok = true;
       while (waited < s0 + 4) {
         const int s = waited + 1;
-        if (!mbarWaitSleep(&full[s & rmask], (s >> rlog) & 1u, kLimit)) {
+        if (!mbarWaitBackoff(&full[s & rmask], (s >> rlog) & 1u, kLimit,
+                             kPollNs)) {
           ok = false;
           break;
         }
         waited = s;
       }
-      if (ok && !mbarWaitSleep(&cfull[c & cmask], (c >> clog) & 1u, kLimit))
+      if (ok && !mbarWaitBackoff(&cfull[c & cmask], (c >> clog) & 1u, kLimit,
+                                 kPollNs))
         ok = false;
       if (!ok || *(volatile int *)&failed) {
         if (lane == 0) {
