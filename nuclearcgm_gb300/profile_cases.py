@@ -3,6 +3,7 @@
 
   python -m nuclearcgm_gb300.profile_cases tcgram      # ncgm_gram, 128 000 x 96
   python -m nuclearcgm_gb300.profile_cases hf_o16      # 4 HF iterations, 16O 30^3
+  python -m nuclearcgm_gb300.profile_cases hf_ca40_tc  # 6 HF iterations, 40Ca 36^3
   python -m nuclearcgm_gb300.profile_cases gcg_step64  # one GCG step, 40^3 x 64
 """
 import sys
@@ -37,6 +38,17 @@ def hf_o16(precision=abi.FP64):
         res.iterations, res.wall_s, res.t_gcg_s, res.t_poisson_s))
 
 
+def hf_ca40_tc(precision=abi.FP32_TC, iterations=6):
+    """Six HF iterations of 40Ca (SLy4, box 20 fm, 36^3) in the mixed
+    tensor-core form."""
+    data = {"functional": "SLy4", "nucleus": {"A": 40, "Z": 20},
+            "box": {"boxSize": 20.0, "axisMeshPoints": 36},
+            "maxIterations": iterations, "energyTol": 0.0}
+    res, _ = hf_run(config.from_input(data, precision=precision))
+    print("iterations %d wall %.3f s (gcg %.3f, poisson %.3f)" % (
+        res.iterations, res.wall_s, res.t_gcg_s, res.t_poisson_s))
+
+
 def gcg_step64(precision=abi.FP64):
     """One GCG iteration on the 40^3 x 64 benchmark workload."""
     a, f, gradf, U, W = workloads.fields(40, 0.5)
@@ -50,7 +62,8 @@ def gcg_step64(precision=abi.FP64):
     ctx.close()
 
 
-CASES = {"tcgram": tcgram, "hf_o16": hf_o16, "gcg_step64": gcg_step64}
+CASES = {"tcgram": tcgram, "hf_o16": hf_o16, "hf_ca40_tc": hf_ca40_tc,
+         "gcg_step64": gcg_step64}
 
 if __name__ == "__main__":
     CASES[sys.argv[1] if len(sys.argv) > 1 else "tcgram"]()
