@@ -161,9 +161,10 @@ static int cholQR2(ncgm_ctx *ctx, const double2 *V, int k, double2 *Q,
   std::vector<int> orig(k);
   std::iota(orig.begin(), orig.end(), 0);
   for (int pass = 0; pass < 2; ++pass) {
-    // mixed form: the first pass's Gram on the tensor cores (FP32-level),
-    // the second in FP64 so the basis is orthonormal to FP64 rounding
-    if (pass == 0 && tcPart)
+    // tensor-core form: both passes' Grams on the tensor cores with exact
+    // digit products (~1e-12 relative; the basis is orthonormal to that
+    // level); otherwise FP64
+    if (tcPart)
       gramTCExact(src, N, cols, src, N, cols, N, G, cols,
                   reinterpret_cast<double *>(tcPart), s);
     else

@@ -2,8 +2,8 @@
 // blocks A (N x p), B (N x q), with the error-free splitting of Ozaki, Ogita,
 // Oishi and Rump (Numer. Algorithms 59, 2012) mapped onto tcgen05 BF16 MMAs.
 //
-// As in k_tcgram.cu the complex product is one real product of the stacked
-// blocks S = [Re A | Im A] (N x 2p) and T = [Re B | Im B] (N x 2q). Every
+// The complex product is one real product of the interleaved blocks S (N x
+// 2p, column 2c = Re A_c, 2c + 1 = Im A_c) and T (N x 2q, same for B). Every
 // column c of S and T is scaled by a power of two 2^-e_c that brings its
 // entries into [-1, 1] (e_c from the column's max-abs, exact), and each
 // scaled value is written as a sum of kDig signed 7-bit integer digits,
@@ -79,11 +79,13 @@ __device__ __forceinline__ bool waitBar(uint64_t *bar, uint32_t phase) {
   return false;
 }
 
+// column c of the interleaved real block: Re (c even) or Im (c odd) of
+// complex column c / 2
 __device__ __forceinline__ double stackedD(const double2 *X, size_t ld, int p,
                                            int c, size_t r) {
-  if (c < p) return X[(size_t)c * ld + r].x;
-  if (c < 2 * p) return X[(size_t)(c - p) * ld + r].y;
-  return 0.0;
+  if (c >= 2 * p) return 0.0;
+  const double2 v = X[(size_t)(c >> 1) * ld + r];
+  return (c & 1) ? v.y : v.x;
 }
 
 // digits of a scaled value: w = round(x 2^(42-e)), |w| < 2^42, written as
@@ -188,36 +190,61 @@ __global__ void __launch_bounds__(kThr, 1)
       break;
     }
     unsigned char *buf = sm + b * kBuf;
-    // stage the digit planes: A rows (kM) then B rows (kN); a warp writes
-    // one 8 x 8 core matrix per step (lane = row & 7, k pair)
-    const int r8 = lane >> 2, k2 = (lane & 3) * 2;
-    for (int g = warp; g < (kM / 8) * (kSlab / 8) + (kN / 8) * (kSlab / 8);
-         g += kThr / 32) {
-      const bool isA = g < (kM / 8) * (kSlab / 8);
-      const int gg = isA ? g : g - (kM / 8) * (kSlab / 8);
-      const int row = (gg >> 2) * 8 + r8, k = (gg & 3) * 8 + k2;
-      float d0[kDig], d1[kDig];
-      for (int h = 0; h < 2; ++h) {
-        const size_t r = r0 + (size_t)s * kSlab + k + h;
-        long long w = 0;
-        if (r < r1) {
-          if (isA) {
-            const int c = mt * kM + row;
-            if (c < 2 * p) w = scaledInt(stackedD(A, lda, p, c, r), eA[c]);
-          } else {
-            const int c = nt * kN + row;
-            if (c < 2 * q) w = scaledInt(stackedD(B, ldb, q, c, r), eB[c]);
+    // stage the digit planes. One warp step covers 8 complex columns x 8
+    // rows: lane (cc = lane >> 2, kp = lane & 3) loads rows 2kp, 2kp + 1 of
+    // complex column cc as double2 (4 lanes read 128 contiguous bytes) and
+    // writes the digits of interleaved rows 2cc (Re) and 2cc + 1 (Im) at
+    // those two k. Steps: 32 for the A tile (64 complex columns x 32 rows),
+    // 16 for B; all of a warp's loads are issued before its digit work.
+    {
+      constexpr int kStepsA = (kM / 16) * (kSlab / 8), kSteps =
+          kStepsA + (kN / 16) * (kSlab / 8);
+      constexpr int kPer = kSteps / (kThr / 32); // 6 steps per warp
+      const int cc = lane >> 2, kp = lane & 3;
+      double2 v[kPer][2];
+#pragma unroll
+      for (int i = 0; i < kPer; ++i) {
+        const int g = warp + i * (kThr / 32);
+        const bool isA = g < kStepsA;
+        const int gg = isA ? g : g - kStepsA;
+        const int col = (gg >> 2) * 8 + cc;        // complex column in tile
+        const int k = (gg & 3) * 8 + 2 * kp;       // slab row
+        const int gcol = isA ? mt * (kM / 2) + col : nt * (kN / 2) + col;
+        const int ncol = isA ? p : q;
+        const double2 *X = isA ? A : B;
+        const size_t ld = isA ? lda : ldb;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const size_t r = r0 + (size_t)s * kSlab + k + h;
+          v[i][h] = (gcol < ncol && r < r1) ? X[(size_t)gcol * ld + r]
+                                            : make_double2(0.0, 0.0);
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < kPer; ++i) {
+        const int g = warp + i * (kThr / 32);
+        const bool isA = g < kStepsA;
+        const int gg = isA ? g : g - kStepsA;
+        const int col = (gg >> 2) * 8 + cc;
+        const int k = (gg & 3) * 8 + 2 * kp;
+        const int gcol = isA ? mt * (kM / 2) + col : nt * (kN / 2) + col;
+        const int ncol = isA ? p : q;
+#pragma unroll
+        for (int part = 0; part < 2; ++part) { // 0: Re, 1: Im
+          const int row = 2 * col + part;        // interleaved tile row
+          const int e = gcol < ncol ? (isA ? eA : eB)[2 * gcol + part] : 0;
+          float d0[kDig], d1[kDig];
+          digits(scaledInt(part ? v[i][0].y : v[i][0].x, e), d0);
+          digits(scaledInt(part ? v[i][1].y : v[i][1].x, e), d1);
+          const uint32_t o = off16(row, k);
+#pragma unroll
+          for (int t = 0; t < kDig; ++t) {
+            unsigned char *plane =
+                isA ? buf + t * kABytes : buf + kDig * kABytes + t * kBBytes;
+            *reinterpret_cast<__nv_bfloat162 *>(plane + o) =
+                __floats2bfloat162_rn(d0[t], d1[t]);
           }
         }
-        digits(w, h ? d1 : d0);
-      }
-      const uint32_t o = off16(row, k);
-      for (int t = 0; t < kDig; ++t) {
-        unsigned char *plane =
-            isA ? buf + t * kABytes
-                : buf + kDig * kABytes + t * kBBytes;
-        __nv_bfloat162 v2 = __floats2bfloat162_rn(d0[t], d1[t]);
-        *reinterpret_cast<__nv_bfloat162 *>(plane + o) = v2;
       }
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -332,8 +359,8 @@ __global__ void exactGramReduce(const double *__restrict__ part, int chunks,
   double re = 0, im = 0;
   for (int ch = 0; ch < chunks; ++ch) {
     const double *P = part + (size_t)ch * H * W;
-    re += P[(size_t)i * W + j] + P[(size_t)(p + i) * W + q + j];
-    im += P[(size_t)i * W + q + j] - P[(size_t)(p + i) * W + j];
+    re += P[(size_t)(2 * i) * W + 2 * j] + P[(size_t)(2 * i + 1) * W + 2 * j + 1];
+    im += P[(size_t)(2 * i) * W + 2 * j + 1] - P[(size_t)(2 * i + 1) * W + 2 * j];
   }
   C[(size_t)j * ldc + i] = make_double2(re, im);
 }
