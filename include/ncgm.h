@@ -274,6 +274,16 @@ int ncgm_hf_run(const ncgm_hf_config *cfg, ncgm_hf_result *res, double *spe_n,
 int ncgm_gram(ncgm_ctx *ctx, const double *A, int p, const double *B, int q,
               double *C, int precision);
 
+/* Y = V C for a block V (N x m, N = 2 n^3, column-major complex<double>)
+ * and a small matrix C (m x k, column-major): the subspace rotation of the
+ * GCG's orthonormalisation and Rayleigh-Ritz steps (the reference forms it
+ * with Eigen products, src/solver/solver.cpp:418-463, 669-677). Host or
+ * device pointers. precision NCGM_FP64: FP64 CUDA cores; NCGM_FP32_TC:
+ * tensor cores with the exact digit products of ncgm_gram (~1e-12 relative
+ * of the column maxima). */
+int ncgm_vc(ncgm_ctx *ctx, const double *V, int m, const double *C, int k,
+            double *Y, int precision);
+
 /* Batch of independent HF runs on one GPU (the reference runs the points of
  * a deformation curve one after another, src/main.cpp:176-185 with
  * Utilities::curve, src/util/utilities.cpp:71-73). Every configuration runs

@@ -146,11 +146,22 @@ double msSince(std::chrono::steady_clock::time_point t0) {
 
 // Orthonormalise the k columns of V (N x k, ld N) into Q with MGS-equivalent
 // dropping (pivot <= 1e-24). Returns kept column count; Q gets them compacted.
+// reads and clears the error word of the exact-digit tensor-core kernels
+static int takeExactErr() {
+  int flag = 0, zero = 0;
+  if (cudaMemcpy(&flag, exactGramErrWord(), sizeof(int),
+                 cudaMemcpyDeviceToHost) != cudaSuccess)
+    return 1;
+  if (flag)
+    cudaMemcpy(exactGramErrWord(), &zero, sizeof(int), cudaMemcpyHostToDevice);
+  return flag;
+}
+
 static int cholQR2(ncgm_ctx *ctx, const double2 *V, int k, double2 *Q,
                    double2 *Q1, double2 *small, double2 *partials,
                    int maxChunks, int *dKeep, int *dIdx, cudaStream_t s,
                    std::vector<int> *keptOrig = nullptr,
-                   float *tcPart = nullptr) {
+                   float *tcPart = nullptr, void *vcPart = nullptr) {
   const size_t N = ctx->N;
   double2 *G = small, *R = small + (size_t)k * k, *T = small + 2 * (size_t)k * k,
           *Tk = small + 3 * (size_t)k * k;
@@ -187,7 +198,10 @@ static int cholQR2(ncgm_ctx *ctx, const double2 *V, int k, double2 *Q,
     gatherSmall<<<(cols * kept + 255) / 256, 256, 0, s>>>(T, cols, cols, dIdx,
                                                           kept, Tk, cols);
     double2 *out = (pass == 0) ? dst : Q;
-    gemmVC(src, N, cols, Tk, cols, kept, out, N, N, 0.0, s);
+    if (vcPart)
+      gemmVCExact(src, N, cols, Tk, cols, kept, out, N, N, vcPart, s);
+    else
+      gemmVC(src, N, cols, Tk, cols, kept, out, N, N, 0.0, s);
     src = out;
     cols = kept;
   }
@@ -237,10 +251,12 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
   char *base = static_cast<char *>(ctx->buf(10, need + 64 * 4096));
   if (!base) return NCGM_ERR_NOMEM;
   float *tcPart = nullptr;
+  void *vcPart = nullptr;
   if (tc) {
     tcPart = static_cast<float *>(ctx->buf(
         11, sizeof(double) * exactGramScratchDoubles(N, vmax, vmax) + 256));
-    if (!tcPart) return NCGM_ERR_NOMEM;
+    vcPart = ctx->buf(31, exactVCScratchBytes(vmax, vmax));
+    if (!tcPart || !vcPart) return NCGM_ERR_NOMEM;
   }
   Carve ar{base};
   double2 *V = ar.take<double2>(N * vmax), *Q = ar.take<double2>(N * vmax),
@@ -486,7 +502,7 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
     }
     const int vcols = nconv + nact + pc + nact;
     int m = cholQR2(ctx, V, vcols, Q, Q1, Gs, partials, (int)maxChunks, dKeep,
-                    dIdx, s, nullptr, tcPart);
+                    dIdx, s, nullptr, tcPart, vcPart);
     if (m < 0) return NCGM_ERR_CUDA;
     if (m == 0) {
       setError("ncgm_gcg: search space collapsed");
@@ -502,8 +518,13 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
       gram(Q, N, m, AV, N, m, N, Ap, m, partials, (int)maxChunks, s);
     heig(Ap, m, m, Cw, Ev, dW, dPerm, dStat, s);
     const int rr = std::min(nev, m);
-    gemmVC(Q, N, m, Ev, m, rr, Xn, N, N, 0.0, s);
-    gemmVC(AV, N, m, Ev, m, rr, AXn, N, N, 0.0, s);
+    if (tc) {
+      gemmVCExact(Q, N, m, Ev, m, rr, Xn, N, N, vcPart, s);
+      gemmVCExact(AV, N, m, Ev, m, rr, AXn, N, N, vcPart, s);
+    } else {
+      gemmVC(Q, N, m, Ev, m, rr, Xn, N, N, 0.0, s);
+      gemmVC(AV, N, m, Ev, m, rr, AXn, N, N, 0.0, s);
+    }
     axpyCols<<<gridN(rr), 256, 0, s>>>(AXn, Xn, N, rr, -shift); // = A Xn
     NCGM_CUDA(cudaMemcpyAsync(hw.data(), dW, sizeof(double) * m,
                               cudaMemcpyDeviceToHost, s));
@@ -599,6 +620,10 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
   for (int k = 0; k < nev; ++k) lamOut[k] = finalL[order[k]];
   NCGM_CUDA(cudaStreamSynchronize(s));
   NCGM_CUDA(cudaGetLastError());
+  if (tc && takeExactErr()) {
+    setError("ncgm_gcg: tensor-core kernel wait timed out");
+    return NCGM_ERR_TIMEOUT;
+  }
   if (stats) {
     int live = 0;
     cudaMemcpyAsync(&live, dLive, sizeof(int), cudaMemcpyDeviceToHost, s);
@@ -731,11 +756,11 @@ extern "C" int ncgm_gram(ncgm_ctx *ctx, const double *A, int p,
   NCGM_CUDA(cudaStreamSynchronize(s));
   NCGM_CUDA(cudaGetLastError());
   int flag = 0;
+  if (precision == NCGM_FP32_TC) flag = takeExactErr();
+  if (precision == NCGM_FP32)
+    NCGM_CUDA(cudaMemcpy(&flag, tcGramErrWord(), sizeof(int),
+                         cudaMemcpyDeviceToHost));
   if (precision != NCGM_FP64) {
-    NCGM_CUDA(cudaMemcpy(&flag,
-                         precision == NCGM_FP32 ? tcGramErrWord()
-                                                : exactGramErrWord(),
-                         sizeof(int), cudaMemcpyDeviceToHost));
     if (flag) {
       setError("ncgm_gram: tensor-core kernel wait timed out");
       return NCGM_ERR_TIMEOUT;
@@ -744,3 +769,47 @@ extern "C" int ncgm_gram(ncgm_ctx *ctx, const double *A, int p,
   return NCGM_OK;
 }
 
+extern "C" int ncgm_vc(ncgm_ctx *ctx, const double *V, int m, const double *C,
+                       int k, double *Y, int precision) {
+  if (!ctx || !V || !C || !Y || m < 1 || k < 1 || m > 4096 || k > 4096 ||
+      (precision != NCGM_FP64 && precision != NCGM_FP32_TC)) {
+    setError("ncgm_vc: bad argument");
+    return NCGM_ERR_ARG;
+  }
+  using namespace ncgm;
+  const size_t N = ctx->N;
+  cudaStream_t s = ctx->stream;
+  auto stage = [&](const double *h, size_t count, int slot) -> double2 * {
+    if (isDevicePtr(h)) return reinterpret_cast<double2 *>(const_cast<double *>(h));
+    auto *d = static_cast<double2 *>(ctx->buf(slot, count * sizeof(double2)));
+    if (d && cudaMemcpyAsync(d, h, count * sizeof(double2),
+                             cudaMemcpyHostToDevice, s) != cudaSuccess)
+      return nullptr;
+    return d;
+  };
+  const double2 *dV = stage(V, N * (size_t)m, 26);
+  const double2 *dC = stage(C, (size_t)m * k, 27);
+  if (!dV || !dC) return NCGM_ERR_NOMEM;
+  const bool devOut = isDevicePtr(Y);
+  double2 *dY = devOut ? reinterpret_cast<double2 *>(Y)
+                       : static_cast<double2 *>(
+                             ctx->buf(28, N * (size_t)k * sizeof(double2)));
+  if (!dY) return NCGM_ERR_NOMEM;
+  if (precision == NCGM_FP32_TC) {
+    void *part = ctx->buf(29, exactVCScratchBytes(m, k));
+    if (!part) return NCGM_ERR_NOMEM;
+    gemmVCExact(dV, N, m, dC, m, k, dY, N, N, part, s);
+  } else {
+    gemmVC(dV, N, m, dC, m, k, dY, N, N, 0.0, s);
+  }
+  if (!devOut)
+    NCGM_CUDA(cudaMemcpyAsync(Y, dY, N * (size_t)k * sizeof(double2),
+                              cudaMemcpyDeviceToHost, s));
+  NCGM_CUDA(cudaStreamSynchronize(s));
+  NCGM_CUDA(cudaGetLastError());
+  if (precision == NCGM_FP32_TC && takeExactErr()) {
+    setError("ncgm_vc: tensor-core kernel wait timed out");
+    return NCGM_ERR_TIMEOUT;
+  }
+  return NCGM_OK;
+}

@@ -27,6 +27,13 @@ void gramTCExact(const double2 *A, size_t lda, int p, const double2 *B,
                  double *scratch, cudaStream_t s);
 size_t exactGramScratchDoubles(size_t N, int p, int q);
 int *exactGramErrWord();
+// Y = V C on the tensor cores with the exact digit products of gramTCExact
+// (~1e-12 relative of the column maxima; k_tcgram_exact.cu). scratch:
+// exactVCScratchBytes(m, k) bytes.
+void gemmVCExact(const double2 *V, size_t ldv, int m, const double2 *C,
+                 int ldc, int k, double2 *Y, size_t ldy, size_t N,
+                 void *scratch, cudaStream_t s);
+size_t exactVCScratchBytes(int m, int k);
 // Y = V C + beta Y (V: N x m with m <= 1600, C: m x k; C is staged in
 // shared memory in blocks of columns).
 void gemmVC(const double2 *V, size_t ldv, int m, const double2 *C, int ldc,

@@ -38,7 +38,8 @@ constexpr int kThr = 256;
 constexpr int kABytes = kM * kSlab * 2;  // one digit plane of A: 8 KB
 constexpr int kBBytes = kN * kSlab * 2;  // one digit plane of B: 4 KB
 constexpr int kBuf = kDig * (kABytes + kBBytes); // 72 KB
-constexpr int kAccBytes = kM * kN * 8;           // FP64 tile: 64 KB
+constexpr int kAccLd = kN + 1;                   // padded row: no bank conflicts
+constexpr int kAccBytes = kM * kAccLd * 8;       // FP64 tile: 65 KB
 constexpr int kSmem = 2 * kBuf + kAccBytes + 64;
 constexpr uint32_t kLBO = 128, kSBO = 512;       // 8 rows x 16 B cores; K 32
 constexpr uint32_t kTmemCols = 512; // kDig levels x kN = 384 -> 512
@@ -90,16 +91,27 @@ __device__ __forceinline__ double stackedD(const double2 *X, size_t ld, int p,
 
 // digits of a scaled value: w = round(x 2^(42-e)), |w| < 2^42, written as
 // sum_t a_t 2^(42-7t) with |a_1| <= 128 and |a_t| <= 64, by integer rounding
-// divisions (exact; the digits are integers, exact in BF16)
+// divisions (exact; the digits are integers, exact in BF16). One 64-bit
+// rounding split w = h 2^21 + l (|l| <= 2^20) leaves 32-bit work: three
+// digits from each half, and 32-bit integer-to-float conversions (the
+// 64-bit conversion runs on the slow FP64 pipe).
+static_assert(kDig == 6, "digits() splits 42 bits as 3 + 3 digits");
 __device__ __forceinline__ void digits(long long w, float d[kDig]) {
+  const long long hh = (w + (1ll << 20)) >> 21;
+  int l = (int)(w - (hh << 21));
+  int h = (int)hh;
 #pragma unroll
-  for (int t = 0; t < kDig - 1; ++t) {
-    const int sh = 35 - 7 * t;
-    const long long a = (w + (1ll << (sh - 1))) >> sh;
+  for (int t = 0; t < 2; ++t) {
+    const int sh = 14 - 7 * t;
+    const int a = (h + (1 << (sh - 1))) >> sh;
     d[t] = (float)a;
-    w -= a << sh;
+    h -= a << sh;
+    const int b = (l + (1 << (sh - 1))) >> sh;
+    d[3 + t] = (float)b;
+    l -= b << sh;
   }
-  d[kDig - 1] = (float)w;
+  d[2] = (float)h;
+  d[5] = (float)l;
 }
 
 // w = round(x 2^(42 - e)) for |x| < 2^e, from the bits of x with integer
@@ -173,7 +185,7 @@ __global__ void __launch_bounds__(kThr, 1)
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sAddr(&mbar[1])));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  for (int e = tid; e < kM * kN; e += kThr) acc[e] = 0.0;
+  for (int e = tid; e < kM * kAccLd; e += kThr) acc[e] = 0.0;
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -316,7 +328,7 @@ __global__ void __launch_bounds__(kThr, 1)
         const double w = ldexp(1.0, -7 * (kDig + 1));
 #pragma unroll
         for (int j = 0; j < 16; ++j)
-          acc[row * kN + c0 + j] += (double)sum[j] * w;
+          acc[row * kAccLd + c0 + j] += (double)sum[j] * w;
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncthreads();
@@ -335,7 +347,7 @@ __global__ void __launch_bounds__(kThr, 1)
       const int gr = mt * kM + row, gc = nt * kN + col;
       if (gr < 2 * p && gc < 2 * q)
         part[((size_t)chunk * 2 * p + gr) * (2 * q) + gc] =
-            acc[e] * scA[gr] * scB[gc];
+            acc[row * kAccLd + col] * scA[gr] * scB[gc];
     }
   } else if (tid == 0) {
     atomicExch(err, 1);
@@ -363,6 +375,259 @@ __global__ void exactGramReduce(const double *__restrict__ part, int chunks,
     im += P[(size_t)(2 * i) * W + 2 * j + 1] - P[(size_t)(2 * i + 1) * W + 2 * j];
   }
   C[(size_t)j * ldc + i] = make_double2(re, im);
+}
+
+// ---------------------------------------------------------------------------
+// Y = V C (V: N x m, C: m x k, complex FP64) with the same exact digit
+// products. Real form: A = V interleaved (N x 2m, column 2c = Re V_c,
+// 2c + 1 = Im V_c), B (2m x 2k) with B[2c][2j] = Re C_cj, B[2c+1][2j] =
+// -Im C_cj, B[2c][2j+1] = Im C_cj, B[2c+1][2j+1] = Re C_cj, so that column
+// 2j of A B is Re Y_j and 2j + 1 is Im Y_j. A's columns are scaled by powers
+// of two 2^-eA (colMaxKernel); the scales move into B, whose columns are
+// scaled again by 2^-eB, and the digits of that B are precomputed once
+// (vcPrepKernel) in the shared-memory image the MMAs read. The reduction
+// (K = 2m <= 512) is a few 32-row slabs; every 8 slabs the level sums fold
+// into FP64. Each CTA owns 128 rows of Y and 64 of its 2k real columns.
+
+// digits of B = diag(2^eA) B0 2^-eB, laid out per (column tile, slab, digit)
+// as the K-major core-matrix image of one 64 x 32 BF16 plane
+__global__ void vcMaxKernel(const double2 *__restrict__ Cm, int ldc, int m,
+                            int k, const int *__restrict__ eA, double *scB,
+                            int *eB) {
+  const int jr = blockIdx.x * blockDim.x + threadIdx.x; // real column of B
+  if (jr >= 2 * k) return;
+  const int j = jr >> 1, b = jr & 1;
+  int emax = -100000;
+  for (int c = 0; c < m; ++c) {
+    const double2 t = Cm[(size_t)j * ldc + c];
+    // rows 2c, 2c+1 of column jr: (Re, -Im) for b = 0, (Im, Re) for b = 1
+    const double v0 = b ? t.y : t.x, v1 = b ? t.x : -t.y;
+    int e0 = -100000, e1 = -100000;
+    if (v0 != 0.0) { frexp(v0, &e0); e0 += eA[2 * c]; }
+    if (v1 != 0.0) { frexp(v1, &e1); e1 += eA[2 * c + 1]; }
+    emax = max(emax, max(e0, e1));
+  }
+  if (emax == -100000) emax = 0; // an all-zero column
+  eB[jr] = emax;                  // |B[., jr]| 2^eA < 2^emax
+  scB[jr] = ldexp(1.0, emax);
+}
+
+__global__ void vcPrepKernel(const double2 *__restrict__ Cm, int ldc, int m,
+                             int k, const int *__restrict__ eA,
+                             const int *__restrict__ eB, int nslab,
+                             unsigned char *__restrict__ dig) {
+  const int ntile = (2 * k + kN - 1) / kN;
+  const size_t total = (size_t)nslab * kSlab * ntile * kN;
+  const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= total) return;
+  const int cr = (int)(e % ((size_t)nslab * kSlab)); // row of B (K index)
+  const int jr = (int)(e / ((size_t)nslab * kSlab)); // column of B
+  long long w = 0;
+  if (cr < 2 * m && jr < 2 * k) {
+    const int c = cr >> 1, a = cr & 1, j = jr >> 1, b = jr & 1;
+    const double2 t = Cm[(size_t)j * ldc + c];
+    const double v = b ? (a ? t.x : t.y) : (a ? -t.y : t.x);
+    // v 2^eA[cr] 2^-eB[jr] scaled to 42 bits: scaledInt(v, eB - eA)
+    w = scaledInt(v, eB[jr] - eA[cr]);
+  }
+  float d[kDig];
+  digits(w, d);
+  const int s = cr / kSlab, kk = cr % kSlab, nt = jr / kN, jj = jr % kN;
+  unsigned char *base =
+      dig + ((size_t)(nt * nslab + s) * kDig) * (size_t)kBBytes;
+  const uint32_t o = off16(jj, kk);
+#pragma unroll
+  for (int t = 0; t < kDig; ++t)
+    *reinterpret_cast<__nv_bfloat16 *>(base + (size_t)t * kBBytes + o) =
+        __float2bfloat16_rn(d[t]);
+}
+
+__global__ void __launch_bounds__(kThr, 1)
+    exactVCKernel(const double2 *__restrict__ V, size_t ldv, int m,
+                  const int *__restrict__ eA,
+                  const unsigned char *__restrict__ dig,
+                  const double *__restrict__ scB, int k, int nslab,
+                  double2 *__restrict__ Y, size_t ldy, size_t N, int *err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  double *acc = reinterpret_cast<double *>(sm + 2 * kBuf);
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + 2 * kBuf + kAccBytes);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int mt = blockIdx.x, nt = blockIdx.y;
+  const size_t r0 = (size_t)mt * kM;
+
+  if (warp == 0) {
+    asm volatile(
+        "tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::
+            "r"(sAddr(tslot)),
+        "r"(kTmemCols)
+        : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;"
+                 ::
+                     : "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sAddr(&mbar[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sAddr(&mbar[1])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (int e = tid; e < kM * kAccLd; e += kThr) acc[e] = 0.0;
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t taddr = *tslot;
+  bool ok = true;
+  __shared__ int nCommitted;
+  int committed = 0;
+
+  for (int s = 0; s < nslab && ok; ++s) {
+    const int b = s & 1;
+    if (s >= 2 && !waitBar(&mbar[b], ((s - 2) >> 1) & 1)) ok = false;
+    if (!__syncthreads_and(ok)) {
+      ok = false;
+      break;
+    }
+    unsigned char *buf = sm + b * kBuf;
+    // A digits: 128 rows x 16 complex columns. A warp step covers 8 rows x
+    // 4 complex columns (one core matrix): lane (r8 = lane >> 2, kp =
+    // lane & 3) loads V[col, row] and writes the (Re, Im) digit pair at
+    // k = 2 col. 64 steps, 8 per warp; loads first.
+    {
+      constexpr int kPer = (kM / 8) * (kSlab / 8) / (kThr / 32);
+      const int r8 = lane >> 2, kp = lane & 3;
+      double2 v[kPer];
+#pragma unroll
+      for (int i = 0; i < kPer; ++i) {
+        const int g = warp + i * (kThr / 32);
+        const int row = (g >> 2) * 8 + r8, col = (g & 3) * 4 + kp;
+        const int gc = s * (kSlab / 2) + col;
+        const size_t r = r0 + row;
+        v[i] = (gc < m && r < N) ? V[(size_t)gc * ldv + r]
+                                 : make_double2(0.0, 0.0);
+      }
+#pragma unroll
+      for (int i = 0; i < kPer; ++i) {
+        const int g = warp + i * (kThr / 32);
+        const int row = (g >> 2) * 8 + r8, col = (g & 3) * 4 + kp;
+        const int gc = s * (kSlab / 2) + col;
+        float d0[kDig], d1[kDig];
+        if (gc < m) {
+          digits(scaledInt(v[i].x, eA[2 * gc]), d0);
+          digits(scaledInt(v[i].y, eA[2 * gc + 1]), d1);
+        } else {
+          digits(0, d0);
+          digits(0, d1);
+        }
+        const uint32_t o = off16(row, 2 * col);
+#pragma unroll
+        for (int t = 0; t < kDig; ++t)
+          *reinterpret_cast<__nv_bfloat162 *>(buf + t * kABytes + o) =
+              __floats2bfloat162_rn(d0[t], d1[t]);
+      }
+    }
+    // B digits: the precomputed image of this (column tile, slab)
+    {
+      const uint4 *src = reinterpret_cast<const uint4 *>(
+          dig + ((size_t)(nt * nslab + s) * kDig) * (size_t)kBBytes);
+      uint4 *dst = reinterpret_cast<uint4 *>(buf + kDig * kABytes);
+      for (int e = tid; e < kDig * kBBytes / 16; e += kThr) dst[e] = src[e];
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t base = sAddr(buf);
+      const bool first = (s % kFold) == 0;
+      for (int ks = 0; ks < kSlab / 16; ++ks) {
+        const uint32_t kofs = ks * 2 * kLBO;
+        for (int t = 0; t < kDig; ++t)
+          for (int u = 0; u + t < kDig; ++u) {
+            const int lev = t + u;
+            const uint64_t ad = smemDesc(base + t * kABytes + kofs);
+            const uint64_t bd =
+                smemDesc(base + kDig * kABytes + u * kBBytes + kofs);
+            const uint32_t accum = (first && ks == 0 && t == 0) ? 0u : 1u;
+            const uint32_t td = taddr + (uint32_t)(lev * kN);
+            asm volatile("{\n .reg .pred pa;\n setp.ne.b32 pa, %4, 0;\n"
+                         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, "
+                         "%3, pa;\n}\n" ::"r"(td),
+                         "l"(ad), "l"(bd), "r"(kIdesc), "r"(accum)
+                         : "memory");
+          }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::"
+                   "cluster.b64 [%0];" ::"r"(sAddr(&mbar[b]))
+                   : "memory");
+      committed = s + 1;
+    }
+    if ((s % kFold) == kFold - 1 || s == nslab - 1) {
+      if (!waitBar(&mbar[b], (s >> 1) & 1)) ok = false;
+      if (!__syncthreads_and(ok)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int lw = warp & 3, row = lw * 32 + lane;
+      const int cBeg = (warp >> 2) * (kN / 2);
+      for (int c0 = cBeg; c0 < cBeg + kN / 2; c0 += 16) {
+        long long sum[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) sum[j] = 0;
+        for (int lev = 0; lev < kDig; ++lev) {
+          uint32_t v[16];
+          const uint32_t ta =
+              taddr + ((uint32_t)(lw * 32) << 16) + (uint32_t)(lev * kN + c0);
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, "
+              "%5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+              : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]),
+                "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]),
+                "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                "=r"(v[14]), "=r"(v[15])
+              : "r"(ta));
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int j = 0; j < 16; ++j)
+            sum[j] = sum[j] * 128 + (long long)__float2int_rn(
+                                         __uint_as_float(v[j]));
+        }
+        const double w = ldexp(1.0, -7 * (kDig + 1));
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          acc[row * kAccLd + c0 + j] += (double)sum[j] * w;
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+    }
+  }
+  if (tid == 0) nCommitted = committed;
+  __syncthreads();
+  if (!ok && nCommitted > 0) {
+    const int last = nCommitted - 1;
+    waitBar(&mbar[last & 1], (last >> 1) & 1);
+  }
+  ok = __syncthreads_and(ok);
+  if (ok) {
+    // Y[j][r] = (acc[r][2j] 2^eB[2j], acc[r][2j+1] 2^eB[2j+1])
+    for (int e = tid; e < kM * (kN / 2); e += kThr) {
+      const int row = e % kM, jc = e / kM;
+      const size_t r = r0 + row;
+      const int jr = nt * kN + 2 * jc;
+      if (r < N && jr < 2 * k)
+        Y[(size_t)(jr >> 1) * ldy + r] =
+            make_double2(acc[row * kAccLd + 2 * jc] * scB[jr],
+                         acc[row * kAccLd + 2 * jc + 1] * scB[jr + 1]);
+    }
+  } else if (tid == 0) {
+    atomicExch(err, 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(
+                     taddr),
+                 "r"(kTmemCols)
+                 : "memory");
 }
 
 int chunkRows(size_t N, int p, int q) {
@@ -418,6 +683,49 @@ void gramTCExact(const double2 *A, size_t lda, int p, const double2 *B,
                                             exactGramErrWord());
   exactGramReduce<<<(p * q + 127) / 128, 128, 0, s>>>(part, chunks, p, q, C,
                                                       ldc);
+}
+
+// scratch of gemmVCExact in bytes: A column scales / exponents (2m), B
+// column scales / exponents (2k), the digit image of B
+size_t exactVCScratchBytes(int m, int k) {
+  const size_t nslab = (2 * (size_t)m + kSlab - 1) / kSlab;
+  const size_t ntile = (2 * (size_t)k + kN - 1) / kN;
+  return 256 + 16 * (size_t)(2 * m + 2 * k) + ntile * nslab * kDig * kBBytes;
+}
+
+// Y = V C (beta = 0) to ~1e-12 relative of the column maxima (see above)
+void gemmVCExact(const double2 *V, size_t ldv, int m, const double2 *Cm,
+                 int ldc, int k, double2 *Y, size_t ldy, size_t N,
+                 void *scratch, cudaStream_t s) {
+  if (k == 0 || N == 0) return;
+  if (m == 0) {
+    for (int j = 0; j < k; ++j)
+      cudaMemsetAsync(Y + (size_t)j * ldy, 0, N * sizeof(double2), s);
+    return;
+  }
+  static const bool attr = [] {
+    cudaFuncSetAttribute(exactVCKernel,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
+    return true;
+  }();
+  (void)attr;
+  const int nslab = (2 * m + kSlab - 1) / kSlab;
+  const int ntile = (2 * k + kN - 1) / kN;
+  unsigned char *base = static_cast<unsigned char *>(scratch);
+  double *scA = reinterpret_cast<double *>(base);
+  double *scB = scA + 2 * (size_t)m;
+  int *eA = reinterpret_cast<int *>(scB + 2 * (size_t)k);
+  int *eB = eA + 2 * (size_t)m;
+  unsigned char *dig =
+      base + (((size_t)16 * (2 * m + 2 * k) + 255) & ~(size_t)255);
+  colMaxKernel<<<2 * m, 256, 0, s>>>(V, ldv, m, N, scA, eA);
+  vcMaxKernel<<<(2 * k + 127) / 128, 128, 0, s>>>(Cm, ldc, m, k, eA, scB, eB);
+  const size_t total = (size_t)nslab * kSlab * ntile * kN;
+  vcPrepKernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(
+      Cm, ldc, m, k, eA, eB, nslab, dig);
+  dim3 grid((unsigned)((N + kM - 1) / kM), ntile);
+  exactVCKernel<<<grid, kThr, kSmem, s>>>(V, ldv, m, eA, dig, scB, k, nslab, Y,
+                                          ldy, N, exactGramErrWord());
 }
 
 } // namespace ncgm
