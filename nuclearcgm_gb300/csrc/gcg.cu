@@ -300,7 +300,7 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
                             cudaMemcpyDeviceToDevice, s));
   std::vector<int> keptInit;
   int nkept = cholQR2(ctx, V, nev, Q, Q1, Gs, partials, (int)maxChunks, dKeep,
-                      dIdx, s, &keptInit);
+                      dIdx, s, &keptInit, tcPart, vcPart);
   if (nkept < 0) return NCGM_ERR_CUDA;
   if (nkept == 0) {
     setError("ncgm_gcg: initial block has no independent columns");
@@ -321,13 +321,23 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
   // initial Rayleigh-Ritz (rayleighRitz_complex_no_B, solver.cpp:418-463)
   {
     applyA(Xa, AV, nx, shift);
-    gram(Xa, N, nx, AV, N, nx, N, Ap, nx, partials, (int)maxChunks, s);
+    if (tc)
+      gramTCExact(Xa, N, nx, AV, N, nx, N, Ap, nx,
+                  reinterpret_cast<double *>(tcPart), s);
+    else
+      gram(Xa, N, nx, AV, N, nx, N, Ap, nx, partials, (int)maxChunks, s);
     heig(Ap, nx, nx, Cw, Ev, dW, dPerm, dStat, s);
-    gemmVC(Xa, N, nx, Ev, nx, nx, Xn, N, N, 0.0, s);
+    if (tc)
+      gemmVCExact(Xa, N, nx, Ev, nx, nx, Xn, N, N, vcPart, s);
+    else
+      gemmVC(Xa, N, nx, Ev, nx, nx, Xn, N, N, 0.0, s);
     NCGM_CUDA(cudaMemcpyAsync(Xa, Xn, N * (size_t)nx * sizeof(double2),
                               cudaMemcpyDeviceToDevice, s));
     // A X of the rotated block (shift removed), kept for the FP32 correction
-    gemmVC(AV, N, nx, Ev, nx, nx, AXa, N, N, 0.0, s);
+    if (tc)
+      gemmVCExact(AV, N, nx, Ev, nx, nx, AXa, N, N, vcPart, s);
+    else
+      gemmVC(AV, N, nx, Ev, nx, nx, AXa, N, N, 0.0, s);
     if (shift != 0.0)
       axpyCols<<<gridN(nx), 256, 0, s>>>(AXa, Xa, N, nx, -shift);
     NCGM_CUDA(cudaMemcpyAsync(hw.data(), dW, sizeof(double) * nx,

@@ -396,8 +396,100 @@ void gemmVC(const double2 *V, size_t ldv, int m, const double2 *Cm, int ldc,
   }
 }
 
+// Same factorisation in shared memory, right-looking: at step j the pivot is
+// the updated diagonal A_jj = G_jj - sum_{k<j} |R_kj|^2, row j of R is
+// A_j. / R_jj, and the trailing upper triangle takes the rank-1 update
+// A_ab -= conj(R_ja) R_jb in parallel (one barrier-separated phase per
+// step instead of a serial dot product per element). The drop rule and
+// T = R^{-1} are those of cholDropKernel.
+constexpr int kCholSmemMax = 80; // 2 m^2 double2 <= 200 KB
+__global__ void cholDropSmemKernel(const double2 *G, int ldg, int m,
+                                   double dropTol, double2 *R, double2 *T,
+                                   int *keep) {
+  extern __shared__ double2 csm[];
+  double2 *A = csm;          // m x m column-major; upper triangle -> R
+  double2 *Ts = csm + m * m; // T
+  __shared__ int kp[kCholSmemMax];
+  __shared__ double piv;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < m * m; e += nt) {
+    A[e] = G[(size_t)(e / m) * ldg + (e % m)];
+    Ts[e] = make_double2(0, 0);
+  }
+  __syncthreads();
+  for (int j = 0; j < m; ++j) {
+    if (tid == 0) {
+      const double d = A[(size_t)j * m + j].x;
+      const double gjj = G[(size_t)j * ldg + j].x;
+      const double floor = fmax(dropTol, 64.0 * 2.220446049250313e-16 * gjj);
+      const int k = (d > floor) ? 1 : 0;
+      kp[j] = k;
+      keep[j] = k;
+      piv = k ? d : 0.0;
+    }
+    __syncthreads();
+    const double pv = piv;
+    if (pv > 0.0) {
+      const double rjj = sqrt(pv);
+      for (int i = j + 1 + tid; i < m; i += nt) {
+        const double2 a = A[(size_t)i * m + j];
+        A[(size_t)i * m + j] = make_double2(a.x / rjj, a.y / rjj);
+      }
+      if (tid == 0) A[(size_t)j * m + j] = make_double2(rjj, 0.0);
+      __syncthreads();
+      const int w = m - j - 1;
+      for (int e = tid; e < w * w; e += nt) {
+        const int a = j + 1 + e % w, b = j + 1 + e / w;
+        if (a <= b) {
+          const double2 t = cconjmul(A[(size_t)a * m + j], A[(size_t)b * m + j]);
+          double2 &x = A[(size_t)b * m + a];
+          x.x -= t.x;
+          x.y -= t.y;
+        }
+      }
+    } else {
+      for (int i = j + tid; i < m; i += nt) A[(size_t)i * m + j] = make_double2(0, 0);
+    }
+    __syncthreads();
+  }
+  // T = R^{-1} on the kept columns, one thread per column of T
+  for (int c = tid; c < m; c += nt) {
+    if (!kp[c]) continue;
+    for (int i = c; i >= 0; --i) {
+      if (!kp[i]) continue;
+      double2 sum = make_double2(i == c ? 1.0 : 0.0, 0.0);
+      for (int k = i + 1; k <= c; ++k) {
+        if (!kp[k]) continue;
+        const double2 t = cmul(A[(size_t)k * m + i], Ts[(size_t)c * m + k]);
+        sum.x -= t.x;
+        sum.y -= t.y;
+      }
+      const double rii = A[(size_t)i * m + i].x;
+      Ts[(size_t)c * m + i] = make_double2(sum.x / rii, sum.y / rii);
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < m * m; e += nt) {
+    const int row = e % m, col = e / m;
+    R[e] = row <= col ? A[e] : make_double2(0, 0);
+    T[e] = Ts[e];
+  }
+}
+
 void cholDrop(const double2 *G, int ldg, int m, double dropTol, double2 *R,
               double2 *T, int *keep, cudaStream_t s) {
+  if (m <= kCholSmemMax) {
+    static const bool attr = [] {
+      cudaFuncSetAttribute(cholDropSmemKernel,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           2 * kCholSmemMax * kCholSmemMax * (int)sizeof(double2));
+      return true;
+    }();
+    (void)attr;
+    cholDropSmemKernel<<<1, 256, 2 * (size_t)m * m * sizeof(double2), s>>>(
+        G, ldg, m, dropTol, R, T, keep);
+    return;
+  }
   cholDropKernel<<<1, 256, 0, s>>>(G, ldg, m, dropTol, R, T, keep);
 }
 

@@ -26,6 +26,8 @@
 
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 namespace ncgm {
 
 namespace {
@@ -80,14 +82,6 @@ __device__ __forceinline__ bool waitBar(uint64_t *bar, uint32_t phase) {
   return false;
 }
 
-// column c of the interleaved real block: Re (c even) or Im (c odd) of
-// complex column c / 2
-__device__ __forceinline__ double stackedD(const double2 *X, size_t ld, int p,
-                                           int c, size_t r) {
-  if (c >= 2 * p) return 0.0;
-  const double2 v = X[(size_t)(c >> 1) * ld + r];
-  return (c & 1) ? v.y : v.x;
-}
 
 // digits of a scaled value: w = round(x 2^(42-e)), |w| < 2^42, written as
 // sum_t a_t 2^(42-7t) with |a_1| <= 128 and |a_t| <= 64, by integer rounding
@@ -129,27 +123,54 @@ __device__ __forceinline__ long long scaledInt(double x, int e) {
   return bits < 0 ? -w : w;
 }
 
-// per column of the stacked block X (N x 2p): the power of two sc[c] = 2^e
-// above its max-abs, and its exponent ex[c] = e (one block per column)
+// per column c of the interleaved block X (N x 2p): the power of two
+// sc[c] = 2^e above its max-abs, and e = ex[c]. Pass 1: blocks (complex
+// column, row chunk) fold |Re| and |Im| maxima into sc as IEEE bit patterns
+// (for non-negative doubles the integer order is the numeric order); pass
+// 2 turns them into exponents.
 __global__ void colMaxKernel(const double2 *X, size_t ld, int p, size_t N,
-                             double *mx, int *exq) {
-  __shared__ double sh[256];
+                             size_t rowsPerBlock, double *sc) {
+  __shared__ double sh[2][256];
   const int c = blockIdx.x;
-  double m = 0;
-  for (size_t r = threadIdx.x; r < N; r += blockDim.x)
-    m = fmax(m, fabs(stackedD(X, ld, p, c, r)));
-  sh[threadIdx.x] = m;
+  const size_t r0 = (size_t)blockIdx.y * rowsPerBlock;
+  const size_t r1 = r0 + rowsPerBlock < N ? r0 + rowsPerBlock : N;
+  double mr = 0, mi = 0;
+  for (size_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+    const double2 v = X[(size_t)c * ld + r];
+    mr = fmax(mr, fabs(v.x));
+    mi = fmax(mi, fabs(v.y));
+  }
+  sh[0][threadIdx.x] = mr;
+  sh[1][threadIdx.x] = mi;
   __syncthreads();
   for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + s]);
+    if (threadIdx.x < s) {
+      sh[0][threadIdx.x] = fmax(sh[0][threadIdx.x], sh[0][threadIdx.x + s]);
+      sh[1][threadIdx.x] = fmax(sh[1][threadIdx.x], sh[1][threadIdx.x + s]);
+    }
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    int e = 0;
-    if (sh[0] > 0) frexp(sh[0], &e); // sh[0] < 2^e
-    mx[c] = ldexp(1.0, e);           // column scale: entries / mx in (-1, 1)
-    exq[c] = e;
-  }
+  if (threadIdx.x < 2)
+    atomicMax(reinterpret_cast<unsigned long long *>(sc) + 2 * c + threadIdx.x,
+              (unsigned long long)__double_as_longlong(sh[threadIdx.x][0]));
+}
+__global__ void colExpKernel(int cols, double *sc, int *exq) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cols) return;
+  const double m = sc[c]; // the bit pattern written by colMaxKernel
+  int e = 0;
+  if (m > 0) frexp(m, &e); // m < 2^e
+  sc[c] = ldexp(1.0, e);   // column scale: entries / sc in (-1, 1)
+  exq[c] = e;
+}
+// column maxima of the p complex columns of X (2p interleaved real columns)
+void colMax(const double2 *X, size_t ld, int p, size_t N, double *sc, int *ex,
+            cudaStream_t s) {
+  const int chunks = (int)std::min<size_t>(16, (N + 4095) / 4096);
+  const size_t rows = (N + chunks - 1) / chunks;
+  cudaMemsetAsync(sc, 0, 2 * (size_t)p * sizeof(double), s);
+  colMaxKernel<<<dim3(p, chunks), 256, 0, s>>>(X, ld, p, N, rows, sc);
+  colExpKernel<<<(2 * p + 127) / 128, 128, 0, s>>>(2 * p, sc, ex);
 }
 
 __global__ void __launch_bounds__(kThr, 1)
@@ -673,8 +694,8 @@ void gramTCExact(const double2 *A, size_t lda, int p, const double2 *B,
   int *eA = reinterpret_cast<int *>(scB + 2 * (size_t)q);
   int *eB = eA + 2 * (size_t)p;
   double *part = scB + 4 * (size_t)q + 2 * (size_t)p + 8;
-  colMaxKernel<<<2 * p, 256, 0, s>>>(A, lda, p, N, scA, eA);
-  colMaxKernel<<<2 * q, 256, 0, s>>>(B, ldb, q, N, scB, eB);
+  colMax(A, lda, p, N, scA, eA, s);
+  colMax(B, ldb, q, N, scB, eB, s);
   const int rows = chunkRows(N, p, q);
   const int chunks = (int)((N + rows - 1) / rows);
   dim3 grid((2 * p + kM - 1) / kM, (2 * q + kN - 1) / kN, chunks);
@@ -718,7 +739,7 @@ void gemmVCExact(const double2 *V, size_t ldv, int m, const double2 *Cm,
   int *eB = eA + 2 * (size_t)m;
   unsigned char *dig =
       base + (((size_t)16 * (2 * m + 2 * k) + 255) & ~(size_t)255);
-  colMaxKernel<<<2 * m, 256, 0, s>>>(V, ldv, m, N, scA, eA);
+  colMax(V, ldv, m, N, scA, eA, s);
   vcMaxKernel<<<(2 * k + 127) / 128, 128, 0, s>>>(Cm, ldc, m, k, eA, scB, eB);
   const size_t total = (size_t)nslab * kSlab * ntile * kN;
   vcPrepKernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(
