@@ -326,7 +326,7 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
                   reinterpret_cast<double *>(tcPart), s);
     else
       gram(Xa, N, nx, AV, N, nx, N, Ap, nx, partials, (int)maxChunks, s);
-    heig(Ap, nx, nx, Cw, Ev, dW, dPerm, dStat, s);
+    heig(Ap, nx, nx, Cw, Ev, dW, dPerm, dStat, s, fp32);
     if (tc)
       gemmVCExact(Xa, N, nx, Ev, nx, nx, Xn, N, N, vcPart, s);
     else
@@ -526,7 +526,7 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
                   reinterpret_cast<double *>(tcPart), s);
     else
       gram(Q, N, m, AV, N, m, N, Ap, m, partials, (int)maxChunks, s);
-    heig(Ap, m, m, Cw, Ev, dW, dPerm, dStat, s);
+    heig(Ap, m, m, Cw, Ev, dW, dPerm, dStat, s, fp32);
     const int rr = std::min(nev, m);
     if (tc) {
       gemmVCExact(Q, N, m, Ev, m, rr, Xn, N, N, vcPart, s);

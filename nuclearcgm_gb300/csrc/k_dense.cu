@@ -12,6 +12,7 @@
 #include "k_dense.cuh"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 
 namespace ncgm {
@@ -183,52 +184,17 @@ __global__ void cholDropKernel(const double2 *G, int ldg, int m,
   }
 }
 
-// One CTA parallel-order Jacobi (round-robin pairing: every round rotates
-// m/2 disjoint (p,q) pairs at once, m-1 rounds per sweep) on a Hermitian
-// m x m matrix whose lower triangle is read. A, Vm: m x m workspaces;
-// w: eigenvalues ascending; Vm: eigenvectors in the same order.
-__global__ void heigKernel(const double2 *Ain, int lda, int m, double2 *Ag,
-                           double2 *Vg, double *w, int *perm, int *status,
-                           int useSmem) {
-  // working copies in shared memory when they fit: useSmem 2 = A and V
-  // (m <= 81), 1 = A only (m <= 114), 0 = both in the global work buffers
-  extern __shared__ double2 hsm[];
-  double2 *A = useSmem ? hsm : Ag;
-  double2 *Vm = useSmem == 2 ? hsm + (size_t)m * m : Vg;
+// FP64 cyclic Jacobi sweeps sweep0 .. 59 on the Hermitian A (m x m,
+// column-major), rotations accumulated into Vm (round-robin pairing: every
+// round rotates m/2 disjoint (p,q) pairs at once). Returns 1 on convergence.
+__device__ int jacobiSweeps64(double2 *A, double2 *Vm, int m, double fro,
+                              int sweep0, int *P, int *Q, double *C,
+                              double *S, double2 *E, double *red) {
   const int tid = threadIdx.x, nt = blockDim.x;
-  for (int e = tid; e < m * m; e += nt) {
-    int i = e % m, j = e / m;
-    double2 v;
-    if (i > j) v = Ain[(size_t)j * lda + i];
-    else if (i < j) {
-      double2 l = Ain[(size_t)i * lda + j];
-      v = make_double2(l.x, -l.y);
-    } else v = make_double2(Ain[(size_t)j * lda + i].x, 0.0);
-    A[e] = v;
-    Vm[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
-  }
   const int mp = (m % 2) ? m + 1 : m; // players incl. a dummy for odd m
   const int npairs = mp / 2;
-  __shared__ int P[256], Q[256];
-  __shared__ double C[256], S[256];
-  __shared__ double2 E[256];
-  __shared__ double red[512]; // blockDim.x <= 512
-  __syncthreads();
-  double fro = 0;
-  {
-    double loc = 0;
-    for (int e = tid; e < m * m; e += nt) loc += A[e].x * A[e].x + A[e].y * A[e].y;
-    red[tid] = loc;
-    __syncthreads();
-    for (int st = nt / 2; st > 0; st >>= 1) {
-      if (tid < st) red[tid] += red[tid + st];
-      __syncthreads();
-    }
-    fro = red[0];
-    __syncthreads();
-  }
   int converged = 0;
-  for (int sweep = 0; sweep < 60; ++sweep) {
+  for (int sweep = sweep0; sweep < 60; ++sweep) {
     double loc = 0;
     for (int e = tid; e < m * m; e += nt) {
       int i = e % m, j = e / m;
@@ -320,6 +286,16 @@ __global__ void heigKernel(const double2 *Ain, int lda, int m, double2 *Ag,
       __syncthreads();
     }
   }
+  return converged;
+}
+
+// ascending order of the diagonal (stable insertion sort by thread 0),
+// eigenvalues w, status, and the permuted eigenvectors written to Vg (A is
+// reused as the staging copy)
+__device__ void jacobiFinish(double2 *A, const double2 *Vm, int m,
+                             int converged, double2 *Vg, double *w, int *perm,
+                             int *status) {
+  const int tid = threadIdx.x, nt = blockDim.x;
   // sort ascending (stable insertion sort by thread 0), permute eigenvectors
   if (tid == 0) {
     for (int i = 0; i < m; ++i) perm[i] = i;
@@ -343,6 +319,253 @@ __global__ void heigKernel(const double2 *Ain, int lda, int m, double2 *Ag,
   }
   __syncthreads();
   for (int e = tid; e < m * m; e += nt) Vg[e] = A[e];
+}
+
+
+// One CTA parallel-order Jacobi (round-robin pairing: every round rotates
+// m/2 disjoint (p,q) pairs at once, m-1 rounds per sweep) on a Hermitian
+// m x m matrix whose lower triangle is read. A, Vm: m x m workspaces;
+// w: eigenvalues ascending; Vm: eigenvectors in the same order.
+__global__ void heigKernel(const double2 *Ain, int lda, int m, double2 *Ag,
+                           double2 *Vg, double *w, int *perm, int *status,
+                           int useSmem) {
+  // working copies in shared memory when they fit: useSmem 2 = A and V
+  // (m <= 81), 1 = A only (m <= 114), 0 = both in the global work buffers
+  extern __shared__ double2 hsm[];
+  double2 *A = useSmem ? hsm : Ag;
+  double2 *Vm = useSmem == 2 ? hsm + (size_t)m * m : Vg;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < m * m; e += nt) {
+    int i = e % m, j = e / m;
+    double2 v;
+    if (i > j) v = Ain[(size_t)j * lda + i];
+    else if (i < j) {
+      double2 l = Ain[(size_t)i * lda + j];
+      v = make_double2(l.x, -l.y);
+    } else v = make_double2(Ain[(size_t)j * lda + i].x, 0.0);
+    A[e] = v;
+    Vm[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+  }
+  __shared__ int P[256], Q[256];
+  __shared__ double C[256], S[256];
+  __shared__ double2 E[256];
+  __shared__ double red[512]; // blockDim.x <= 512
+  __syncthreads();
+  double fro = 0;
+  {
+    double loc = 0;
+    for (int e = tid; e < m * m; e += nt) loc += A[e].x * A[e].x + A[e].y * A[e].y;
+    red[tid] = loc;
+    __syncthreads();
+    for (int st = nt / 2; st > 0; st >>= 1) {
+      if (tid < st) red[tid] += red[tid + st];
+      __syncthreads();
+    }
+    fro = red[0];
+    __syncthreads();
+  }
+  const int converged =
+      jacobiSweeps64(A, Vm, m, fro, 0, P, Q, C, S, E, red);
+  jacobiFinish(A, Vm, m, converged, Vg, w, perm, status);
+}
+
+// ---- double-float (df64) form of the Jacobi eigensolver ----
+// GB300's FP64 pipe retires 2 FMAs per clock per SM, its FP32 pipe 128, so
+// the one-CTA Jacobi is FP64-throughput-bound (about 19 k cycles per round at
+// m = 60). Here the rotation updates, most of the work, run in double-float
+// arithmetic: a value is an unevaluated sum hi + lo of two floats (~48-bit
+// significand), with Knuth's two-sum and the FMA two-product (Dekker; Hida,
+// Li and Bailey's double-double algorithms, restated for float pairs). The
+// rotation parameters and the convergence test stay FP64. Accumulated
+// rounding over a few hundred rotations per element: ~1e-13 relative. The
+// double-float sweeps stop at an off-diagonal norm of 1e-12 relative; the
+// matrices are then converted in place to FP64 and the FP64 sweeps finish
+// (one or two sweeps from there, as Jacobi converges quadratically).
+struct dfl {
+  float hi, lo;
+};
+struct dfc {
+  dfl re, im;
+};
+// The operations of the error-free transformations use the _rn intrinsics,
+// which the compiler never contracts into FMAs (a contracted p + e in the
+// product, for instance, loses the low part: 1e-9 instead of 1e-13).
+__device__ __forceinline__ dfl dfAdd(dfl a, dfl b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float v = __fsub_rn(s, a.hi);
+  float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)), __fsub_rn(b.hi, v));
+  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  const float h = __fadd_rn(s, e);
+  return {h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+__device__ __forceinline__ dfl dfNeg(dfl a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ dfl dfMul(dfl a, dfl b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  const float h = __fadd_rn(p, e);
+  return {h, __fsub_rn(e, __fsub_rn(h, p))};
+}
+__device__ __forceinline__ dfl dfFrom(double x) {
+  const float h = __double2float_rn(x);
+  return {h, __double2float_rn(__dsub_rn(x, (double)h))};
+}
+__device__ __forceinline__ double dfTo(dfl a) { return (double)a.hi + (double)a.lo; }
+// c x - s (w y), s x + c (w y) for complex x, y, w and real c, s
+__device__ __forceinline__ void dfRot(dfc &x, dfc &y, dfl c, dfl s, dfc w) {
+  const dfc t = {dfAdd(dfMul(w.re, y.re), dfNeg(dfMul(w.im, y.im))),
+                 dfAdd(dfMul(w.re, y.im), dfMul(w.im, y.re))};
+  const dfc nx = {dfAdd(dfMul(c, x.re), dfNeg(dfMul(s, t.re))),
+                  dfAdd(dfMul(c, x.im), dfNeg(dfMul(s, t.im)))};
+  const dfc ny = {dfAdd(dfMul(s, x.re), dfMul(c, t.re)),
+                  dfAdd(dfMul(s, x.im), dfMul(c, t.im))};
+  x = nx;
+  y = ny;
+}
+
+constexpr int kHeigDfMax = 80; // A and V in shared memory: 2 m^2 x 16 B
+// Same algorithm, pairing and output as heigKernel, with A and V held as
+// double-float complex values in shared memory.
+__global__ void heigDfKernel(const double2 *Ain, int lda, int m, double2 *Vg,
+                             double *w, int *perm, int *status) {
+  extern __shared__ dfc dsm[];
+  dfc *A = dsm, *Vm = dsm + (size_t)m * m;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < m * m; e += nt) {
+    const int i = e % m, j = e / m;
+    double2 v;
+    if (i > j) v = Ain[(size_t)j * lda + i];
+    else if (i < j) {
+      const double2 l = Ain[(size_t)i * lda + j];
+      v = make_double2(l.x, -l.y);
+    } else v = make_double2(Ain[(size_t)j * lda + i].x, 0.0);
+    A[e] = {dfFrom(v.x), dfFrom(v.y)};
+    Vm[e] = {{i == j ? 1.f : 0.f, 0.f}, {0.f, 0.f}};
+  }
+  const int mp = (m % 2) ? m + 1 : m;
+  const int npairs = mp / 2;
+  __shared__ int P[kHeigDfMax / 2 + 1], Q[kHeigDfMax / 2 + 1];
+  __shared__ dfl C[kHeigDfMax / 2 + 1], S[kHeigDfMax / 2 + 1];
+  __shared__ dfc E[kHeigDfMax / 2 + 1];
+  __shared__ int act[kHeigDfMax / 2 + 1];
+  __shared__ double red[512];
+  __syncthreads();
+  auto mag2 = [](const dfc &a) {
+    const double x = dfTo(a.re), y = dfTo(a.im);
+    return x * x + y * y;
+  };
+  double fro;
+  {
+    double loc = 0;
+    for (int e = tid; e < m * m; e += nt) loc += mag2(A[e]);
+    red[tid] = loc;
+    __syncthreads();
+    for (int st = nt / 2; st > 0; st >>= 1) {
+      if (tid < st) red[tid] += red[tid + st];
+      __syncthreads();
+    }
+    fro = red[0];
+    __syncthreads();
+  }
+  int dfSweeps = 0;
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double loc = 0;
+    for (int e = tid; e < m * m; e += nt) {
+      const int i = e % m, j = e / m;
+      if (i > j) loc += mag2(A[e]);
+    }
+    red[tid] = loc;
+    __syncthreads();
+    for (int st = nt / 2; st > 0; st >>= 1) {
+      if (tid < st) red[tid] += red[tid + st];
+      __syncthreads();
+    }
+    const double off = red[0];
+    __syncthreads();
+    if (off <= 1e-24 * fro || off == 0.0) break;
+    ++dfSweeps;
+    for (int r = 0; r < mp - 1; ++r) {
+      for (int k = tid; k < npairs; k += nt) {
+        int a, b;
+        if (k == 0) {
+          a = mp - 1;
+          b = r;
+        } else {
+          a = (r + k) % (mp - 1);
+          b = (r - k + (mp - 1)) % (mp - 1);
+        }
+        const int p = min(a, b), q = max(a, b);
+        P[k] = p;
+        Q[k] = q;
+        act[k] = 0;
+        if (q < m) {
+          const dfc apqd = A[(size_t)q * m + p];
+          const double ax = dfTo(apqd.re), ay = dfTo(apqd.im);
+          const double mag = sqrt(ax * ax + ay * ay);
+          const double app = dfTo(A[(size_t)p * m + p].re),
+                       aqq = dfTo(A[(size_t)q * m + q].re);
+          if (mag != 0.0 &&
+              !(sweep > 3 && mag < 1e-18 * sqrt(fabs(app * aqq)) + 1e-300)) {
+            const double tau = (aqq - app) / (2.0 * mag);
+            const double t = (tau >= 0 ? 1.0 : -1.0) /
+                             (fabs(tau) + sqrt(1.0 + tau * tau));
+            const double c = 1.0 / sqrt(1.0 + t * t);
+            C[k] = dfFrom(c);
+            S[k] = dfFrom(t * c);
+            E[k] = {dfFrom(ax / mag), dfFrom(ay / mag)};
+            act[k] = 1;
+          }
+        }
+      }
+      __syncthreads();
+      // A <- A U and V <- V U: thread per (row, pair); U mixes columns p, q
+      // with conj(e) on column q
+      for (int e = tid; e < m * npairs; e += nt) {
+        const int row = e % m, k = e / m;
+        if (!act[k]) continue;
+        const int p = P[k], q = Q[k];
+        const dfc ec = {E[k].re, dfNeg(E[k].im)};
+        dfRot(A[(size_t)p * m + row], A[(size_t)q * m + row], C[k], S[k], ec);
+        dfRot(Vm[(size_t)p * m + row], Vm[(size_t)q * m + row], C[k], S[k],
+              ec);
+      }
+      __syncthreads();
+      // A <- U^H A: thread per (pair, column); rows p, q with e on row q
+      for (int e = tid; e < m * npairs; e += nt) {
+        const int col = e % m, k = e / m;
+        if (!act[k]) continue;
+        const int p = P[k], q = Q[k];
+        dfRot(A[(size_t)col * m + p], A[(size_t)col * m + q], C[k], S[k],
+              E[k]);
+      }
+      __syncthreads();
+      for (int k = tid; k < npairs; k += nt) {
+        if (!act[k]) continue;
+        const int p = P[k], q = Q[k];
+        A[(size_t)q * m + p] = {{0.f, 0.f}, {0.f, 0.f}};
+        A[(size_t)p * m + q] = {{0.f, 0.f}, {0.f, 0.f}};
+        A[(size_t)p * m + p].im = {0.f, 0.f};
+        A[(size_t)q * m + q].im = {0.f, 0.f};
+      }
+      __syncthreads();
+    }
+  }
+  // in place to FP64 (a dfc and a double2 are both 16 bytes; every thread
+  // converts the elements it reads), then the FP64 sweeps
+  double2 *A64 = reinterpret_cast<double2 *>(A);
+  double2 *V64 = reinterpret_cast<double2 *>(Vm);
+  for (int e = tid; e < m * m; e += nt) {
+    const dfc a = A[e], v = Vm[e];
+    A64[e] = make_double2(dfTo(a.re), dfTo(a.im));
+    V64[e] = make_double2(dfTo(v.re), dfTo(v.im));
+  }
+  __syncthreads();
+  __shared__ double C64[kHeigDfMax / 2 + 1], S64[kHeigDfMax / 2 + 1];
+  __shared__ double2 E64[kHeigDfMax / 2 + 1];
+  const int converged =
+      jacobiSweeps64(A64, V64, m, fro, dfSweeps, P, Q, C64, S64, E64, red);
+  jacobiFinish(A64, V64, m, converged, Vg, w, perm, status);
 }
 
 } // namespace
@@ -493,8 +716,17 @@ void cholDrop(const double2 *G, int ldg, int m, double dropTol, double2 *R,
   cholDropKernel<<<1, 256, 0, s>>>(G, ldg, m, dropTol, R, T, keep);
 }
 
+// NCGM_HEIG_FP64=1 keeps the FP64 Jacobi for every size (comparisons)
+static bool heigFp64Only() {
+  static const bool v = [] {
+    const char *e = std::getenv("NCGM_HEIG_FP64");
+    return e && e[0] == '1';
+  }();
+  return v;
+}
+
 void heig(const double2 *A, int lda, int m, double2 *work, double2 *V,
-          double *w, int *perm, int *status, cudaStream_t s) {
+          double *w, int *perm, int *status, cudaStream_t s, bool fast) {
   // the round-robin tables hold up to 256 pairs (m <= 512)
   constexpr size_t kMaxDyn = 210 * 1024; // + 14 KB static <= 227 KB
   static const bool attr = [] {
@@ -503,6 +735,19 @@ void heig(const double2 *A, int lda, int m, double2 *work, double2 *V,
     return true;
   }();
   (void)attr;
+  if (fast && m <= kHeigDfMax && !heigFp64Only()) {
+    static const bool dfAttr = [] {
+      cudaFuncSetAttribute(heigDfKernel,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           2 * kHeigDfMax * kHeigDfMax * (int)sizeof(dfc));
+      return true;
+    }();
+    (void)dfAttr;
+    const int threads = m <= 32 ? 128 : (m <= 48 ? 256 : 512);
+    heigDfKernel<<<1, threads, 2 * (size_t)m * m * sizeof(dfc), s>>>(
+        A, lda, m, V, w, perm, status);
+    return;
+  }
   const size_t mat = (size_t)m * m * sizeof(double2);
   const int sm = 2 * mat <= kMaxDyn ? 2 : (mat <= kMaxDyn ? 1 : 0);
   const size_t smem = sm == 2 ? 2 * mat : (sm == 1 ? mat : 0);

@@ -43,7 +43,11 @@ void gemmVC(const double2 *V, size_t ldv, int m, const double2 *C, int ldc,
 void cholDrop(const double2 *G, int ldg, int m, double dropTol, double2 *R,
               double2 *T, int *keep, cudaStream_t s);
 // Hermitian eigensolver (lower triangle): w ascending, V eigenvectors (m x m).
+// fast: for m <= 80, double-float sweeps finished by FP64 sweeps (same
+// accuracy, a different rounding path, so degenerate eigenvectors may come
+// out rotated within their eigenspace); otherwise the FP64 Jacobi.
 void heig(const double2 *A, int lda, int m, double2 *work, double2 *V,
-          double *w, int *perm, int *status, cudaStream_t s);
+          double *w, int *perm, int *status, cudaStream_t s,
+          bool fast = false);
 
 } // namespace ncgm
