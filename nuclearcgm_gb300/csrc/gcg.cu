@@ -248,6 +248,7 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
   need += (size_t)mx * mx * sizeof(double2) * 8;  // small matrices
   need += maxChunks * (size_t)mx * mx * sizeof(double2);
   need += (size_t)nev * 128 * 5 * sizeof(double) + 64 * 1024;
+  need += ctx->ns * sizeof(float) + 256; // FP32 inverse Jacobi diagonal
   char *base = static_cast<char *>(ctx->buf(10, need + 64 * 4096));
   if (!base) return NCGM_ERR_NOMEM;
   float *tcPart = nullptr;
@@ -282,6 +283,7 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
          *pp2 = ar.take<double>((size_t)nev * 128 * 2);
   int *dLive = ar.take<int>(1), *dNdone = ar.take<int>(1);
   unsigned *dArrive = ar.take<unsigned>(2 * (size_t)nev);
+  float *dInv32 = ar.take<float>(ctx->ns);
   double2 *Gs = small, *Cw = small + 4 * (size_t)mx * mx,
           *Ev = small + 5 * (size_t)mx * mx, *Ap = small + 6 * (size_t)mx * mx;
 
@@ -294,6 +296,7 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
   NCGM_CUDA(cudaMemsetAsync(dLive, 0, sizeof(int), s));
   const double *dDiag = jacobiDiagonal(ctx, species, s);
   if (!dDiag) return NCGM_ERR_NOMEM;
+  if (fp32) inverseDiagonal32(dDiag, prm.shift, ctx->ns, dInv32, s);
 
   // X = X_init.leftCols(nev), orthonormalised (solver.cpp:669,677)
   NCGM_CUDA(cudaMemcpyAsync(V, Xinit, N * (size_t)nev * sizeof(double2),
@@ -478,6 +481,7 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
         pl.onlyCorrection = true;
         pl.lamShift = dLs;
         pl.coef = dDiag;
+        pl.invd = dInv32;
         pl.arrive = dArrive;
         pl.shift = shift;
         pl.tol = prm.cg_tol;

@@ -9,6 +9,8 @@
 // Vectors are FP64 (plain form) or FP32 (mixed form, dots in FP64).
 #include "k_pcg.cuh"
 
+#include <type_traits>
+
 #include <cfloat>
 #include <cstdlib>
 #include <vector>
@@ -285,13 +287,28 @@ __global__ void pcgDotKernel(const typename C2<T>::type *P,
   const int col = blockIdx.y;
   if (st[col].done) return;
   double re = 0, im = 0;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
-       i += (size_t)gridDim.x * blockDim.x) {
-    size_t o = (size_t)col * N + i;
-    auto p = P[o];
-    auto a = AP[o];
-    re += (double)p.x * a.x + (double)p.y * a.y;
-    im += (double)p.x * a.y - (double)p.y * a.x;
+  if (std::is_same<T, float>::value) {
+    // FP32 form: per-thread sums in FP32, block sums in FP64
+    float re32 = 0.f, im32 = 0.f;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+         i += (size_t)gridDim.x * blockDim.x) {
+      const size_t o = (size_t)col * N + i;
+      const auto p = P[o];
+      const auto a = AP[o];
+      re32 += (float)p.x * (float)a.x + (float)p.y * (float)a.y;
+      im32 += (float)p.x * (float)a.y - (float)p.y * (float)a.x;
+    }
+    re = re32;
+    im = im32;
+  } else {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+         i += (size_t)gridDim.x * blockDim.x) {
+      size_t o = (size_t)col * N + i;
+      auto p = P[o];
+      auto a = AP[o];
+      re += (double)p.x * a.x + (double)p.y * a.y;
+      im += (double)p.x * a.y - (double)p.y * a.x;
+    }
   }
   double s0 = blockSum(re, sh), s1 = blockSum(im, sh);
   double *pp = partials + (size_t)col * nblk * 3;
@@ -323,32 +340,62 @@ __global__ void pcgUpdateKernel(typename C2<T>::type *Wv,
                                 const typename C2<T>::type *P,
                                 const typename C2<T>::type *AP, size_t N,
                                 PcgCol *st, const double *diag, double shift,
-                                double *partials2, int nblk, unsigned *arrive,
-                                int *live, int *ndone) {
+                                const float *invd, double *partials2,
+                                int nblk, unsigned *arrive, int *live,
+                                int *ndone) {
   __shared__ double sh[kThreads];
   const int col = blockIdx.y;
   if (st[col].done) return;
   const double alr = st[col].alphaR, ali = st[col].alphaI;
   double rr = 0, rz = 0;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
-       i += (size_t)gridDim.x * blockDim.x) {
-    size_t o = (size_t)col * N + i;
-    auto p = P[o];
-    auto a = AP[o];
-    auto w = Wv[o];
-    auto r = R[o];
-    double px = p.x, py = p.y, ax = a.x, ay = a.y;
-    double wx = (double)w.x + (alr * px - ali * py);
-    double wy = (double)w.y + (alr * py + ali * px);
-    double rx = (double)r.x - (alr * ax - ali * ay);
-    double ry = (double)r.y - (alr * ay + ali * ax);
-    double m = invDiag(diag, i / 2, shift);
-    double zx = m * rx, zy = m * ry;
-    Wv[o] = {(T)wx, (T)wy};
-    R[o] = {(T)rx, (T)ry};
-    Z[o] = {(T)zx, (T)zy};
-    rr += rx * rx + ry * ry;
-    rz += rx * zx + ry * zy;
+  if (std::is_same<T, float>::value && invd) {
+    // FP32 form: the element arithmetic in FP32 (the vectors are FP32; the
+    // FP64 pipe of GB300 retires 2 FMAs per clock per SM), per-thread sums
+    // in FP32 over a handful of elements, block sums in FP64
+    const float fr = (float)alr, fi = (float)ali;
+    float rr32 = 0.f, rz32 = 0.f;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+         i += (size_t)gridDim.x * blockDim.x) {
+      const size_t o = (size_t)col * N + i;
+      const auto p = P[o];
+      const auto a = AP[o];
+      const auto w = Wv[o];
+      const auto r = R[o];
+      const float wx = (float)w.x + (fr * (float)p.x - fi * (float)p.y);
+      const float wy = (float)w.y + (fr * (float)p.y + fi * (float)p.x);
+      const float rx = (float)r.x - (fr * (float)a.x - fi * (float)a.y);
+      const float ry = (float)r.y - (fr * (float)a.y + fi * (float)a.x);
+      const float m = invd[i / 2];
+      const float zx = m * rx, zy = m * ry;
+      Wv[o] = {(T)wx, (T)wy};
+      R[o] = {(T)rx, (T)ry};
+      Z[o] = {(T)zx, (T)zy};
+      rr32 += rx * rx + ry * ry;
+      rz32 += rx * zx + ry * zy;
+    }
+    rr = rr32;
+    rz = rz32;
+  } else {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+         i += (size_t)gridDim.x * blockDim.x) {
+      size_t o = (size_t)col * N + i;
+      auto p = P[o];
+      auto a = AP[o];
+      auto w = Wv[o];
+      auto r = R[o];
+      double px = p.x, py = p.y, ax = a.x, ay = a.y;
+      double wx = (double)w.x + (alr * px - ali * py);
+      double wy = (double)w.y + (alr * py + ali * px);
+      double rx = (double)r.x - (alr * ax - ali * ay);
+      double ry = (double)r.y - (alr * ay + ali * ax);
+      double m = invDiag(diag, i / 2, shift);
+      double zx = m * rx, zy = m * ry;
+      Wv[o] = {(T)wx, (T)wy};
+      R[o] = {(T)rx, (T)ry};
+      Z[o] = {(T)zx, (T)zy};
+      rr += rx * rx + ry * ry;
+      rz += rx * zx + ry * zy;
+    }
   }
   double s0 = blockSum(rr, sh), s1 = blockSum(rz, sh);
   double *pp = partials2 + (size_t)col * nblk * 2;
@@ -384,12 +431,17 @@ __global__ void pcgPKernel(typename C2<T>::type *P,
   const int col = blockIdx.y;
   if (st[col].done) return;
   const double b = st[col].beta;
+  const float b32 = (float)b;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
        i += (size_t)gridDim.x * blockDim.x) {
     size_t o = (size_t)col * N + i;
     auto z = Z[o];
     auto p = P[o];
-    P[o] = {(T)((double)z.x + b * p.x), (T)((double)z.y + b * p.y)};
+    if (std::is_same<T, float>::value)
+      P[o] = {(T)((float)z.x + b32 * (float)p.x),
+              (T)((float)z.y + b32 * (float)p.y)};
+    else
+      P[o] = {(T)((double)z.x + b * p.x), (T)((double)z.y + b * p.y)};
   }
 }
 
@@ -429,6 +481,20 @@ ExitPoll *exitPoll() {
   for (auto &e : p->ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
   pool.push_back(p);
   return p;
+}
+
+namespace {
+__global__ void invDiag32Kernel(const double *c0, double shift, size_t ns,
+                                float *inv) {
+  const size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (p < ns) inv[p] = (float)invDiag(c0, p, shift);
+}
+} // namespace
+
+void inverseDiagonal32(const double *c0, double shift, size_t ns, float *inv,
+                       cudaStream_t s) {
+  invDiag32Kernel<<<(unsigned)((ns + 255) / 256), 256, 0, s>>>(c0, shift, ns,
+                                                               inv);
 }
 
 int pcgBlocks(size_t N) {
@@ -498,7 +564,8 @@ void pcgRun(const PcgPlan<T> &pl, cudaStream_t s) {
         reinterpret_cast<V *>(pl.W), reinterpret_cast<V *>(pl.R),
         reinterpret_cast<V *>(pl.Z), reinterpret_cast<const V *>(pl.P),
         reinterpret_cast<const V *>(pl.AP), pl.N, pl.st, pl.coef, pl.shift,
-        pl.partials2, nblk, pl.arrive + pl.ncols, pl.live, pl.ndone);
+        pl.invd, pl.partials2, nblk, pl.arrive + pl.ncols, pl.live,
+        pl.ndone);
     pcgPKernel<T><<<grid, kThreads, 0, s>>>(
         reinterpret_cast<V *>(pl.P), reinterpret_cast<const V *>(pl.Z), pl.N,
         pl.st);

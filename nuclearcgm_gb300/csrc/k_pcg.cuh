@@ -25,6 +25,9 @@ template <class T> struct PcgPlan {
   void *W = nullptr, *R = nullptr, *Z = nullptr, *P = nullptr, *AP = nullptr;
   const double *lamShift = nullptr; // lambda_k + shift per column (device)
   const double *coef = nullptr;     // Jacobi diagonal c0 per point (n^3)
+  // FP32 plans: 1 / (c0 + shift) per point in FP32 (n^3), for the step's
+  // preconditioner (null: FP64 division from coef)
+  const float *invd = nullptr;
   double shift = 0, tol = 0;
   int maxSteps = 0;
   PcgCol *st = nullptr;
@@ -56,6 +59,9 @@ int pcgBlocks(size_t N);
 // The Jacobi diagonal c0 = U + UC + 7.5 f / h^2 of a species' current
 // coefficient table, one double per lattice point, in a context buffer.
 double *jacobiDiagonal(ncgm_ctx *ctx, int species, cudaStream_t s);
+// inv[p] = 1 / (c0[p] + shift) in FP32 (1 where the sum is 0)
+void inverseDiagonal32(const double *c0, double shift, size_t ns, float *inv,
+                       cudaStream_t s);
 template <class T> void pcgRun(const PcgPlan<T> &plan, cudaStream_t s);
 
 } // namespace ncgm
