@@ -378,9 +378,9 @@ __global__ void heigKernel(const double2 *Ain, int lda, int m, double2 *Ag,
 // Li and Bailey's double-double algorithms, restated for float pairs). The
 // rotation parameters and the convergence test stay FP64. Accumulated
 // rounding over a few hundred rotations per element: ~1e-13 relative. The
-// double-float sweeps stop at an off-diagonal norm of 1e-12 relative; the
-// matrices are then converted in place to FP64 and the FP64 sweeps finish
-// (one or two sweeps from there, as Jacobi converges quadratically).
+// sweeps stop at an off-diagonal norm of 3e-13 relative (the FP64 Jacobi
+// stops at 1e-16); the matrices are then converted in place to FP64 for the
+// output, and only if that level was not reached do FP64 sweeps continue.
 struct dfl {
   float hi, lo;
 };
@@ -468,7 +468,7 @@ __global__ void heigDfKernel(const double2 *Ain, int lda, int m, double2 *Vg,
     fro = red[0];
     __syncthreads();
   }
-  int dfSweeps = 0;
+  int dfSweeps = 0, dfConverged = 0;
   for (int sweep = 0; sweep < 60; ++sweep) {
     double loc = 0;
     for (int e = tid; e < m * m; e += nt) {
@@ -483,7 +483,10 @@ __global__ void heigDfKernel(const double2 *Ain, int lda, int m, double2 *Vg,
     }
     const double off = red[0];
     __syncthreads();
-    if (off <= 1e-24 * fro || off == 0.0) break;
+    if (off <= 1e-25 * fro || off == 0.0) {
+      dfConverged = 1;
+      break;
+    }
     ++dfSweeps;
     for (int r = 0; r < mp - 1; ++r) {
       for (int k = tid; k < npairs; k += nt) {
@@ -564,7 +567,9 @@ __global__ void heigDfKernel(const double2 *Ain, int lda, int m, double2 *Vg,
   __shared__ double C64[kHeigDfMax / 2 + 1], S64[kHeigDfMax / 2 + 1];
   __shared__ double2 E64[kHeigDfMax / 2 + 1];
   const int converged =
-      jacobiSweeps64(A64, V64, m, fro, dfSweeps, P, Q, C64, S64, E64, red);
+      dfConverged ? 1
+                  : jacobiSweeps64(A64, V64, m, fro, dfSweeps, P, Q, C64, S64,
+                                   E64, red);
   jacobiFinish(A64, V64, m, converged, Vg, w, perm, status);
 }
 
@@ -633,21 +638,23 @@ __global__ void cholDropSmemKernel(const double2 *G, int ldg, int m,
   double2 *A = csm;          // m x m column-major; upper triangle -> R
   double2 *Ts = csm + m * m; // T
   __shared__ int kp[kCholSmemMax];
+  __shared__ double gd[kCholSmemMax]; // the Gram diagonal (drop floor)
   __shared__ double piv;
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int e = tid; e < m * m; e += nt) {
-    A[e] = G[(size_t)(e / m) * ldg + (e % m)];
+    const double2 g = G[(size_t)(e / m) * ldg + (e % m)];
+    A[e] = g;
     Ts[e] = make_double2(0, 0);
+    if (e / m == e % m) gd[e % m] = g.x;
   }
   __syncthreads();
   for (int j = 0; j < m; ++j) {
     if (tid == 0) {
       const double d = A[(size_t)j * m + j].x;
-      const double gjj = G[(size_t)j * ldg + j].x;
-      const double floor = fmax(dropTol, 64.0 * 2.220446049250313e-16 * gjj);
+      const double floor =
+          fmax(dropTol, 64.0 * 2.220446049250313e-16 * gd[j]);
       const int k = (d > floor) ? 1 : 0;
       kp[j] = k;
-      keep[j] = k;
       piv = k ? d : 0.0;
     }
     __syncthreads();
@@ -697,6 +704,7 @@ __global__ void cholDropSmemKernel(const double2 *G, int ldg, int m,
     R[e] = row <= col ? A[e] : make_double2(0, 0);
     T[e] = Ts[e];
   }
+  for (int j = tid; j < m; j += nt) keep[j] = kp[j];
 }
 
 void cholDrop(const double2 *G, int ldg, int m, double dropTol, double2 *R,

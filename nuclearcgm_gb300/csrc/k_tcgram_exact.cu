@@ -382,20 +382,28 @@ __global__ void __launch_bounds__(kThr, 1)
                  : "memory");
 }
 
+// one warp per output element: lane l sums chunks l, l + 32, ...; the lane
+// sums are combined in a fixed shuffle order (deterministic)
 __global__ void exactGramReduce(const double *__restrict__ part, int chunks,
                                 int p, int q, double2 *__restrict__ C,
                                 int ldc) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (e >= p * q) return;
   const int i = e % p, j = e / p;
   const size_t W = 2 * (size_t)q, H = 2 * (size_t)p;
   double re = 0, im = 0;
-  for (int ch = 0; ch < chunks; ++ch) {
+  for (int ch = lane; ch < chunks; ch += 32) {
     const double *P = part + (size_t)ch * H * W;
     re += P[(size_t)(2 * i) * W + 2 * j] + P[(size_t)(2 * i + 1) * W + 2 * j + 1];
     im += P[(size_t)(2 * i) * W + 2 * j + 1] - P[(size_t)(2 * i + 1) * W + 2 * j];
   }
-  C[(size_t)j * ldc + i] = make_double2(re, im);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    re += __shfl_xor_sync(0xffffffffu, re, o);
+    im += __shfl_xor_sync(0xffffffffu, im, o);
+  }
+  if (lane == 0) C[(size_t)j * ldc + i] = make_double2(re, im);
 }
 
 // ---------------------------------------------------------------------------
@@ -702,8 +710,8 @@ void gramTCExact(const double2 *A, size_t lda, int p, const double2 *B,
   exactGramKernel<<<grid, kThr, kSmem, s>>>(A, lda, p, B, ldb, q, N, scA, eA,
                                             scB, eB, rows, part,
                                             exactGramErrWord());
-  exactGramReduce<<<(p * q + 127) / 128, 128, 0, s>>>(part, chunks, p, q, C,
-                                                      ldc);
+  exactGramReduce<<<(unsigned)(((size_t)p * q * 32 + 255) / 256), 256, 0, s>>>(
+      part, chunks, p, q, C, ldc);
 }
 
 // scratch of gemmVCExact in bytes: A column scales / exponents (2m), B
