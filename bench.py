@@ -165,6 +165,8 @@ def _hf_wall_ca40():
              ("mixed_tc_gpu", abi.FP32_TC, abi.PRECOND_JACOBI)]
     if lp is not None:
         forms.append(("learned_mixed_gpu", abi.FP32, abi.PRECOND_LEARNED))
+        forms.append(("learned_mixed_tc_gpu", abi.FP32_TC,
+                      abi.PRECOND_LEARNED))
     for name, prec, pc in forms:
         cfg = config.from_input(CA40_HF, precision=prec)
         cfg.hf_gcg.precond = pc
@@ -199,6 +201,8 @@ def _hf_wall(with_cpu):
              ("mixed_tc_gpu", abi.FP32_TC, abi.PRECOND_JACOBI)]
     if lp is not None:
         forms.append(("learned_mixed_gpu", abi.FP32, abi.PRECOND_LEARNED))
+        forms.append(("learned_mixed_tc_gpu", abi.FP32_TC,
+                      abi.PRECOND_LEARNED))
     out = {"workload": "16O HF ground state, SLy4, 30^3 lattice, box 18 fm, "
                        "|dE| < 1 keV", "unit": "s"}
     for name, prec, pc in forms:
