@@ -317,16 +317,31 @@ __global__ void pcgDotKernel(const typename C2<T>::type *P,
     pp[nblk + blockIdx.x] = s1;
   }
   // the last block sums the partials in block order: alpha = absNew / p^H Ap
-  if (lastArrival(&arrive[col], nblk) && threadIdx.x == 0) {
+  // the last block sums the partials. FP32 plans: with all its threads (one
+  // L2 round trip, then a fixed-order tree; a serial sum was a chain of
+  // ~nblk L2 latencies per PCG step). FP64 plans keep the serial block order,
+  // the rounding path the FP64 parity tests were validated on.
+  if (lastArrival(&arrive[col], nblk)) {
     double r = 0, m = 0;
-    for (int b = 0; b < nblk; ++b) {
-      r += ((volatile double *)pp)[b];
-      m += ((volatile double *)pp)[nblk + b];
+    if (std::is_same<T, float>::value) {
+      for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
+        r += __ldcg(pp + b);
+        m += __ldcg(pp + nblk + b);
+      }
+      r = blockSum(r, sh);
+      m = blockSum(m, sh);
+    } else if (threadIdx.x == 0) {
+      for (int b = 0; b < nblk; ++b) {
+        r += ((volatile double *)pp)[b];
+        m += ((volatile double *)pp)[nblk + b];
+      }
     }
-    const double den = r * r + m * m;
-    const double a = st[col].absNew;
-    st[col].alphaR = a * r / den;
-    st[col].alphaI = -a * m / den;
+    if (threadIdx.x == 0) {
+      const double den = r * r + m * m;
+      const double a = st[col].absNew;
+      st[col].alphaR = a * r / den;
+      st[col].alphaI = -a * m / den;
+    }
   }
 }
 
@@ -403,12 +418,22 @@ __global__ void pcgUpdateKernel(typename C2<T>::type *Wv,
     pp[blockIdx.x] = s0;
     pp[nblk + blockIdx.x] = s1;
   }
-  if (lastArrival(&arrive[col], nblk) && threadIdx.x == 0) {
+  if (lastArrival(&arrive[col], nblk)) {
     double tr = 0, tz = 0;
-    for (int b = 0; b < nblk; ++b) {
-      tr += ((volatile double *)pp)[b];
-      tz += ((volatile double *)pp)[nblk + b];
+    if (std::is_same<T, float>::value) { // see pcgDotKernel
+      for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
+        tr += __ldcg(pp + b);
+        tz += __ldcg(pp + nblk + b);
+      }
+      tr = blockSum(tr, sh);
+      tz = blockSum(tz, sh);
+    } else if (threadIdx.x == 0) {
+      for (int b = 0; b < nblk; ++b) {
+        tr += ((volatile double *)pp)[b];
+        tz += ((volatile double *)pp)[nblk + b];
+      }
     }
+    if (threadIdx.x != 0) return;
     PcgCol c = st[col];
     if (tr < c.thr) {
       c.done = 1;
