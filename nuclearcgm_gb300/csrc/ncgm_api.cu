@@ -3,6 +3,8 @@
 // lets a C++ exception cross the boundary.
 #include "ncgm_internal.cuh"
 
+#include <algorithm>
+
 #include <cstring>
 #include <exception>
 #include <string>
@@ -139,6 +141,9 @@ int ncgm_destroy(ncgm_ctx *ctx) {
   }
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  for (auto e : ctx->xev) cudaEventDestroy(e);
+  if (ctx->xin) cudaStreamDestroy(ctx->xin);
+  if (ctx->xout) cudaStreamDestroy(ctx->xout);
   if (ctx->ownStream) ctx->stream = ctx->ownStream;
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -213,6 +218,66 @@ int ncgm_apply_h(ncgm_ctx *ctx, int species, const double *X, double *Y,
   }
   const size_t cnt = ctx->N * (size_t)ncols; // complex entries
   const bool dX = isDevicePtr(X), dY = isDevicePtr(Y);
+  // Host in and out with several columns: a three-stage pipeline over
+  // column chunks of ~16 MB (copy in on one stream, convert and apply on the
+  // context stream, copy out on a third), so the host<->device copies of
+  // consecutive chunks overlap each other and the compute. Every column is
+  // computed by the same kernels as in one launch (columns are independent),
+  // so the results are identical.
+  const int chunkCols = std::max<int>(
+      1, (int)std::min<size_t>(ncols, (size_t)(16u << 20) /
+                                          (ctx->N * sizeof(double2))));
+  if (!dX && !dY && ncols > chunkCols) {
+    const int nch = (ncols + chunkCols - 1) / chunkCols;
+    if (!ctx->xin)
+      NCGM_CUDA(cudaStreamCreateWithFlags(&ctx->xin, cudaStreamNonBlocking));
+    if (!ctx->xout)
+      NCGM_CUDA(cudaStreamCreateWithFlags(&ctx->xout, cudaStreamNonBlocking));
+    while ((int)ctx->xev.size() < 2 * nch + 1) {
+      cudaEvent_t e;
+      NCGM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      ctx->xev.push_back(e);
+    }
+    auto *Xs = static_cast<double2 *>(ctx->buf(3, cnt * sizeof(double2)));
+    auto *Ys = static_cast<double2 *>(ctx->buf(4, cnt * sizeof(double2)));
+    float2 *x32 = nullptr, *y32 = nullptr;
+    if (precision == NCGM_FP32) {
+      x32 = static_cast<float2 *>(ctx->buf(5, cnt * sizeof(float2)));
+      y32 = static_cast<float2 *>(ctx->buf(6, cnt * sizeof(float2)));
+    }
+    if (!Xs || !Ys || (precision == NCGM_FP32 && (!x32 || !y32)))
+      return NCGM_ERR_NOMEM;
+    // the copy streams start after earlier work on the context stream
+    NCGM_CUDA(cudaEventRecord(ctx->xev[0], ctx->stream));
+    NCGM_CUDA(cudaStreamWaitEvent(ctx->xin, ctx->xev[0], 0));
+    NCGM_CUDA(cudaStreamWaitEvent(ctx->xout, ctx->xev[0], 0));
+    const double2 *Xh = reinterpret_cast<const double2 *>(X);
+    double2 *Yh = reinterpret_cast<double2 *>(Y);
+    for (int c = 0; c < nch; ++c) {
+      const int c0 = c * chunkCols, cc = std::min(chunkCols, ncols - c0);
+      const size_t off = (size_t)c0 * ctx->N, len = (size_t)cc * ctx->N;
+      cudaEvent_t in = ctx->xev[1 + 2 * c], done = ctx->xev[2 + 2 * c];
+      NCGM_CUDA(cudaMemcpyAsync(Xs + off, Xh + off, len * sizeof(double2),
+                                cudaMemcpyHostToDevice, ctx->xin));
+      NCGM_CUDA(cudaEventRecord(in, ctx->xin));
+      NCGM_CUDA(cudaStreamWaitEvent(ctx->stream, in, 0));
+      if (precision == NCGM_FP64) {
+        applyH64(ctx, species, Xs + off, Ys + off, cc, 0.0, ctx->stream);
+      } else {
+        convert64to32(Xs + off, x32 + off, len, ctx->stream);
+        applyH32(ctx, species, x32 + off, y32 + off, cc, 0.f, ctx->stream);
+        convert32to64(y32 + off, Ys + off, len, ctx->stream);
+      }
+      NCGM_CUDA(cudaGetLastError());
+      NCGM_CUDA(cudaEventRecord(done, ctx->stream));
+      NCGM_CUDA(cudaStreamWaitEvent(ctx->xout, done, 0));
+      NCGM_CUDA(cudaMemcpyAsync(Yh + off, Ys + off, len * sizeof(double2),
+                                cudaMemcpyDeviceToHost, ctx->xout));
+    }
+    NCGM_CUDA(cudaStreamSynchronize(ctx->xout));
+    NCGM_CUDA(cudaStreamSynchronize(ctx->stream));
+    return NCGM_OK;
+  }
   const double2 *Xd = reinterpret_cast<const double2 *>(X);
   double2 *Yd = reinterpret_cast<double2 *>(Y);
   if (!dX) {

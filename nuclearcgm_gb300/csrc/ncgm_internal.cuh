@@ -66,6 +66,10 @@ struct ncgm_ctx {
   void *buf(int slot, size_t bytes);
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   ncgm_lp *lp = nullptr; // learned preconditioner (not owned)
+  // host-buffer applies: copy-in / copy-out streams and their events,
+  // created on first use
+  cudaStream_t xin = nullptr, xout = nullptr;
+  std::vector<cudaEvent_t> xev;
 };
 
 namespace ncgm {

@@ -121,3 +121,30 @@ def test_full_size_linearity_and_fp32_error():
     Y64 = H.apply(X)
     Y32 = H.apply(X, abi.FP32)
     assert np.abs(Y32 - Y64).max() <= FP32_TOL * np.abs(Y64).max()
+
+
+@pytest.mark.parametrize("precision", [abi.FP64, abi.FP32])
+def test_host_pipeline_matches_device_apply(precision):
+    """Host buffers with more columns than one ~16 MB chunk (40^3: 8 columns
+    per chunk) take the chunked copy-in / apply / copy-out pipeline; every
+    column must equal the single device-side apply bit for bit (20 columns:
+    chunks of 8, 8 and 4)."""
+    torch = pytest.importorskip("torch")
+    a, f, gradf, U, W = workloads.fields(40, 0.5)
+    ctx = ng.Context(ng.Grid(40, a), 20)
+    H = ng.Hamiltonian(ctx, abi.NEUTRON).set_fields(f, gradf.T, U, W.T)
+    X = workloads.orthonormal_block(2 * 40 ** 3, 20, seed=4)
+    Yh = H.apply(X, precision)
+    if precision == abi.FP64:
+        Xd = torch.from_numpy(np.ascontiguousarray(X.T)).cuda()
+        Yd = H.apply(Xd).cpu().numpy().T
+    else:
+        Xd = torch.from_numpy(np.ascontiguousarray(X.T)).to(torch.complex64).cuda()
+        Yd = torch.empty_like(Xd)
+        ng._check(ng.load().ncgm_apply_h_device(ctx.h, abi.NEUTRON, Xd.data_ptr(),
+                                                Yd.data_ptr(), 20, abi.FP32,
+                                                0.0))
+        torch.cuda.synchronize()
+        Yd = Yd.cpu().numpy().T.astype(np.complex128)
+    assert np.array_equal(Yh, Yd)
+    ctx.close()
