@@ -284,6 +284,18 @@ int ncgm_gram(ncgm_ctx *ctx, const double *A, int p, const double *B, int q,
 int ncgm_vc(ncgm_ctx *ctx, const double *V, int m, const double *C, int k,
             double *Y, int precision);
 
+/* Eigenpairs of a Hermitian m x m matrix A (column-major complex<double>,
+ * lower triangle read; m <= 1024): w ascending, V the eigenvectors in the
+ * same order. This is the projected eigenproblem of the GCG's Rayleigh-Ritz
+ * step (the reference's SelfAdjointEigenSolver on the lower triangle,
+ * src/solver/solver.cpp:766-777) and of the HFB step. m <= 80: one-CTA
+ * Jacobi in shared memory (NCGM_FP64: FP64 rotations; NCGM_FP32 and
+ * NCGM_FP32_TC: double-float rotations); m > 80: Householder
+ * tridiagonalisation, bisection and inverse iteration over the whole GPU.
+ * Host or device pointers. */
+int ncgm_heig(ncgm_ctx *ctx, const double *A, int m, double *w, double *V,
+              int precision);
+
 /* Batch of independent HF runs on one GPU (the reference runs the points of
  * a deformation curve one after another, src/main.cpp:176-185 with
  * Utilities::curve, src/util/utilities.cpp:71-73). Every configuration runs

@@ -109,6 +109,7 @@ SIGNATURES = {
     "ncgm_hf_run_batch": ([_vp, _i, _i, _vp, _vp, _vp, _vp], _i),
     "ncgm_gram": ([_vp, _vp, _i, _vp, _i, _vp, _i], _i),
     "ncgm_vc": ([_vp, _vp, _i, _vp, _i, _vp, _i], _i),
+    "ncgm_heig": ([_vp, _vp, _i, _vp, _vp, _i], _i),
     "ncgm_lp_num_params": ([], _i),
     "ncgm_lp_create": ([C.POINTER(_vp), C.c_ulonglong], _i),
     "ncgm_lp_destroy": ([_vp], _i),

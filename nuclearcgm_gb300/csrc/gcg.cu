@@ -827,3 +827,36 @@ extern "C" int ncgm_vc(ncgm_ctx *ctx, const double *V, int m, const double *C,
   }
   return NCGM_OK;
 }
+
+extern "C" int ncgm_heig(ncgm_ctx *ctx, const double *A, int m, double *w,
+                         double *V, int precision) {
+  if (!ctx || !A || !w || !V || m < 1 || m > 1024 ||
+      (precision != NCGM_FP64 && precision != NCGM_FP32 &&
+       precision != NCGM_FP32_TC)) {
+    setError("ncgm_heig: bad argument");
+    return NCGM_ERR_ARG;
+  }
+  using namespace ncgm;
+  cudaStream_t s = ctx->stream;
+  const size_t mm = (size_t)m * m;
+  char *base = static_cast<char *>(ctx->buf(
+      30, 3 * mm * sizeof(double2) + m * (sizeof(double) + sizeof(int)) + 1024));
+  if (!base) return NCGM_ERR_NOMEM;
+  double2 *dA = reinterpret_cast<double2 *>(base);
+  double2 *work = dA + mm, *dV = work + mm;
+  double *dw = reinterpret_cast<double *>(dV + mm);
+  int *perm = reinterpret_cast<int *>(dw + m), *st = perm + m;
+  NCGM_CUDA(cudaMemcpyAsync(dA, A, mm * sizeof(double2), cudaMemcpyDefault, s));
+  heig(dA, m, m, work, dV, dw, perm, st, s, precision != NCGM_FP64);
+  int hs = 0;
+  NCGM_CUDA(cudaMemcpyAsync(w, dw, m * sizeof(double), cudaMemcpyDefault, s));
+  NCGM_CUDA(cudaMemcpyAsync(V, dV, mm * sizeof(double2), cudaMemcpyDefault, s));
+  NCGM_CUDA(cudaMemcpyAsync(&hs, st, sizeof(int), cudaMemcpyDeviceToHost, s));
+  NCGM_CUDA(cudaStreamSynchronize(s));
+  NCGM_CUDA(cudaGetLastError());
+  if (hs != 0) {
+    setError("ncgm_heig: eigensolver did not converge");
+    return NCGM_ERR_EIG;
+  }
+  return NCGM_OK;
+}

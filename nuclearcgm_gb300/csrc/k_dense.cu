@@ -724,7 +724,8 @@ void cholDrop(const double2 *G, int ldg, int m, double dropTol, double2 *R,
   cholDropKernel<<<1, 256, 0, s>>>(G, ldg, m, dropTol, R, T, keep);
 }
 
-// NCGM_HEIG_FP64=1 keeps the FP64 Jacobi for every size (comparisons)
+// NCGM_HEIG_FP64=1 keeps the one-CTA FP64 Jacobi for every size
+// (comparisons)
 static bool heigFp64Only() {
   static const bool v = [] {
     const char *e = std::getenv("NCGM_HEIG_FP64");
@@ -755,6 +756,17 @@ void heig(const double2 *A, int lda, int m, double2 *work, double2 *V,
     heigDfKernel<<<1, threads, 2 * (size_t)m * m * sizeof(dfc), s>>>(
         A, lda, m, V, w, perm, status);
     return;
+  }
+  if (m > kHeigDfMax && !heigFp64Only()) {
+    // above the shared-memory tier: the multi-kernel solver over the whole
+    // GPU (stream-ordered scratch; concurrent contexts stay independent)
+    void *scr = nullptr;
+    if (cudaMallocAsync(&scr, heigLargeScratchBytes(m), s) == cudaSuccess) {
+      heigLarge(A, lda, m, V, w, perm, status, scr, s);
+      cudaFreeAsync(scr, s);
+      return;
+    }
+    cudaGetLastError();
   }
   const size_t mat = (size_t)m * m * sizeof(double2);
   const int sm = 2 * mat <= kMaxDyn ? 2 : (mat <= kMaxDyn ? 1 : 0);

@@ -42,6 +42,11 @@ void gemmVC(const double2 *V, size_t ldv, int m, const double2 *C, int ldc,
 // Cholesky of Gram G with MGS-equivalent drop; T = R^{-1}; keep flags.
 void cholDrop(const double2 *G, int ldg, int m, double dropTol, double2 *R,
               double2 *T, int *keep, cudaStream_t s);
+// Multi-kernel Hermitian eigensolver for m > 80 (k_heig_large.cu): Householder
+// tridiagonalisation, bisection, inverse iteration, back-transformation.
+void heigLarge(const double2 *A, int lda, int m, double2 *V, double *w,
+               int *perm, int *status, void *scratch, cudaStream_t s);
+size_t heigLargeScratchBytes(int m);
 // Hermitian eigensolver (lower triangle): w ascending, V eigenvectors (m x m).
 // fast: for m <= 80, double-float sweeps finished by FP64 sweeps (same
 // accuracy, a different rounding path, so degenerate eigenvectors may come
