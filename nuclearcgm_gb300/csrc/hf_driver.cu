@@ -468,7 +468,16 @@ int hfbSpecies(Run &R, Species &S, int target, HFBRes &out) {
     out = nullHFB(target, S.e);
     return NCGM_OK;
   }
+  // Fermi level: N(lambda) - target = 0 inside [lambda - 1.7, lambda + 1.7]
+  // to |N - target| < 1e-12, as the reference's bisection
+  // (iteration_data.cpp:605-850). The first trial is the previous lambda;
+  // once both signs are known the next trial is the Illinois regula falsi
+  // point (Dowell and Jarratt 1971) instead of the midpoint, so a converged
+  // HF run needs a few eigensolves per step instead of ~45.
   double bmin = lambda - 1.7, bmax = lambda + 1.7, cur = lambda;
+  double flo = 0, fhi = 0;
+  bool haveLo = false, haveHi = false;
+  int side = 0; // Illinois: which end was kept last
   const int m2 = 2 * nS;
   std::vector<double> U((size_t)nS * nS), V((size_t)nS * nS);
   std::vector<double2> H((size_t)m2 * m2);
@@ -498,9 +507,27 @@ int hfbSpecies(Run &R, Species &S, int target, HFBRes &out) {
     num += start;
     double diff = num - target;
     if (std::abs(diff) < 1e-12) break;
-    if (diff > 0) bmax = cur;
-    else bmin = cur;
-    cur = (bmax + bmin) / 2.0;
+    if (diff > 0) {
+      bmax = cur;
+      fhi = diff;
+      haveHi = true;
+      if (side == 1) flo *= 0.5;
+      side = 1;
+    } else {
+      bmin = cur;
+      flo = diff;
+      haveLo = true;
+      if (side == -1) fhi *= 0.5;
+      side = -1;
+    }
+    double next = (bmax + bmin) / 2.0;
+    if (haveLo && haveHi && fhi != flo) {
+      const double rf = bmin - flo * (bmax - bmin) / (fhi - flo);
+      if (rf > bmin && rf < bmax) next = rf;
+    }
+    if (next == cur || bmax - bmin <= 1e-15 * std::max(1.0, std::abs(cur)))
+      break;
+    cur = next;
   }
   lambda = cur;
   double pe = 0;
