@@ -181,6 +181,19 @@ struct Run {
   std::vector<Constraint> cons;
   double tPair = 0, tFields = 0, tPoisson = 0, tGcg = 0;
   std::vector<void *> allocs;
+  // tensor-core form: scratch of the exact-digit Gram / V C products of the
+  // driver's own overlaps and rotations (allocated on first use)
+  void *tcScr = nullptr;
+  bool tc() const { return cfg.hf_gcg.precision == NCGM_FP32_TC; }
+  void *tcScratch() {
+    if (!tcScr) {
+      int M = std::max(sp[0].orb, sp[1].orb);
+      size_t b = std::max(exactGramScratchDoubles(N, M, M) * sizeof(double),
+                          exactVCScratchBytes(M, M));
+      tcScr = alloc<char>(b + 1024);
+    }
+    return tcScr;
+  }
 
   template <class T> T *alloc(size_t count) {
     void *p = nullptr;
@@ -220,7 +233,11 @@ int hostGram(Run &R, const double2 *A, int p, const double2 *B, int q,
     }
     cap = need;
   }
-  gram(A, R.N, p, B, R.N, q, R.N, R.cplx, p, parts, maxChunks, R.s);
+  if (R.tc() && R.tcScratch())
+    gramTCExact(A, R.N, p, B, R.N, q, R.N, R.cplx, p,
+                static_cast<double *>(R.tcScratch()), R.s);
+  else
+    gram(A, R.N, p, B, R.N, q, R.N, R.cplx, p, parts, maxChunks, R.s);
   C.resize((size_t)p * q);
   cudaMemcpyAsync(C.data(), R.cplx, sizeof(double2) * p * q,
                   cudaMemcpyDeviceToHost, R.s);
@@ -566,7 +583,11 @@ int occupy(Run &R, Species &S, const std::vector<double2> &T) {
   const int M = S.orb;
   cudaMemcpyAsync(R.cplx, T.data(), sizeof(double2) * M * M,
                   cudaMemcpyHostToDevice, R.s);
-  gemmVC(S.X, R.N, M, R.cplx, M, M, S.Phi, R.N, R.N, 0.0, R.s);
+  if (R.tc() && R.tcScratch())
+    gemmVCExact(S.X, R.N, M, R.cplx, M, M, S.Phi, R.N, R.N, R.tcScratch(),
+                R.s);
+  else
+    gemmVC(S.X, R.N, M, R.cplx, M, M, S.Phi, R.N, R.N, 0.0, R.s);
   return NCGM_OK;
 }
 
@@ -887,7 +908,11 @@ int conjDir(Run &R, Species &S) {
                   cudaMemcpyHostToDevice, R.s);
   cudaMemcpyAsync(S.CD, S.Xn, sizeof(double2) * R.N * M,
                   cudaMemcpyDeviceToDevice, R.s);
-  gemmVC(S.X, R.N, M, R.cplx, M, M, S.CD, R.N, R.N, 1.0, R.s);
+  if (R.tc() && R.tcScratch())
+    gemmVCExact(S.X, R.N, M, R.cplx, M, M, S.CD, R.N, R.N, R.tcScratch(),
+                R.s, true);
+  else
+    gemmVC(S.X, R.N, M, R.cplx, M, M, S.CD, R.N, R.N, 1.0, R.s);
   normalizeEuclid(S.CD, R.N, R.N, M, R.small, R.s);
   S.cdCols = M;
   return sync(R);

@@ -707,8 +707,94 @@ __global__ void cholDropSmemKernel(const double2 *G, int ldg, int m,
   for (int j = tid; j < m; j += nt) keep[j] = kp[j];
 }
 
+// Large m (> 80): the same right-looking factorisation in global memory with
+// one launch pair per column (pivot and row scaling in one block, the rank-1
+// update of the trailing triangle over the whole GPU), then T = R^{-1} one
+// thread per column. G's diagonal (drop floor) and the pivots are kept in
+// T's first 2m entries until T is computed.
+__global__ void cholCopyKernel(const double2 *G, int ldg, int m, double2 *R,
+                               double2 *T) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m * m) return;
+  const int row = e % m, col = e / m;
+  const double2 g = G[(size_t)col * ldg + row];
+  R[e] = g;
+  if (row == col) T[row] = make_double2(g.x, 0.0);
+}
+__global__ void cholPivotKernel(double2 *R, int m, int j, double dropTol,
+                                double2 *T, int *keep) {
+  __shared__ double piv;
+  if (threadIdx.x == 0) {
+    const double d = R[(size_t)j * m + j].x;
+    const double floor =
+        fmax(dropTol, 64.0 * 2.220446049250313e-16 * T[j].x);
+    const int k = (d > floor) ? 1 : 0;
+    keep[j] = k;
+    piv = k ? d : 0.0;
+    T[m + j] = make_double2(piv, 0.0);
+  }
+  __syncthreads();
+  if (piv > 0.0) {
+    const double rjj = sqrt(piv);
+    for (int i = j + 1 + threadIdx.x; i < m; i += blockDim.x) {
+      const double2 a = R[(size_t)i * m + j];
+      R[(size_t)i * m + j] = make_double2(a.x / rjj, a.y / rjj);
+    }
+    if (threadIdx.x == 0) R[(size_t)j * m + j] = make_double2(rjj, 0.0);
+  } else {
+    for (int i = j + threadIdx.x; i < m; i += blockDim.x)
+      R[(size_t)i * m + j] = make_double2(0, 0);
+  }
+}
+__global__ void cholUpdateKernel(double2 *R, int m, int j, const double2 *T) {
+  if (T[m + j].x <= 0.0) return;
+  const int a = j + 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = j + 1 + blockIdx.y;
+  if (a >= m || a > b) return;
+  const double2 t = cconjmul(R[(size_t)a * m + j], R[(size_t)b * m + j]);
+  double2 &x = R[(size_t)b * m + a];
+  x.x -= t.x;
+  x.y -= t.y;
+}
+__global__ void cholFinishKernel(double2 *R, int m, double2 *T) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m * m) return;
+  if (e % m > e / m) R[e] = make_double2(0, 0); // lower triangle
+  T[e] = make_double2(0, 0);
+}
+__global__ void cholInvKernel(const double2 *R, int m, const int *keep,
+                              double2 *T) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m || !keep[c]) return;
+  for (int i = c; i >= 0; --i) {
+    if (!keep[i]) continue;
+    double2 sum = make_double2(i == c ? 1.0 : 0.0, 0.0);
+    for (int k = i + 1; k <= c; ++k) {
+      if (!keep[k]) continue;
+      const double2 t = cmul(R[(size_t)k * m + i], T[(size_t)c * m + k]);
+      sum.x -= t.x;
+      sum.y -= t.y;
+    }
+    const double rii = R[(size_t)i * m + i].x;
+    T[(size_t)c * m + i] = make_double2(sum.x / rii, sum.y / rii);
+  }
+}
+
 void cholDrop(const double2 *G, int ldg, int m, double dropTol, double2 *R,
               double2 *T, int *keep, cudaStream_t s) {
+  if (m > kCholSmemMax) {
+    const unsigned gm = (unsigned)(((size_t)m * m + 255) / 256);
+    cholCopyKernel<<<gm, 256, 0, s>>>(G, ldg, m, R, T);
+    for (int j = 0; j < m; ++j) {
+      cholPivotKernel<<<1, 128, 0, s>>>(R, m, j, dropTol, T, keep);
+      const int w = m - j - 1;
+      if (w > 0)
+        cholUpdateKernel<<<dim3((w + 127) / 128, w), 128, 0, s>>>(R, m, j, T);
+    }
+    cholFinishKernel<<<gm, 256, 0, s>>>(R, m, T);
+    cholInvKernel<<<(m + 63) / 64, 64, 0, s>>>(R, m, keep, T);
+    return;
+  }
   if (m <= kCholSmemMax) {
     static const bool attr = [] {
       cudaFuncSetAttribute(cholDropSmemKernel,

@@ -32,7 +32,7 @@ int *exactGramErrWord();
 // exactVCScratchBytes(m, k) bytes.
 void gemmVCExact(const double2 *V, size_t ldv, int m, const double2 *C,
                  int ldc, int k, double2 *Y, size_t ldy, size_t N,
-                 void *scratch, cudaStream_t s);
+                 void *scratch, cudaStream_t s, bool accum = false);
 size_t exactVCScratchBytes(int m, int k);
 // Y = V C + beta Y (V: N x m with m <= 1600, C: m x k; C is staged in
 // shared memory in blocks of columns).

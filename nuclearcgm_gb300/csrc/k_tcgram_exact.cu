@@ -476,7 +476,8 @@ __global__ void __launch_bounds__(kThr, 1)
                   const int *__restrict__ eA,
                   const unsigned char *__restrict__ dig,
                   const double *__restrict__ scB, int k, int nslab,
-                  double2 *__restrict__ Y, size_t ldy, size_t N, int *err) {
+                  double2 *__restrict__ Y, size_t ldy, size_t N, int accum,
+                  int *err) {
   extern __shared__ __align__(1024) unsigned char sm[];
   double *acc = reinterpret_cast<double *>(sm + 2 * kBuf);
   uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + 2 * kBuf + kAccBytes);
@@ -642,10 +643,16 @@ __global__ void __launch_bounds__(kThr, 1)
       const int row = e % kM, jc = e / kM;
       const size_t r = r0 + row;
       const int jr = nt * kN + 2 * jc;
-      if (r < N && jr < 2 * k)
-        Y[(size_t)(jr >> 1) * ldy + r] =
-            make_double2(acc[row * kAccLd + 2 * jc] * scB[jr],
-                         acc[row * kAccLd + 2 * jc + 1] * scB[jr + 1]);
+      if (r < N && jr < 2 * k) {
+        double2 v = make_double2(acc[row * kAccLd + 2 * jc] * scB[jr],
+                                 acc[row * kAccLd + 2 * jc + 1] * scB[jr + 1]);
+        double2 &y = Y[(size_t)(jr >> 1) * ldy + r];
+        if (accum) {
+          v.x += y.x;
+          v.y += y.y;
+        }
+        y = v;
+      }
     }
   } else if (tid == 0) {
     atomicExch(err, 1);
@@ -722,12 +729,14 @@ size_t exactVCScratchBytes(int m, int k) {
   return 256 + 16 * (size_t)(2 * m + 2 * k) + ntile * nslab * kDig * kBBytes;
 }
 
-// Y = V C (beta = 0) to ~1e-12 relative of the column maxima (see above)
+// Y = V C (accum: Y += V C) to ~1e-12 relative of the column maxima (see
+// above)
 void gemmVCExact(const double2 *V, size_t ldv, int m, const double2 *Cm,
                  int ldc, int k, double2 *Y, size_t ldy, size_t N,
-                 void *scratch, cudaStream_t s) {
+                 void *scratch, cudaStream_t s, bool accum) {
   if (k == 0 || N == 0) return;
   if (m == 0) {
+    if (accum) return;
     for (int j = 0; j < k; ++j)
       cudaMemsetAsync(Y + (size_t)j * ldy, 0, N * sizeof(double2), s);
     return;
@@ -754,7 +763,8 @@ void gemmVCExact(const double2 *V, size_t ldv, int m, const double2 *Cm,
       Cm, ldc, m, k, eA, eB, nslab, dig);
   dim3 grid((unsigned)((N + kM - 1) / kM), ntile);
   exactVCKernel<<<grid, kThr, kSmem, s>>>(V, ldv, m, eA, dig, scB, k, nslab, Y,
-                                          ldy, N, exactGramErrWord());
+                                          ldy, N, accum ? 1 : 0,
+                                          exactGramErrWord());
 }
 
 } // namespace ncgm

@@ -67,6 +67,61 @@ def test_one_gcg_step_fixed_pcg_length_matches_oracle(n, nev, pcols):
     assert st.basis_cols == info["basis_cols"]
 
 
+def test_wide_search_space_matches_oracle():
+    """nev = 32 with 32 conjugate directions: a 96-column search space, past
+    the shared-memory tier, so the multi-kernel Cholesky-with-drop and
+    eigensolver run (FP64 form). With 32 unconverged columns the 80-step PCG
+    amplifies rounding differences between the two machines to ~1e-8 of the
+    Ritz values (measured at nev = 32 without directions, where the
+    small-tier kernels run, too), hence the looser bounds of this case."""
+    precision = abi.FP64
+    n, nev, pcols = 10, 32, 32
+    ctx, H, R = _phys(n, 0.9)
+    N = 2 * n ** 3
+    X0 = random_block(N, nev, 1)
+    P = random_block(N, pcols, 2)
+    P /= np.linalg.norm(P, axis=0)
+    prm = abi.GcgParams(max_iter=1, tol=1e-6, cg_steps=80, cg_tol=0.0,
+                        shift=0.0, ordering=abi.ORDER_ASCENDING,
+                        precision=precision, precond=0)
+    Xg, lg, st = H.gcg(X0, nev, P, prm)
+    Xo, lo, info = R.gcg(X0, nev, P, 0.0, 1, 1e-6, 80, 0.0, 1)
+    print("wide search space: %d columns, max |dlambda| %.2e MeV, projector "
+          "gap %.2e" % (st.basis_cols, np.abs(lg - lo).max(),
+                        _projector_gap(Xg, Xo)))
+    assert st.basis_cols > 80
+    assert np.allclose(lg, lo, rtol=1e-7)
+    assert _projector_gap(Xg, Xo) < 1e-4
+
+
+def test_wide_search_space_tensor_core_step_is_consistent():
+    """The tensor-core form on the same 96-column search space. From a random
+    block its single step follows another PCG trajectory than FP64 (FP32
+    corrections of an indefinite shifted system; both are upper bounds of the
+    true levels), so the check is self-consistency: the returned block is
+    orthonormal and each Ritz value equals the Rayleigh quotient of its vector
+    under the oracle's CSR Hamiltonian. The Hamiltonian is made Hermitian
+    (constant f, no spin-orbit field) so that the Rayleigh quotient is the
+    quantity the lower-triangle Rayleigh-Ritz step returns."""
+    n, nev, pcols = 10, 32, 32
+    ctx, H, R = _hams(n, 0.5 * (n - 1) * 0.9, 77, so=False, const_f=True)
+    N = 2 * n ** 3
+    X0 = random_block(N, nev, 1)
+    P = random_block(N, pcols, 2)
+    P /= np.linalg.norm(P, axis=0)
+    prm = abi.GcgParams(max_iter=1, tol=1e-6, cg_steps=80, cg_tol=0.0,
+                        shift=0.0, ordering=abi.ORDER_ASCENDING,
+                        precision=abi.FP32_TC, precond=0)
+    Xg, lg, st = H.gcg(X0, nev, P, prm)
+    assert st.basis_cols > 80
+    orth = np.abs(Xg.conj().T @ Xg - np.eye(nev)).max()
+    rq = np.real(np.einsum("ij,ij->j", Xg.conj(), R.apply(Xg)))
+    print("tensor-core wide step: orthonormality %.1e, max |RQ - lambda| "
+          "%.1e MeV" % (orth, np.abs(rq - lg).max()))
+    assert orth < 1e-10
+    assert np.abs(rq - lg).max() < 1e-6 * np.abs(lg).max()
+
+
 @pytest.mark.parametrize("n,nev,pcols", [(10, 8, 0), (12, 6, 6), (9, 5, 3)])
 def test_one_hf_gcg_step_matches_oracle(n, nev, pcols):
     """One outer iteration with the HF parameters (1, 1e-6, 80, 1e-5): the
