@@ -19,8 +19,10 @@
 #include <thread>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
+#include <string>
 #include <tuple>
 #include <vector>
 
@@ -161,6 +163,11 @@ struct Species {
 
 struct Run {
   ncgm_ctx *ctx = nullptr;
+  // proton context: its own stream and workspace, so that the two species'
+  // eigenproblems of an HF iteration run on two host threads at once
+  // (null when the species run one after the other on ctx)
+  ncgm_ctx *ctxP = nullptr;
+  cudaEvent_t evFields = nullptr, evProtons = nullptr;
   ncgm_hf_config cfg;
   int n = 0;
   size_t ns = 0, N = 0;
@@ -203,7 +210,11 @@ struct Run {
     return static_cast<T *>(p);
   }
   ~Run() {
+    if (ctxP) cudaStreamSynchronize(ctxP->stream);
     for (void *p : allocs) cudaFree(p);
+    if (evFields) cudaEventDestroy(evFields);
+    if (evProtons) cudaEventDestroy(evProtons);
+    if (ctxP) ncgm_destroy(ctxP);
     if (ctx) ncgm_destroy(ctx);
   }
 };
@@ -987,6 +998,22 @@ int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
     return NCGM_ERR_ARG;
   }
   R.ctx->lp = cfg.lp;
+  // Both species need their own eigenproblem when the Coulomb field or N != Z
+  // makes them differ. Each HF iteration then solves them concurrently, on
+  // two contexts and host threads; NCGM_HF_SERIAL=1 solves them one after
+  // the other on one context. Either way each species runs the same kernels
+  // on the same inputs, so the results are the same.
+  const bool twoSpecies = cfg.use_coulomb || N != Z;
+  {
+    const char *ser = std::getenv("NCGM_HF_SERIAL");
+    if (twoSpecies && !(ser && ser[0] == '1')) {
+      NCGM_TRY(ncgm_create(&R.ctxP, R.n, R.a, 4 * mx + 8, 0));
+      R.ctxP->lp = cfg.lp;
+      NCGM_CUDA(cudaEventCreateWithFlags(&R.evFields, cudaEventDisableTiming));
+      NCGM_CUDA(
+          cudaEventCreateWithFlags(&R.evProtons, cudaEventDisableTiming));
+    }
+  }
   R.sp[0].orb = orbN;
   R.sp[1].orb = orbP;
   R.sp[0].par = cfg.pair_n;
@@ -1080,18 +1107,47 @@ int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
     NCGM_TRY(updateQuantities(R, it));
     NCGM_TRY(buildCoefficients(R.ctx, 0, R.f[0], R.gf[0], R.U[0],
                                cfg.spin_orbit ? R.W[0] : nullptr, nullptr));
-    NCGM_TRY(buildCoefficients(R.ctx, 1, R.f[1], R.gf[1], R.U[1],
+    // the proton context's stream waits for this iteration's fields and
+    // orbitals, which were made on the main stream
+    ncgm_ctx *const ctxP = R.ctxP ? R.ctxP : R.ctx;
+    if (R.ctxP) {
+      NCGM_CUDA(cudaEventRecord(R.evFields, R.s));
+      NCGM_CUDA(cudaStreamWaitEvent(R.ctxP->stream, R.evFields, 0));
+    }
+    NCGM_TRY(buildCoefficients(ctxP, 1, R.f[1], R.gf[1], R.U[1],
                                cfg.spin_orbit ? R.W[1] : nullptr,
                                cfg.use_coulomb ? R.UCoul : nullptr));
     t0 = now();
     std::vector<double> lamN(orbN), lamP(orbP);
     Species &Sn = R.sp[0], &Sp = R.sp[1];
-    NCGM_TRY(gcgRun(R.ctx, 0, Sn.X, orbN, Sn.cdCols ? Sn.CD : nullptr,
-                    Sn.cdCols, orbN, hp, Sn.Xn, lamN.data(), nullptr));
-    if (cfg.use_coulomb || N != Z) {
+    if (twoSpecies && R.ctxP) {
+      int stP = NCGM_OK;
+      std::string errP;
+      std::thread protons([&] {
+        cudaSetDevice(R.ctx->device);
+        stP = gcgRun(R.ctxP, 1, Sp.X, orbP, Sp.cdCols ? Sp.CD : nullptr,
+                     Sp.cdCols, orbP, hp, Sp.Xn, lamP.data(), nullptr);
+        if (stP != NCGM_OK) errP = ncgm_last_error();
+      });
+      const int stN =
+          gcgRun(R.ctx, 0, Sn.X, orbN, Sn.cdCols ? Sn.CD : nullptr,
+                 Sn.cdCols, orbN, hp, Sn.Xn, lamN.data(), nullptr);
+      protons.join();
+      if (stN != NCGM_OK) return stN;
+      if (stP != NCGM_OK) {
+        setError(errP);
+        return stP;
+      }
+      NCGM_CUDA(cudaEventRecord(R.evProtons, R.ctxP->stream));
+      NCGM_CUDA(cudaStreamWaitEvent(R.s, R.evProtons, 0));
+    } else if (twoSpecies) {
+      NCGM_TRY(gcgRun(R.ctx, 0, Sn.X, orbN, Sn.cdCols ? Sn.CD : nullptr,
+                      Sn.cdCols, orbN, hp, Sn.Xn, lamN.data(), nullptr));
       NCGM_TRY(gcgRun(R.ctx, 1, Sp.X, orbP, Sp.cdCols ? Sp.CD : nullptr,
                       Sp.cdCols, orbP, hp, Sp.Xn, lamP.data(), nullptr));
     } else {
+      NCGM_TRY(gcgRun(R.ctx, 0, Sn.X, orbN, Sn.cdCols ? Sn.CD : nullptr,
+                      Sn.cdCols, orbN, hp, Sn.Xn, lamN.data(), nullptr));
       cudaMemcpyAsync(Sp.Xn, Sn.Xn, sizeof(double2) * R.N * orbP,
                       cudaMemcpyDeviceToDevice, R.s);
       std::copy(lamN.begin(), lamN.begin() + orbP, lamP.begin());
@@ -1105,7 +1161,7 @@ int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
       NCGM_TRY(ncgm_lp_collect(cfg.lp, R.ctx, 0,
                                reinterpret_cast<const double *>(Sn.Xn), orbN,
                                lamN.data(), shN, 2000, 1e-10));
-      NCGM_TRY(ncgm_lp_collect(cfg.lp, R.ctx, 1,
+      NCGM_TRY(ncgm_lp_collect(cfg.lp, ctxP, 1,
                                reinterpret_cast<const double *>(Sp.Xn), orbP,
                                lamP.data(), shP, 2000, 1e-10));
     }

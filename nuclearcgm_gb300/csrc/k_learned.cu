@@ -510,6 +510,10 @@ struct ncgm_lp {
   int *dIdx = nullptr;
   int idxCap = 0;
   std::mutex mu; // one user at a time (batched runs may share a network)
+  // recorded after each inference on the caller's stream: the next caller,
+  // possibly on another stream, waits for it before reusing the activations
+  cudaEvent_t done = nullptr;
+  bool doneRecorded = false;
 };
 
 namespace ncgm {
@@ -798,6 +802,7 @@ int lpInitialCorrection(ncgm_lp *lp, ncgm_ctx *ctx, int species,
   LpAct *a = actsFor(lp, n, B);
   float *scale = scratch(lp, (size_t)B);
   if (!a || !scale) return NCGM_ERR_NOMEM;
+  if (lp->doneRecorded) NCGM_CUDA(cudaStreamWaitEvent(s, lp->done, 0));
   residualRmsKernel<<<B, 256, 0, s>>>(X, AX, lam, N, ns, scale);
   packInputKernel<<<blocksFor((long long)B * ns), 256, 0, s>>>(
       X, AX, lam, scale, ctx->sp[species].coef64, ctx->h * ctx->h, shift, N,
@@ -807,6 +812,8 @@ int lpInitialCorrection(ncgm_lp *lp, ncgm_ctx *ctx, int species,
       a->y, scale, N, ns, ncols,
       reinterpret_cast<typename Cplx<T>::type *>(D0));
   NCGM_CUDA(cudaGetLastError());
+  NCGM_CUDA(cudaEventRecord(lp->done, s));
+  lp->doneRecorded = true;
   return NCGM_OK;
 }
 
@@ -874,6 +881,8 @@ int ncgm_lp_create(ncgm_lp **out, unsigned long long seed) {
   const bool ok = lp->w && lp->m && lp->v && lp->g && lp->dLoss &&
                   cudaMalloc(&q, lp->P * sizeof(__nv_bfloat16)) == cudaSuccess &&
                   cudaStreamCreateWithFlags(&lp->s, cudaStreamNonBlocking) ==
+                      cudaSuccess &&
+                  cudaEventCreateWithFlags(&lp->done, cudaEventDisableTiming) ==
                       cudaSuccess;
   lp->wq = static_cast<__nv_bfloat16 *>(q);
   if (!ok) {
@@ -920,6 +929,7 @@ int ncgm_lp_destroy(ncgm_lp *lp) {
   }
   for (auto &g : lp->groups) cudaFree(g.data);
   if (lp->s) cudaStreamDestroy(lp->s);
+  if (lp->done) cudaEventDestroy(lp->done);
   delete lp;
   return NCGM_OK;
 }

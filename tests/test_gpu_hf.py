@@ -202,3 +202,27 @@ def test_o16_hfb_fixed_point():
     assert abs(rg.lambda_n - ro.lambda_n) < 1e-4
     assert np.abs(og["spe_n"] - oo["spe_n"]).max() < 1e-4
     assert np.abs(og["rho_n"] - oo["rho_n"]).max() < 1e-6
+
+
+@pytest.mark.parametrize("precision", [abi.FP64, abi.FP32_TC])
+def test_concurrent_species_match_serial(precision, monkeypatch):
+    """With the Coulomb field on, the neutron and proton eigenproblems of an
+    HF iteration run concurrently on two contexts and host threads.
+    NCGM_HF_SERIAL=1 runs them one after the other on one context. Both run
+    the same kernels on the same inputs (the reductions use no floating-point
+    atomics), so the trajectories agree to the last bit."""
+    data = dict(O16, maxIterations=25)
+    cfg = config.from_input(data, precision=precision)
+    monkeypatch.delenv("NCGM_HF_SERIAL", raising=False)
+    r_c, o_c = ng.hf_run(cfg)
+    monkeypatch.setenv("NCGM_HF_SERIAL", "1")
+    r_s, o_s = ng.hf_run(cfg)
+    dE = np.abs(o_c["energies"] - o_s["energies"]).max()
+    drho = max(np.abs(o_c["rho_n"] - o_s["rho_n"]).max(),
+               np.abs(o_c["rho_p"] - o_s["rho_p"]).max())
+    print("concurrent vs serial: max dE %.3e MeV, max drho %.3e" % (dE, drho))
+    assert r_c.iterations == r_s.iterations
+    assert np.array_equal(o_c["energies"], o_s["energies"])
+    assert np.array_equal(o_c["spe_n"], o_s["spe_n"])
+    assert np.array_equal(o_c["spe_p"], o_s["spe_p"])
+    assert np.array_equal(o_c["rho_p"], o_s["rho_p"])
