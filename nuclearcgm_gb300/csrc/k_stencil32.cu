@@ -588,16 +588,17 @@ size_t kernelSmem(int kind, int n, int TY, int ring, int threads, int ppt,
 struct Shape {
   int TY, ring, ppt, ctasPerSM;
   int kind; // 0: stencilStream32, 1: stencilMarch32 (ppt unused),
-            // 2: stencilStage32 (ppt = rows per thread)
+            // 2: stencilStage32 (ppt = rows per thread),
+            // 3: stencilStage32 with the z-neighbours in registers
   int cpa;  // kind 0: coefficients prefetched with cp.async;
-            // kind 2: coefficient ring depth
-  int nc;   // kind 2: columns per X box
+            // kinds 2, 3: coefficient ring depth
+  int nc;   // kind 2: columns per X box (kind 3: 1)
 };
 
 bool validShape(int n, const Shape &s, int &threads) {
-  if (s.kind == 2)
+  if (s.kind == 2 || s.kind == 3)
     return validStage(n, s.TY, s.ring, s.cpa, s.ppt, s.nc, s.ctasPerSM,
-                      threads);
+                      s.kind == 3, threads);
   if (s.TY < 1 || s.TY > n || s.ring < 4 || (s.ring & (s.ring - 1)) ||
       s.ring > 64 || s.ctasPerSM < 1)
     return false;
@@ -627,9 +628,9 @@ bool launchStream(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
   const int n = ctx->n;
   int threads = 0;
   if (!validShape(n, sh, threads)) return false;
-  if (sh.kind == 2)
+  if (sh.kind == 2 || sh.kind == 3)
     return launchStage(ctx, species, X, Y, ncols, shift, st, sh.TY, sh.ring,
-                       sh.cpa, sh.ppt, sh.nc, sh.ctasPerSM);
+                       sh.cpa, sh.ppt, sh.nc, sh.ctasPerSM, sh.kind == 3);
   CUtensorMap map;
   bool flat = false;
   if (!tensorMapFor(X, n, ncols, sh.TY, flat, &map)) return false;
@@ -751,11 +752,13 @@ static Shape tune(ncgm_ctx *ctx, int species, int ncols) {
   for (int TY = 2; TY <= std::min(n, 40); TY += 2) srows.push_back(TY);
   for (int TY : srows)
     for (int yr : {1, 2, 4})
-      for (int nc : {1, 2})
-        for (int ring : {8, 16})
-          for (int cring : {2, 4, 8})
-            for (int cps : {1, 2})
+      for (int ring : {8, 16})
+        for (int cring : {2, 4, 8})
+          for (int cps : {1, 2}) {
+            for (int nc : {1, 2})
               trial(Shape{TY, ring, yr, cps, 2, cring, nc});
+            trial(Shape{TY, ring, yr, cps, 3, cring, 1});
+          }
   return best;
 }
 

@@ -16,6 +16,11 @@
 //    shared loads per point instead of 13.
 //  * One X box holds NC adjacent columns (spinors); both are computed with
 //    the same coefficient registers.
+//  * Launch kind 3 (ZQ) also keeps the z-neighbours of a thread's own points
+//    in registers (planes k-2, k-1, k+1), so a plane is read from shared
+//    memory only as the centre plane and once as plane k+2. Consumers then
+//    hold three planes of the ring instead of five: with a ring of 8 the
+//    producer runs five planes ahead instead of three.
 // Adjacent consumer threads take adjacent x, so the 16-byte shared loads of
 // a warp are contiguous runs (conflict-free).
 #include "ncgm_internal.cuh"
@@ -42,14 +47,15 @@ struct StageArgs {
 };
 
 // block-size limit per variant (register budget 102 at 640 threads, 128 at
-// 512: the multi-row and two-column forms hold larger register windows)
-constexpr int stageMaxThreads(int yr, int nc) {
-  return (yr >= 2 || nc == 2) ? 512 : 640;
+// 512, 168 at 384: the multi-row, two-column and z-queue forms hold larger
+// register windows)
+constexpr int stageMaxThreads(int yr, int nc, bool zq = false) {
+  return zq ? (yr >= 4 ? 384 : 512) : ((yr >= 2 || nc == 2) ? 512 : 640);
 }
 constexpr int kStageItems = 2; // items per consumer thread at most
 
-template <int YR, int NC, int WFIX>
-__global__ void __launch_bounds__(stageMaxThreads(YR, NC), 1)
+template <int YR, int NC, int WFIX, bool ZQ>
+__global__ void __launch_bounds__(stageMaxThreads(YR, NC, ZQ), 1)
     stencilStage32(const __grid_constant__ CUtensorMap xmap,
                    const __grid_constant__ CUtensorMap cmap, StageArgs A) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -173,11 +179,99 @@ __global__ void __launch_bounds__(stageMaxThreads(YR, NC), 1)
   }
 
   // ---- consumers: item it -> (x = it % n, rows rb .. rb + YR - 1) ----
-  // A thread owns items ct and ct + nct (launch shapes give at most two);
-  // their slot and table offsets are fixed for the whole kernel.
   const int ct = threadIdx.x - 64, nct = nCons * 32;
   const int nC = WFIX ? WFIX - 4 : n; // compile-time lattice size if known
   const int items = (TY / YR) * nC;
+  if constexpr (ZQ) {
+    // one item per thread; zm2/zm1/zp1 hold the own points of planes k-2,
+    // k-1 and k+1 while the thread marches in z through a run
+    static_assert(NC == 1, "the z-queue form takes one column per box");
+    const bool has = ct < items;
+    const int x = ct % nC, rb = (ct / nC) * YR;
+    const int wo = rb * W + x + 2, co = rb * nC + x;
+    float4 zm2[YR], zm1[YR], zp1[YR];
+    int waited = -1, c = 0;
+    const float shift = A.shift;
+    for (int r = 0; r < NR; ++r) {
+      const Run R = runs[r];
+      const int cg = R.cb / A.nbands, band = R.cb % A.nbands;
+      const int y0 = band * TY;
+      const int rowsValid = min(TY, n - y0);
+      float4 *Yb = A.Y + (size_t)cg * A.ns + (size_t)y0 * n;
+      for (int k = R.ka; k < R.kb; ++k) {
+        const int s0 = R.base + (k - R.ka);
+        bool ok = true;
+        while (waited < s0 + 4) {
+          const int s = waited + 1;
+          if (!mbarWaitBackoff(&full[s & rmask], (s >> rlog) & 1u, kLimit,
+                               kPollNs)) {
+            ok = false;
+            break;
+          }
+          waited = s;
+        }
+        if (ok && !mbarWaitBackoff(&cfull[c & cmask], (c >> clog) & 1u,
+                                   kLimit, kPollNs))
+          ok = false;
+        if (!ok || *(volatile int *)&failed) {
+          if (lane == 0) {
+            atomicExch(A.err, 1);
+            *(volatile int *)&failed = 1;
+          }
+          return;
+        }
+        const float4 *pc = xr + (size_t)((s0 + 2) & rmask) * slotElems;
+        const float4 *pp2 = xr + (size_t)((s0 + 4) & rmask) * slotElems;
+        const float4 *cs = cr + (size_t)(c & cmask) * cElems;
+        float4 *Yk = Yb + (size_t)k * nC * nC;
+        if (has) {
+          if (k == R.ka) {
+            const float4 *pm2 = xr + (size_t)(s0 & rmask) * slotElems;
+            const float4 *pm1 = xr + (size_t)((s0 + 1) & rmask) * slotElems;
+            const float4 *pp1 = xr + (size_t)((s0 + 3) & rmask) * slotElems;
+#pragma unroll
+            for (int t = 0; t < YR; ++t) {
+              const int l = wo + (t + 2) * W;
+              zm2[t] = pm2[l];
+              zm1[t] = pm1[l];
+              zp1[t] = pp1[l];
+            }
+          }
+          float4 win[YR + 4];
+#pragma unroll
+          for (int q = 0; q < YR + 4; ++q) win[q] = pc[wo + q * W];
+#pragma unroll
+          for (int t = 0; t < YR; ++t) {
+            const int ci = co + t * nC;
+            const float4 ca = cs[ci], cb = cs[cHalf + ci];
+            const int l = wo + (t + 2) * W;
+            const float4 zp2 = pp2[l];
+            const float4 o = pointH2(ca, cb, shift, win[t + 2], pc[l + 1],
+                                     pc[l - 1], pc[l + 2], pc[l - 2],
+                                     win[t + 3], win[t + 1], win[t + 4],
+                                     win[t], zp1[t], zm1[t], zp2, zm2[t]);
+            if (rb + t < rowsValid) Yk[ci] = o;
+            zm2[t] = zm1[t];
+            zm1[t] = win[t + 2];
+            zp1[t] = zp2;
+          }
+        }
+        // release: the centre plane; at the start of a run also the two
+        // planes below it, at the end also the two above
+        __syncwarp();
+        if (lane == 0) {
+          const int first = (k == R.ka) ? s0 : s0 + 2;
+          const int last = (k + 1 < R.kb) ? s0 + 2 : s0 + 4;
+          for (int s = first; s <= last; ++s) mbarArrive(&empty[s & rmask]);
+          mbarArrive(&cempty[c & cmask]);
+        }
+        ++c;
+      }
+    }
+    return;
+  }
+  // A thread owns items ct and ct + nct (launch shapes give at most two);
+  // their slot and table offsets are fixed for the whole kernel.
   int woff[kStageItems], coff[kStageItems], row0[kStageItems];
 #pragma unroll
   for (int m = 0; m < kStageItems; ++m) {
@@ -269,22 +363,27 @@ __global__ void __launch_bounds__(stageMaxThreads(YR, NC), 1)
 
 using StageKernel = void (*)(const CUtensorMap, const CUtensorMap, StageArgs);
 constexpr int kStageWidths[] = {0, 34, 36, 40, 44, 52};
-template <int YR, int NC> StageKernel pickStageW(int W) {
+template <int YR, int NC, bool ZQ> StageKernel pickStageW(int W) {
   switch (W) {
-  case 34: return stencilStage32<YR, NC, 34>;
-  case 36: return stencilStage32<YR, NC, 36>;
-  case 40: return stencilStage32<YR, NC, 40>;
-  case 44: return stencilStage32<YR, NC, 44>;
-  case 52: return stencilStage32<YR, NC, 52>;
-  default: return stencilStage32<YR, NC, 0>;
+  case 34: return stencilStage32<YR, NC, 34, ZQ>;
+  case 36: return stencilStage32<YR, NC, 36, ZQ>;
+  case 40: return stencilStage32<YR, NC, 40, ZQ>;
+  case 44: return stencilStage32<YR, NC, 44, ZQ>;
+  case 52: return stencilStage32<YR, NC, 52, ZQ>;
+  default: return stencilStage32<YR, NC, 0, ZQ>;
   }
 }
-StageKernel pickStage(int yr, int nc, int W) {
+StageKernel pickStage(int yr, int nc, int W, bool zq) {
+  if (zq) {
+    if (yr == 1) return pickStageW<1, 1, true>(W);
+    if (yr == 2) return pickStageW<2, 1, true>(W);
+    return pickStageW<4, 1, true>(W);
+  }
   if (nc == 2) // 4 rows x 2 columns does not fit the register budget
-    return yr == 1 ? pickStageW<1, 2>(W) : pickStageW<2, 2>(W);
-  if (yr == 1) return pickStageW<1, 1>(W);
-  if (yr == 2) return pickStageW<2, 1>(W);
-  return pickStageW<4, 1>(W);
+    return yr == 1 ? pickStageW<1, 2, false>(W) : pickStageW<2, 2, false>(W);
+  if (yr == 1) return pickStageW<1, 1, false>(W);
+  if (yr == 2) return pickStageW<2, 1, false>(W);
+  return pickStageW<4, 1, false>(W);
 }
 
 size_t stageSmem(int n, int TY, int ring, int cring, int nc) {
@@ -297,38 +396,43 @@ size_t stageSmem(int n, int TY, int ring, int cring, int nc) {
 } // namespace
 
 bool validStage(int n, int TY, int ring, int cring, int yr, int nc, int cps,
-                int &threads) {
+                bool zq, int &threads) {
   if (!(yr == 1 || yr == 2 || yr == 4) || !(nc == 1 || nc == 2)) return false;
   if (yr == 4 && nc == 2) return false;
+  if (zq && nc != 1) return false;
   if (TY < yr || TY > n || TY % yr || cps < 1) return false;
   if (ring < 8 || ring > 64 || (ring & (ring - 1))) return false;
   if (cring < 2 || cring > 16 || (cring & (cring - 1))) return false;
   if (TY + 4 > 256 || n + 4 > 256) return false;
   const int items = (TY / yr) * n;
-  const int maxWarps = (stageMaxThreads(yr, nc) - 64) / 32;
+  const int maxWarps = (stageMaxThreads(yr, nc, zq) - 64) / 32;
   threads = 64 + std::min((items + 31) / 32, maxWarps) * 32;
-  if (items > kStageItems * (threads - 64)) return false;
+  if (items > (zq ? 1 : kStageItems) * (threads - 64)) return false;
   return stageSmem(n, TY, ring, cring, nc) * cps <= 220 * 1024;
 }
 
 bool launchStage(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
                  int ncols, float shift, cudaStream_t st, int TY, int ring,
-                 int cring, int yr, int nc, int cps) {
+                 int cring, int yr, int nc, int cps, bool zq) {
   static const bool attr = [] {
     for (int w : kStageWidths)
-      for (int y : {1, 2, 4})
+      for (int y : {1, 2, 4}) {
         for (int c : {1, 2})
           if (!(y == 4 && c == 2))
-            cudaFuncSetAttribute(pickStage(y, c, w),
-                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               220 * 1024);
+            cudaFuncSetAttribute(pickStage(y, c, w, false),
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 220 * 1024);
+        cudaFuncSetAttribute(pickStage(y, 1, w, true),
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             220 * 1024);
+      }
     return true;
   }();
   (void)attr;
   const int n = ctx->n;
   if (nc > ncols) nc = 1; // a single column: no box wider than the block
   int threads = 0;
-  if (!validStage(n, TY, ring, cring, yr, nc, cps, threads)) return false;
+  if (!validStage(n, TY, ring, cring, yr, nc, cps, zq, threads)) return false;
   const float *cs = ctx->sp[species].coef32s;
   if (!cs) return false;
   CUtensorMap xmap, cmap;
@@ -355,7 +459,7 @@ bool launchStage(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
                             ((long long)(kMaxRuns - 2) * n);
   ctas = std::max(ctas, minCtas);
   ctas = std::min<long long>(ctas, A.total);
-  pickStage(yr, nc, n + 4)<<<(unsigned)ctas, threads,
+  pickStage(yr, nc, n + 4, zq)<<<(unsigned)ctas, threads,
                              stageSmem(n, TY, ring, cring, nc), st>>>(xmap,
                                                                       cmap, A);
   return true;

@@ -242,8 +242,8 @@ bool tensorMapX(const void *base, int n, int d4, int boxW, int boxRows,
 // staged-coefficient kernel (k_stencil_stage.cu): TY band rows, X ring and
 // coefficient ring depths, YR rows per thread, NC columns per box, CTAs/SM
 bool validStage(int n, int TY, int ring, int cring, int yr, int nc, int cps,
-                int &threads);
+                bool zq, int &threads);
 bool launchStage(ncgm_ctx *ctx, int species, const float2 *X, float2 *Y,
                  int ncols, float shift, cudaStream_t st, int TY, int ring,
-                 int cring, int yr, int nc, int cps);
+                 int cring, int yr, int nc, int cps, bool zq);
 } // namespace ncgm

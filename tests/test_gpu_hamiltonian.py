@@ -45,11 +45,14 @@ def test_fp32_plane_kernel_error_bound(n):
 # fixed stencil shapes (rows, ring, ppt, CTAs/SM, kind, cpa, nc), bypassing
 # the autotuner: kind 0 = plane-streaming kernel (cpa: coefficient
 # prefetch), kind 1 = z-marching kernel, kind 2 = staged-coefficient kernel
-# (ppt: rows per thread, cpa: coefficient ring depth, nc: columns per box)
+# (ppt: rows per thread, cpa: coefficient ring depth, nc: columns per box),
+# kind 3 = kind 2 with the z-neighbours in registers
 SHAPES = ["3,8,1,1,0", "5,16,4,2,0", "10,8,2,1,0,1", "5,16,4,2,0,1",
           "2,4,1,1,1", "8,8,1,2,1", "12,8,1,1,1", "6,4,1,4,1",
           "12,8,2,1,2,2,1", "10,8,1,1,2,4,2", "8,8,4,1,2,2,1",
-          "6,8,2,1,2,4,2", "4,8,4,2,2,2,1", "2,8,1,1,2,2,2"]
+          "6,8,2,1,2,4,2", "4,8,4,2,2,2,1", "2,8,1,1,2,2,2",
+          "12,8,2,1,3,2,1", "8,8,2,2,3,2,1", "8,16,4,1,3,4,1",
+          "6,8,1,2,3,8,1", "2,8,1,1,3,2,1"]
 
 
 @pytest.mark.parametrize("shape", SHAPES)
