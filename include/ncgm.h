@@ -168,6 +168,18 @@ int ncgm_gcg(ncgm_ctx *ctx, int species, const double *X_init, int xcols,
 int ncgm_densities(ncgm_ctx *ctx, const double *Phi, int ncols, double *rho,
                    double *tau, double *J9, double *divJ);
 
+/* The output step's Lagrange-mesh densities of the same columns: tau and
+ * J_{mu nu} with the Lagrange-mesh first derivative (Operators::gradLagrange)
+ * and, when rho and lap are both given, the Lagrange-mesh Laplacian of rho.
+ * Replaces Wavefunction::kineticDensityLagrange / soDensityLagrange
+ * (src/util/wavefunction.cpp:334-414) and Operators::lapLagrangeNoSpin
+ * (src/operators/differential_operators.cpp:196-235), the parts of
+ * IterationData::recomputeLagrange (src/util/iteration_data.cpp:346-382)
+ * that enter the recomputed energy. */
+int ncgm_lagrange_densities(ncgm_ctx *ctx, const double *Phi, int ncols,
+                            const double *rho, double *tau, double *J9,
+                            double *lap);
+
 /* Coulomb direct potential of a proton density by the Poisson equation with
  * the multipole boundary halo, and UC = direct + Slater exchange. U_guess may
  * be NULL (cold start). Replaces Wavefunction::coulombFieldPoisson and
@@ -254,6 +266,10 @@ typedef struct ncgm_hf_result {
   double wall_s;       /* wall time of the run */
   double last_dE;      /* |Delta E_int| of the final iteration */
   double t_gcg_s, t_fields_s, t_poisson_s, t_pairing_s; /* phase times */
+  /* E_INT recomputed with Lagrange-mesh derivatives for tau, J and the
+   * Laplacian of rho from the final orbitals ("EintLag",
+   * src/system/output.cpp:252-256, iteration_data.cpp:346-382) */
+  double E_int_lagrange;
 } ncgm_hf_result;
 
 /* Runs the WS guess and the HF(B) loop of main() (src/main.cpp:59-342) on the

@@ -71,7 +71,7 @@ class HFResult(C.Structure):
         ("beta", C.c_double), ("gamma", C.c_double), ("wall_s", C.c_double),
         ("last_dE", C.c_double), ("t_gcg_s", C.c_double),
         ("t_fields_s", C.c_double), ("t_poisson_s", C.c_double),
-        ("t_pairing_s", C.c_double)]
+        ("t_pairing_s", C.c_double), ("E_int_lagrange", C.c_double)]
 
 
 NCGM_OK = 0
@@ -104,6 +104,7 @@ SIGNATURES = {
     "ncgm_hf_run": ([C.POINTER(HFConfig), C.POINTER(HFResult), _vp, _vp, _vp,
                      _vp, _vp], _i),
     "ncgm_densities": ([_vp, _vp, _i, _vp, _vp, _vp, _vp], _i),
+    "ncgm_lagrange_densities": ([_vp, _vp, _i, _vp, _vp, _vp, _vp], _i),
     "ncgm_poisson": ([_vp, _vp, _i, _vp, _vp, _vp, _vp], _i),
     "ncgm_poisson_noalloc": ([_i, _d, _vp, _i, _vp, _vp, _vp, _vp, _vp], _i),
     "ncgm_hf_run_batch": ([_vp, _i, _i, _vp, _vp, _vp, _vp], _i),

@@ -803,7 +803,11 @@ double epair(Run &R, int q) {
   return R.sp[q].bcs.Epair;
 }
 
-int energies(Run &R, double &Eint, double &EHF) {
+// the energy integrals (iteration_data_integrals.cpp:95-262) of the run's
+// densities, with tau, J and the Laplacian of rho given; copied to e
+// (kEnergyTerms values) on the run's stream, not synchronised
+void energyTerms(Run &R, double *const tau[2], double *const J9[2],
+                 double *const lap[2], double *e) {
   const ncgm_hf_config &C = R.cfg;
   EnergyIn in;
   in.ns = R.ns;
@@ -814,18 +818,35 @@ int energies(Run &R, double &Eint, double &EHF) {
   in.massCorr = R.massCorr;
   in.rhoN = R.rho[0];
   in.rhoP = R.rho[1];
-  in.tauN = R.tau[0];
-  in.tauP = R.tau[1];
-  in.lapN = R.lap[0];
-  in.lapP = R.lap[1];
+  in.tauN = tau[0];
+  in.tauP = tau[1];
+  in.lapN = lap[0];
+  in.lapP = lap[1];
   in.divJN = R.divJ[0];
   in.divJP = R.divJ[1];
-  in.JN = R.J9[0];
-  in.JP = R.J9[1];
+  in.JN = J9[0];
+  in.JP = J9[1];
   in.UCDir = C.use_coulomb ? R.UCdir : nullptr;
   energyIntegrals(in, R.scratch, R.energy, R.s);
+  cudaMemcpyAsync(e, R.energy, sizeof(double) * kEnergyTerms,
+                  cudaMemcpyDeviceToHost, R.s);
+}
+
+// kinetic + totalEnergyIntegral (main.cpp:300-301) from the terms
+double integratedEnergy(Run &R, const double *e) {
+  const ncgm_hf_config &C = R.cfg;
+  const double cd = C.use_coulomb ? 0.5 * e[10] : 0.0;
+  const double sl = C.use_coulomb ? e[11] : 0.0;
+  const double total = e[0] + e[1] + e[2] + e[3] + e[4] + e[5] + cd +
+                       epair(R, 0) + epair(R, 1) + sl + e[6] + e[7] + e[8] +
+                       e[9];
+  return total + e[12];
+}
+
+int energies(Run &R, double &Eint, double &EHF) {
+  const ncgm_hf_config &C = R.cfg;
   double e[kEnergyTerms];
-  cudaMemcpyAsync(e, R.energy, sizeof(e), cudaMemcpyDeviceToHost, R.s);
+  energyTerms(R, R.tau, R.J9, R.lap, e);
   // constraint energies need int O rho with the current densities
   const int nc = (int)R.cons.size();
   std::vector<double> Qs(nc, 0.0);
@@ -845,13 +866,9 @@ int energies(Run &R, double &Eint, double &EHF) {
       for (int b = 0; b < nblk; ++b) Qs[c] += part[(size_t)c * nblk + b];
   }
   NCGM_TRY(sync(R));
-  const double cd = C.use_coulomb ? 0.5 * e[10] : 0.0;
   const double sl = C.use_coulomb ? e[11] : 0.0;
-  const double total = e[0] + e[1] + e[2] + e[3] + e[4] + e[5] + cd +
-                       epair(R, 0) + epair(R, 1) + sl + e[6] + e[7] + e[8] +
-                       e[9];
   const double kin = e[12];
-  Eint = total + kin;
+  Eint = integratedEnergy(R, e);
   double ce = 0;
   for (int c = 0; c < nc; ++c) {
     const Constraint &k = R.cons[c];
@@ -862,6 +879,34 @@ int energies(Run &R, double &Eint, double &EHF) {
   for (double v : R.sp[1].bcs.qp) qP += v;
   EHF = ce + 0.5 * (qN + qP + kin) + e[13] + sl / 3.0 + epair(R, 0) +
         epair(R, 1);
+  return NCGM_OK;
+}
+
+// Output::shellsToFile's Lagrange-mesh recompute (output.cpp:252-256,
+// iteration_data.cpp:346-382): tau, J and the Laplacian of rho from the
+// final occupied orbitals with Lagrange-mesh derivatives, rho and div J as
+// they are, then kinetic + totalEnergyIntegral ("EintLag").
+int lagrangeEnergy(Run &R, double &E) {
+  const size_t ns = R.ns;
+  double *w = R.alloc<double>(22 * ns);
+  void *scr = R.alloc<char>(lagrangeScratchBytes(R.n));
+  if (!w || !scr) {
+    setError("hf: device allocation for the Lagrange recompute failed");
+    return NCGM_ERR_NOMEM;
+  }
+  double *tau[2] = {w, w + ns}, *J9[2] = {w + 2 * ns, w + 11 * ns},
+         *lap[2] = {w + 20 * ns, w + 21 * ns};
+  for (int q = 0; q < 2; ++q) {
+    int nc = 0;
+    const double2 *Phi = nullptr;
+    NCGM_TRY(occupiedOrbitals(R, q, false, nc, Phi));
+    NCGM_TRY(lagrangeDensities(Phi, R.N, nc, R.n, R.h, R.rho[q], tau[q],
+                               J9[q], lap[q], scr, R.s));
+  }
+  double e[kEnergyTerms];
+  energyTerms(R, tau, J9, lap, e);
+  NCGM_TRY(sync(R));
+  E = integratedEnergy(R, e);
   return NCGM_OK;
 }
 
@@ -1209,6 +1254,7 @@ int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
     Eint = nE;
     EHF = nH;
   }
+  NCGM_TRY(lagrangeEnergy(R, res.E_int_lagrange));
   res.iterations = it;
   res.converged = conv;
   res.E_int = Eint;
@@ -1284,6 +1330,43 @@ extern "C" int ncgm_densities(ncgm_ctx *ctx, const double *Phi, int ncols,
                               cudaMemcpyDefault, ctx->stream));
     NCGM_CUDA(cudaMemcpyAsync(divJ, d + 11 * ns, ns * sizeof(double),
                               cudaMemcpyDefault, ctx->stream));
+    NCGM_CUDA(cudaStreamSynchronize(ctx->stream));
+    return NCGM_OK;
+  } catch (const std::exception &e) {
+    setError(e.what());
+    return NCGM_ERR_ARG;
+  }
+}
+
+extern "C" int ncgm_lagrange_densities(ncgm_ctx *ctx, const double *Phi,
+                                       int ncols, const double *rho,
+                                       double *tau, double *J9, double *lap) {
+  try {
+    if (!ctx || !Phi || ncols < 1 || !tau || !J9 || (!rho != !lap)) {
+      setError("ncgm_lagrange_densities: bad argument");
+      return NCGM_ERR_ARG;
+    }
+    const size_t N = ctx->N, ns = ctx->ns;
+    double2 *dX = static_cast<double2 *>(ctx->buf(26, N * ncols * sizeof(double2)));
+    double *d = static_cast<double *>(ctx->buf(
+        27, 12 * ns * sizeof(double) + lagrangeScratchBytes(ctx->n)));
+    if (!dX || !d) return NCGM_ERR_NOMEM;
+    NCGM_CUDA(cudaMemcpyAsync(dX, Phi, N * ncols * sizeof(double2),
+                              cudaMemcpyDefault, ctx->stream));
+    if (rho)
+      NCGM_CUDA(cudaMemcpyAsync(d + 11 * ns, rho, ns * sizeof(double),
+                                cudaMemcpyDefault, ctx->stream));
+    NCGM_TRY(lagrangeDensities(dX, N, ncols, ctx->n, ctx->h,
+                               rho ? d + 11 * ns : nullptr, d, d + ns,
+                               rho ? d + 10 * ns : nullptr, d + 12 * ns,
+                               ctx->stream));
+    NCGM_CUDA(cudaMemcpyAsync(tau, d, ns * sizeof(double), cudaMemcpyDefault,
+                              ctx->stream));
+    NCGM_CUDA(cudaMemcpyAsync(J9, d + ns, 9 * ns * sizeof(double),
+                              cudaMemcpyDefault, ctx->stream));
+    if (lap)
+      NCGM_CUDA(cudaMemcpyAsync(lap, d + 10 * ns, ns * sizeof(double),
+                                cudaMemcpyDefault, ctx->stream));
     NCGM_CUDA(cudaStreamSynchronize(ctx->stream));
     return NCGM_OK;
   } catch (const std::exception &e) {

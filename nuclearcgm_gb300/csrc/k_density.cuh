@@ -57,4 +57,13 @@ void integral(const double *f, const double *g, int n, double h,
 void normalizeColumns(double2 *X, size_t ld, int ncols, int n, double h,
                       double *work, cudaStream_t s);
 
+// Lagrange-mesh recompute of the output step (k_lagrange.cu): tau and J9
+// of the orbitals Phi (both or neither) and the Laplacian of rho (lap may
+// be null), with the Lagrange-mesh derivative matrices. scratch holds
+// lagrangeScratchBytes(n) device bytes. Synchronises s.
+size_t lagrangeScratchBytes(int n);
+int lagrangeDensities(const double2 *Phi, size_t ld, int M, int n, double h,
+                      const double *rho, double *tau, double *J9, double *lap,
+                      void *scratch, cudaStream_t s);
+
 } // namespace ncgm

@@ -64,6 +64,12 @@ void orc_divj(int n, double a, const double *psi, int ncols, double *divj);
 void orc_grad_nospin(int n, double a, const double *v, double *g3);
 void orc_lap_nospin(int n, double a, const double *v, double *lap);
 void orc_grad_spinor(int n, double a, const double *psi, double *g3);
+/* Lagrange-mesh gradient (g3: 3 x N complex) and the output step's
+ * recomputed tau, J9 and Laplacian of rho (rho and lap may be NULL) */
+void orc_grad_lagrange(int n, double a, const double *psi, double *g3);
+void orc_lagrange_densities(int n, double a, const double *psi, int ncols,
+                            const double *rho, double *tau, double *J9,
+                            double *lap);
 double orc_integral(int n, double a, const double *v);
 
 /* Coulomb direct potential by the Poisson solve (coulombFieldPoisson).

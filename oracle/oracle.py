@@ -50,6 +50,8 @@ def lib():
             "orc_grad_nospin": ([i, d, vp, vp], None),
             "orc_lap_nospin": ([i, d, vp, vp], None),
             "orc_grad_spinor": ([i, d, vp, vp], None),
+            "orc_grad_lagrange": ([i, d, vp, vp], None),
+            "orc_lagrange_densities": ([i, d, vp, i, vp, vp, vp, vp], None),
             "orc_integral": ([i, d, vp], d),
             "orc_poisson": ([i, d, vp, i, vp, vp], i),
             "orc_ho_guess": ([i, d, i, d, d, vp], None),
@@ -207,6 +209,29 @@ def grad_spinor(n, a, psi):
     out = np.zeros((3, 2 * n ** 3), np.complex128)
     lib().orc_grad_spinor(n, a, _p(psi), _p(out))
     return out
+
+
+def grad_lagrange(n, a, psi):
+    """Operators::gradLagrange of one spinor: (3, 2 n^3) complex."""
+    psi = np.ascontiguousarray(psi, np.complex128)
+    out = np.zeros((3, 2 * n ** 3), np.complex128)
+    lib().orc_grad_lagrange(n, a, _p(psi), _p(out))
+    return out
+
+
+def lagrange_densities(n, a, psi, rho=None):
+    """tau (n^3), J_{mu nu} (n^3 x 9) and, with rho, the Laplacian of rho,
+    all with the Lagrange-mesh derivatives of the output step."""
+    psi = _cmat(psi)
+    ncols = 1 if psi.ndim == 1 else psi.shape[1]
+    ns = n ** 3
+    tau, J9 = np.zeros(ns), np.zeros(9 * ns)
+    lap = np.zeros(ns) if rho is not None else None
+    r = _c(rho, np.float64) if rho is not None else None
+    lib().orc_lagrange_densities(n, a, _p(psi), ncols,
+                                 _p(r) if r is not None else None, _p(tau),
+                                 _p(J9), _p(lap) if lap is not None else None)
+    return tau, J9.reshape(9, ns).T, lap
 
 
 def integral(n, a, v):

@@ -157,6 +157,28 @@ void orc_grad_spinor(int n, double a, const double *psi, double *g3) {
   for (int ax = 0; ax < 3; ++ax)
     std::memcpy(g3 + 2 * ax * g.N(), out[ax].data(), sizeof(cd) * g.N());
 }
+void orc_grad_lagrange(int n, double a, const double *psi, double *g3) {
+  Grid g(n, a);
+  std::vector<cd> out[3];
+  gradLagrangeSpinor(g, asC(psi), out);
+  for (int ax = 0; ax < 3; ++ax)
+    std::memcpy(g3 + 2 * ax * g.N(), out[ax].data(), sizeof(cd) * g.N());
+}
+void orc_lagrange_densities(int n, double a, const double *psi, int ncols,
+                            const double *rho, double *tau, double *J9,
+                            double *lap) {
+  Grid g(n, a);
+  const CMat P = wrap(g, psi, ncols);
+  auto t = kineticDensityLagrange(g, P);
+  auto J = soDensityLagrange(g, P);
+  std::memcpy(tau, t.data(), sizeof(double) * t.size());
+  std::memcpy(J9, J.data(), sizeof(double) * J.size());
+  if (rho && lap) {
+    std::vector<double> in(rho, rho + g.ns());
+    auto l = lapLagrangeNoSpin(g, in);
+    std::memcpy(lap, l.data(), sizeof(double) * l.size());
+  }
+}
 double orc_integral(int n, double a, const double *v) {
   Grid g(n, a);
   return integral(g, v);

@@ -1318,6 +1318,24 @@ int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
     Eint = nE;
     EHF = nH;
   }
+  // Output::shellsToFile: tau, J and the Laplacian of rho recomputed with
+  // the Lagrange-mesh derivatives from the final orbitals, then E_INT again
+  // ("EintLag", src/system/output.cpp:252-256; iteration_data.cpp:346-382).
+  // rho and div J keep their values from the loop.
+  {
+    State L = st;
+    const CMat on = occupied(g, n.X, cfg, st, true, false);
+    const CMat op = occupied(g, p.X, cfg, st, false, false);
+    L.tauN = kineticDensityLagrange(g, on);
+    L.tauP = kineticDensityLagrange(g, op);
+    L.JN = soDensityLagrange(g, on);
+    L.JP = soDensityLagrange(g, op);
+    L.JvN = leviCivita(L.JN, g.ns());
+    L.JvP = leviCivita(L.JP, g.ns());
+    L.n2N = lapLagrangeNoSpin(g, st.rhoN);
+    L.n2P = lapLagrangeNoSpin(g, st.rhoP);
+    res.E_int_lagrange = kineticEnergy(g, L) + totalEnergyIntegral(g, cfg, L);
+  }
   res.iterations = it;
   res.converged = conv;
   res.E_int = Eint;

@@ -60,6 +60,13 @@ std::vector<double> density(const Grid &g, const CMat &psi);
 std::vector<double> kineticDensity(const Grid &g, const CMat &psi);
 std::vector<double> soDensity(const Grid &g, const CMat &psi);
 std::vector<double> divJ(const Grid &g, const CMat &psi);
+// Lagrange-mesh forms of the output step
+std::vector<double> lagrangeD1(int n, double h);
+void gradLagrangeSpinor(const Grid &g, const cd *psi, std::vector<cd> out[3]);
+std::vector<double> kineticDensityLagrange(const Grid &g, const CMat &psi);
+std::vector<double> soDensityLagrange(const Grid &g, const CMat &psi);
+std::vector<double> lapLagrangeNoSpin(const Grid &g,
+                                      const std::vector<double> &v);
 void normalize(const Grid &g, CMat &psi);
 CMat timeReverse(const Grid &g, const CMat &psi);
 CMat TROrder(const Grid &g, const CMat &psi);

@@ -274,6 +274,120 @@ std::vector<double> divJ(const Grid &g, const CMat &psi) {
   return W;
 }
 
+// ---------------------------------------------------------------------------
+// Lagrange-mesh derivatives of the output step (IterationData::
+// recomputeLagrange, src/util/iteration_data.cpp:346-382)
+// ---------------------------------------------------------------------------
+
+// lagrangeFirstDerivative (differential_operators.cpp:108-129), row-major:
+// D(s, t) = (-1)^(t-s) pi / (n h) / sin(pi (t - s) / n), zero diagonal
+std::vector<double> lagrangeD1(int n, double h) {
+  std::vector<double> D((std::size_t)n * n, 0.0);
+  for (int s = 0; s < n; ++s)
+    for (int t = 0; t < n; ++t) {
+      if (s == t) continue;
+      const double diff = static_cast<double>(t - s);
+      D[(std::size_t)s * n + t] = std::pow(-1.0, diff) * (M_PI / (n * h)) *
+                                  (1.0 / std::sin(M_PI * diff / n));
+    }
+  return D;
+}
+
+// Operators::gradLagrange (differential_operators.cpp:237-278): D's second
+// index contracted with each axis, negated: g_a = -D psi, both spins
+void gradLagrangeSpinor(const Grid &g, const cd *psi, std::vector<cd> out[3]) {
+  const int n = g.n;
+  const std::vector<double> D = lagrangeD1(n, g.h);
+  for (int ax = 0; ax < 3; ++ax) out[ax].assign(g.N(), cd(0, 0));
+#pragma omp parallel for schedule(static)
+  for (long long p = 0; p < (long long)g.ns(); ++p) {
+    const int i = (int)(p % n), j = (int)((p / n) % n), k = (int)(p / ((long long)n * n));
+    for (int s2 = 0; s2 < 2; ++s2) {
+      cd ax(0, 0), ay(0, 0), az(0, 0);
+      for (int t = 0; t < n; ++t) {
+        ax += D[(std::size_t)i * n + t] * psi[g.idx(t, j, k, s2)];
+        ay += D[(std::size_t)j * n + t] * psi[g.idx(i, t, k, s2)];
+        az += D[(std::size_t)k * n + t] * psi[g.idx(i, j, t, s2)];
+      }
+      out[0][2 * p + s2] = -ax;
+      out[1][2 * p + s2] = -ay;
+      out[2][2 * p + s2] = -az;
+    }
+  }
+}
+
+// kineticDensityLagrange (wavefunction.cpp:334-346)
+std::vector<double> kineticDensityLagrange(const Grid &g, const CMat &psi) {
+  std::vector<double> tau(g.ns(), 0.0);
+  std::vector<cd> gr[3];
+  for (std::size_t c = 0; c < psi.cols; ++c) {
+    gradLagrangeSpinor(g, psi.col(c), gr);
+    for (std::size_t l = 0; l < g.ns(); ++l) {
+      double m0 = 0.0, m1 = 0.0;
+      for (int ax = 0; ax < 3; ++ax) {
+        m0 += std::norm(gr[ax][2 * l]);
+        m1 += std::norm(gr[ax][2 * l + 1]);
+      }
+      tau[l] += m0 + m1;
+    }
+  }
+  return tau;
+}
+
+// soDensityLagrange (wavefunction.cpp:372-414): as soDensity with the
+// Lagrange gradient, n^3 x 9 column-major, col mu*3+nu
+std::vector<double> soDensityLagrange(const Grid &g, const CMat &psi) {
+  const std::size_t ns = g.ns();
+  std::vector<double> J(9 * ns, 0.0);
+  std::vector<cd> gr[3];
+  for (std::size_t c = 0; c < psi.cols; ++c) {
+    gradLagrangeSpinor(g, psi.col(c), gr);
+    const cd *ps = psi.col(c);
+    for (std::size_t l = 0; l < ns; ++l) {
+      const cd p0 = ps[2 * l], p1 = ps[2 * l + 1];
+      for (int mu = 0; mu < 3; ++mu)
+        for (int nu = 0; nu < 3; ++nu) {
+          cd q0, q1;
+          pauliApply(nu, gr[mu][2 * l], gr[mu][2 * l + 1], q0, q1);
+          J[(mu * 3 + nu) * ns + l] += p0.real() * q0.imag() -
+                                       p0.imag() * q0.real() +
+                                       p1.real() * q1.imag() -
+                                       p1.imag() * q1.real();
+        }
+    }
+  }
+  return J;
+}
+
+// Operators::lapLagrangeNoSpin (differential_operators.cpp:196-235): the
+// first index of D D contracted with each axis, x + y + z
+std::vector<double> lapLagrangeNoSpin(const Grid &g,
+                                      const std::vector<double> &v) {
+  const int n = g.n;
+  const std::vector<double> D = lagrangeD1(n, g.h);
+  std::vector<double> D2((std::size_t)n * n, 0.0); // D2(a, b) row-major
+  for (int a = 0; a < n; ++a)
+    for (int b = 0; b < n; ++b) {
+      double acc = 0.0;
+      for (int u = 0; u < n; ++u)
+        acc += D[(std::size_t)a * n + u] * D[(std::size_t)u * n + b];
+      D2[(std::size_t)a * n + b] = acc;
+    }
+  std::vector<double> out(g.ns(), 0.0);
+#pragma omp parallel for schedule(static)
+  for (long long p = 0; p < (long long)g.ns(); ++p) {
+    const int i = (int)(p % n), j = (int)((p / n) % n), k = (int)(p / ((long long)n * n));
+    double ax = 0, ay = 0, az = 0;
+    for (int s = 0; s < n; ++s) {
+      ax += D2[(std::size_t)s * n + i] * v[g.idxNS(s, j, k)];
+      ay += D2[(std::size_t)s * n + j] * v[g.idxNS(i, s, k)];
+      az += D2[(std::size_t)s * n + k] * v[g.idxNS(i, j, s)];
+    }
+    out[p] = ax + ay + az;
+  }
+  return out;
+}
+
 // Wavefunction::normalize (wavefunction.cpp:362-370)
 void normalize(const Grid &g, CMat &psi) {
   std::vector<double> rho(g.ns());

@@ -82,6 +82,11 @@ def _fixed_point(res_g, out_g, res_o, out_o, translation=False):
                               precision=2)))
     assert dE < E_TOL
     assert abs(res_g.E_HF - res_o.E_HF) < E_TOL
+    # the output step's Lagrange-mesh recompute of the same fixed point
+    dL = abs(res_g.E_int_lagrange - res_o.E_int_lagrange)
+    print("  Lagrange-mesh E_INT %.6f / %.6f MeV (|d| %.3e), E_INT %.6f" % (
+        res_g.E_int_lagrange, res_o.E_int_lagrange, dL, res_g.E_int))
+    assert np.isfinite(res_g.E_int_lagrange) and dL < E_TOL
     assert dS < SPE_TOL
     if translation:
         rem, shift = max(_rho_mod_translation(out_g["rho_n"], out_o["rho_n"]),

@@ -38,6 +38,35 @@ def test_densities_match_oracle(n):
         assert np.abs(got - ref).max() <= 1e-12 * max(np.abs(ref).max(), 1e-30)
 
 
+@pytest.mark.parametrize("n", [8, 11, 16])
+def test_lagrange_densities_match_oracle(n):
+    """The output step's Lagrange-mesh tau, J_{mu nu} and Laplacian of rho
+    (ncgm_lagrange_densities) against the oracle's restatement."""
+    a = 0.5 * (n - 1) * 0.8
+    ctx = ng.Context(ng.Grid(n, a), 8)
+    Phi = np.asfortranarray(random_block(2 * n ** 3, 5, 2 * n) * 0.1)
+    ns = n ** 3
+    rho = oracle.density(n, a, Phi)
+    tau, J9, lap = np.zeros(ns), np.zeros(9 * ns), np.zeros(ns)
+    ng._check(ng.load().ncgm_lagrange_densities(
+        ctx.h, Phi.ctypes.data, Phi.shape[1], rho.ctypes.data,
+        tau.ctypes.data, J9.ctypes.data, lap.ctypes.data))
+    tr, Jr, lr = oracle.lagrange_densities(n, a, Phi, rho)
+    for got, ref in ((tau, tr), (J9.reshape(9, ns).T, Jr), (lap, lr)):
+        assert np.abs(got - ref).max() <= 1e-12 * max(np.abs(ref).max(), 1e-30)
+    # without rho the Laplacian is skipped; tau and J are unchanged
+    t2, J2 = np.zeros(ns), np.zeros(9 * ns)
+    ng._check(ng.load().ncgm_lagrange_densities(
+        ctx.h, Phi.ctypes.data, Phi.shape[1], None, t2.ctypes.data,
+        J2.ctypes.data, None))
+    assert np.array_equal(t2, tau) and np.array_equal(J2, J9)
+    # rho without lap is an argument error
+    assert ng.load().ncgm_lagrange_densities(
+        ctx.h, Phi.ctypes.data, Phi.shape[1], rho.ctypes.data,
+        t2.ctypes.data, J2.ctypes.data, None) == abi.NCGM_OK + 1
+    ctx.close()
+
+
 def _gauss_rho(n, a, Z, w=2.5, shift=(0.3, -0.2, 0.5), zfac=1.3):
     h = 2 * a / (n - 1)
     xs = -a + np.arange(n) * h

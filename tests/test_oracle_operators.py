@@ -234,3 +234,68 @@ def test_pcg_reduces_residual():
     # row-point fields make H mildly non-Hermitian: CG still converges here
     assert (np.linalg.norm(R, axis=0) / np.linalg.norm(B, axis=0)).max() < 1e-6
     assert steps.max() <= 200
+
+
+def _index_waves(n, m):
+    """exp(2 pi i (m0 i + m1 j + m2 k) / n) on the lattice indices (x
+    fastest) and its three index wave numbers."""
+    ii = np.arange(n)
+    K, J, I = np.meshgrid(ii, ii, ii, indexing="ij")
+    ph = 2 * np.pi * (m[0] * I + m[1] * J + m[2] * K) / n
+    return np.exp(1j * ph).ravel()
+
+
+def test_lagrange_gradient_exact_on_band_limited_waves():
+    """lagrangeFirstDerivative with the gradLagrange contraction is the
+    derivative of the periodic trigonometric interpolant for odd n: exact
+    (to rounding) on waves below the Nyquist index, both spins, all axes."""
+    n, a = 11, 4.0
+    h = 2 * a / (n - 1)
+    m = (2, -3, 1)
+    up = _index_waves(n, m)
+    dn = 0.5 * _index_waves(n, (-1, 4, -2))
+    psi = np.zeros(2 * n ** 3, np.complex128)
+    psi[0::2], psi[1::2] = up, dn
+    g = oracle.grad_lagrange(n, a, psi)
+    for ax in range(3):
+        want_up = 1j * 2 * np.pi * m[ax] / (n * h) * up
+        want_dn = 1j * 2 * np.pi * (-1, 4, -2)[ax] / (n * h) * dn
+        assert np.abs(g[ax, 0::2] - want_up).max() < 1e-12
+        assert np.abs(g[ax, 1::2] - want_dn).max() < 1e-12
+
+
+def test_lagrange_laplacian_exact_on_band_limited_waves():
+    """lapLagrangeNoSpin (D D on each axis, summed) on a real wave: minus
+    the squared wave numbers, for odd n."""
+    n, a = 13, 5.0
+    h = 2 * a / (n - 1)
+    m = (1, 2, -4)
+    rho = np.real(_index_waves(n, m)) + 0.3
+    _, _, lap = oracle.lagrange_densities(
+        n, a, np.zeros((2 * n ** 3, 1), np.complex128), rho)
+    k2 = sum((2 * np.pi * mi / (n * h)) ** 2 for mi in m)
+    assert np.abs(lap - (-k2) * (rho - 0.3)).max() < 1e-10
+
+
+def test_lagrange_densities_from_the_gradient():
+    """tau = sum |g|^2 and J_{mu nu} = Im(psi^* sigma_nu g_mu) summed over
+    columns, restated in numpy from the oracle's Lagrange gradient."""
+    n, a = 7, 3.0
+    Phi = random_block(2 * n ** 3, 3, 17)
+    tau, J9, _ = oracle.lagrange_densities(n, a, Phi)
+    ns = n ** 3
+    sig = [np.array([[0, 1], [1, 0]]), np.array([[0, -1j], [1j, 0]]),
+           np.array([[1, 0], [0, -1]])]
+    tw, Jw = np.zeros(ns), np.zeros((ns, 9))
+    for c in range(Phi.shape[1]):
+        psi = Phi[:, c]
+        g = oracle.grad_lagrange(n, a, psi)
+        P = psi.reshape(ns, 2)
+        for mu in range(3):
+            G = g[mu].reshape(ns, 2)
+            tw += (np.abs(G) ** 2).sum(axis=1)
+            for nu in range(3):
+                Jw[:, mu * 3 + nu] += np.imag(
+                    (P.conj() * (G @ sig[nu].T)).sum(axis=1))
+    assert np.abs(tau - tw).max() < 1e-12 * np.abs(tw).max()
+    assert np.abs(J9 - Jw).max() < 1e-12 * np.abs(Jw).max()
