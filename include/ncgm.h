@@ -278,6 +278,48 @@ typedef struct ncgm_hf_result {
 int ncgm_hf_run(const ncgm_hf_config *cfg, ncgm_hf_result *res, double *spe_n,
                 double *spe_p, double *rho_n, double *rho_p, double *energies);
 
+/* What the reference's output step (Output::shellsToFile,
+ * src/system/output.cpp:97-408) reads from the final state. Array pointers
+ * may be NULL (not wanted) and may be host or device memory. */
+#define NCGM_ENERGY_TABLE 16
+typedef struct ncgm_hf_outputs {
+  /* final single-particle states, 2 n^3 x orbitals complex (Eigen layout) */
+  double *orbitals_n, *orbitals_p;
+  /* kinetic densities after the Lagrange-mesh recompute (n^3) */
+  double *tau_n, *tau_p;
+  /* Lagrange-mesh gradients of rho_n / rho_p (n^3 x 3, column-major),
+   * Operators::gradLagrangeNoSpin (differential_operators.cpp:156-194) */
+  double *grad_rho_n, *grad_rho_p;
+  /* mean fields U_n / U_p (n^3) */
+  double *U_n, *U_p;
+  /* filled always: the "Density Functional contributions" table
+   * (output.cpp:205-236) in its order: E_kin, C0 rho0, C1 rho1,
+   * C0 nabla2rho0, C1 nabla2rho1, C0 tau0, C1 tau1, C0 div J, C1 div J,
+   * C0 J2, C1 J2, E coulomb direct, E pairing n, E pairing p,
+   * E coulomb exchange, E rearrangement (Erear) */
+  double terms[NCGM_ENERGY_TABLE];
+  /* filled always: sum of the constraints' evaluate() on the final
+   * densities (output.cpp:357-360) */
+  double constraints_energy;
+} ncgm_hf_outputs;
+
+/* ncgm_hf_run plus the output step's arrays and energy table. */
+int ncgm_hf_run_ex(const ncgm_hf_config *cfg, ncgm_hf_result *res,
+                   double *spe_n, double *spe_p, double *rho_n, double *rho_p,
+                   double *energies, ncgm_hf_outputs *out);
+
+/* Shell observables of ncols spinor columns Psi (N x ncols, Eigen layout),
+ * obs (ncols x 5, one row per column): the real parts of
+ * int psi conj(L^2 psi), int psi conj(J^2 psi), int psi conj(Jz Jz psi)
+ * (trapezoid integrals with hbar = 197.327053 MeV fm),
+ * sum_r psi(-r)^* psi(r), and int psi conj(L.S psi). These are the
+ * quantities of Shell::l / j / mj / P (src/util/shell.cpp:22-51) and of the
+ * spin-orbit correction of IterationData::chargeRadius
+ * (src/util/iteration_data.cpp:121-151), with the operators of
+ * src/operators/angular_momentum.cpp. */
+int ncgm_shell_observables(ncgm_ctx *ctx, const double *Psi, int ncols,
+                           double *obs);
+
 /* C (p x q) = A^H B for complex column blocks of ctx->N rows (A: N x p,
  * B: N x q, Eigen layout; host or device buffers): the Gram / projection
  * products of the GCG (src/solver/solver.cpp:750-777, V.adjoint() * W).

@@ -210,19 +210,55 @@ def solve(H: Hamiltonian, ConjDir, calc: dict, guess, nev=None,
                                   precision)
 
 
-def hf_run(cfg: abi.HFConfig):
-    """Runs the WS guess and HF(B) iteration on the GPU (ncgm_hf_run)."""
+def hf_run(cfg: abi.HFConfig, outputs: bool = False):
+    """Runs the WS guess and HF(B) iteration on the GPU (ncgm_hf_run).
+    With outputs, also what the reference's output step reads
+    (ncgm_hf_run_ex): the final orbitals, the recomputed kinetic densities,
+    the Lagrange-mesh gradients of rho, the mean fields and the energy
+    table."""
     res = abi.HFResult()
     on, op = config.orbital_counts(cfg)
     ns = cfg.n ** 3
     spe_n, spe_p = np.zeros(on), np.zeros(op)
     rho_n, rho_p = np.zeros(ns), np.zeros(ns)
     en = np.zeros((max(cfg.max_iterations, 1), 2))
-    _check(load().ncgm_hf_run(C.byref(cfg), C.byref(res), spe_n.ctypes.data,
-                              spe_p.ctypes.data, rho_n.ctypes.data,
-                              rho_p.ctypes.data, en.ctypes.data))
-    return res, {"spe_n": spe_n, "spe_p": spe_p, "rho_n": rho_n,
-                 "rho_p": rho_p, "energies": en[:res.iterations]}
+    arrays = {"spe_n": spe_n, "spe_p": spe_p, "rho_n": rho_n, "rho_p": rho_p}
+    if not outputs:
+        _check(load().ncgm_hf_run(C.byref(cfg), C.byref(res),
+                                  spe_n.ctypes.data, spe_p.ctypes.data,
+                                  rho_n.ctypes.data, rho_p.ctypes.data,
+                                  en.ctypes.data))
+    else:
+        N = 2 * ns
+        extra = {"orbitals_n": np.zeros((N, on), np.complex128, order="F"),
+                 "orbitals_p": np.zeros((N, op), np.complex128, order="F"),
+                 "tau_n": np.zeros(ns), "tau_p": np.zeros(ns),
+                 "grad_rho_n": np.zeros(3 * ns), "grad_rho_p": np.zeros(3 * ns),
+                 "U_n": np.zeros(ns), "U_p": np.zeros(ns)}
+        out = abi.HFOutputs(**{k: v.ctypes.data for k, v in extra.items()})
+        _check(load().ncgm_hf_run_ex(C.byref(cfg), C.byref(res),
+                                     spe_n.ctypes.data, spe_p.ctypes.data,
+                                     rho_n.ctypes.data, rho_p.ctypes.data,
+                                     en.ctypes.data, C.byref(out)))
+        for q in ("n", "p"):
+            extra["grad_rho_" + q] = extra["grad_rho_" + q].reshape(3, ns).T
+        arrays.update(extra)
+        arrays["terms"] = np.array(out.terms[:])
+        arrays["constraints_energy"] = out.constraints_energy
+    arrays["energies"] = en[:res.iterations]
+    return res, arrays
+
+
+def shell_observables(ctx: "Context", psi):
+    """ncgm_shell_observables: per column [<L^2>, <J^2>, <Jz Jz>, parity
+    overlap, <L.S>] (see include/ncgm.h), shape (ncols, 5)."""
+    psi = np.asfortranarray(psi, dtype=np.complex128)
+    if psi.ndim == 1:
+        psi = psi.reshape(-1, 1, order="F")
+    obs = np.zeros((psi.shape[1], 5))
+    _check(load().ncgm_shell_observables(ctx.h, psi.ctypes.data, psi.shape[1],
+                                         obs.ctypes.data))
+    return obs
 
 
 class LearnedPreconditioner:

@@ -74,6 +74,23 @@ class HFResult(C.Structure):
         ("t_pairing_s", C.c_double), ("E_int_lagrange", C.c_double)]
 
 
+ENERGY_TABLE = 16  # NCGM_ENERGY_TABLE
+# labels of ncgm_hf_outputs.terms, as the reference's log prints them
+ENERGY_TABLE_LABELS = (
+    "E (kin)", "C0 Rho0", "C1 Rho1", "C0 nabla2Rho0", "C1 nabla2Rho1",
+    "C0 tau0", "C1 tau1", "C0 div J", "C1 div J", "C0 J2", "C1 J2",
+    "E coulomb direct", "E pairing neutrons", "E pairing protons",
+    "E coulomb exchange", "E (REA)")
+
+
+class HFOutputs(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in (
+        "orbitals_n", "orbitals_p", "tau_n", "tau_p", "grad_rho_n",
+        "grad_rho_p", "U_n", "U_p")] + [
+        ("terms", C.c_double * ENERGY_TABLE),
+        ("constraints_energy", C.c_double)]
+
+
 NCGM_OK = 0
 STATUS = {0: "NCGM_OK", 1: "NCGM_ERR_ARG", 2: "NCGM_ERR_CUDA",
           3: "NCGM_ERR_NAN", 4: "NCGM_ERR_RANK", 5: "NCGM_ERR_TIMEOUT",
@@ -105,6 +122,9 @@ SIGNATURES = {
                      _vp, _vp], _i),
     "ncgm_densities": ([_vp, _vp, _i, _vp, _vp, _vp, _vp], _i),
     "ncgm_lagrange_densities": ([_vp, _vp, _i, _vp, _vp, _vp, _vp], _i),
+    "ncgm_hf_run_ex": ([C.POINTER(HFConfig), C.POINTER(HFResult), _vp, _vp,
+                        _vp, _vp, _vp, C.POINTER(HFOutputs)], _i),
+    "ncgm_shell_observables": ([_vp, _vp, _i, _vp], _i),
     "ncgm_poisson": ([_vp, _vp, _i, _vp, _vp, _vp, _vp], _i),
     "ncgm_poisson_noalloc": ([_i, _d, _vp, _i, _vp, _vp, _vp, _vp, _vp], _i),
     "ncgm_hf_run_batch": ([_vp, _i, _i, _vp, _vp, _vp, _vp], _i),

@@ -187,6 +187,7 @@ struct Run {
   Species sp[2];
   std::vector<Constraint> cons;
   double tPair = 0, tFields = 0, tPoisson = 0, tGcg = 0;
+  double constraintEnergy = 0; // of the last energy evaluation
   std::vector<void *> allocs;
   // tensor-core form: scratch of the exact-digit Gram / V C products of the
   // driver's own overlaps and rotations (allocated on first use)
@@ -874,6 +875,7 @@ int energies(Run &R, double &Eint, double &EHF) {
     const Constraint &k = R.cons[c];
     ce += k.C * std::pow(Qs[c] - k.target, 2) + k.lambda * (Qs[c] - k.target);
   }
+  R.constraintEnergy = ce;
   double qN = 0, qP = 0;
   for (double v : R.sp[0].bcs.qp) qN += v;
   for (double v : R.sp[1].bcs.qp) qP += v;
@@ -886,28 +888,85 @@ int energies(Run &R, double &Eint, double &EHF) {
 // iteration_data.cpp:346-382): tau, J and the Laplacian of rho from the
 // final occupied orbitals with Lagrange-mesh derivatives, rho and div J as
 // they are, then kinetic + totalEnergyIntegral ("EintLag").
-int lagrangeEnergy(Run &R, double &E) {
+// With out, the recomputed tau and the Lagrange-mesh gradient of rho (the
+// fields the reference's output step writes after the recompute) are copied
+// to it as well.
+int lagrangeEnergy(Run &R, double &E, ncgm_hf_outputs *out) {
   const size_t ns = R.ns;
-  double *w = R.alloc<double>(22 * ns);
+  double *w = R.alloc<double>(28 * ns);
   void *scr = R.alloc<char>(lagrangeScratchBytes(R.n));
   if (!w || !scr) {
     setError("hf: device allocation for the Lagrange recompute failed");
     return NCGM_ERR_NOMEM;
   }
   double *tau[2] = {w, w + ns}, *J9[2] = {w + 2 * ns, w + 11 * ns},
-         *lap[2] = {w + 20 * ns, w + 21 * ns};
+         *lap[2] = {w + 20 * ns, w + 21 * ns},
+         *g3[2] = {w + 22 * ns, w + 25 * ns};
   for (int q = 0; q < 2; ++q) {
     int nc = 0;
     const double2 *Phi = nullptr;
     NCGM_TRY(occupiedOrbitals(R, q, false, nc, Phi));
     NCGM_TRY(lagrangeDensities(Phi, R.N, nc, R.n, R.h, R.rho[q], tau[q],
-                               J9[q], lap[q], scr, R.s));
+                               J9[q], lap[q], out ? g3[q] : nullptr, scr,
+                               R.s));
   }
   double e[kEnergyTerms];
   energyTerms(R, tau, J9, lap, e);
   NCGM_TRY(sync(R));
   E = integratedEnergy(R, e);
+  if (out) {
+    double *const dt[2] = {out->tau_n, out->tau_p};
+    double *const dg[2] = {out->grad_rho_n, out->grad_rho_p};
+    for (int q = 0; q < 2; ++q) {
+      if (dt[q])
+        NCGM_CUDA(cudaMemcpyAsync(dt[q], tau[q], ns * sizeof(double),
+                                  cudaMemcpyDefault, R.s));
+      if (dg[q])
+        NCGM_CUDA(cudaMemcpyAsync(dg[q], g3[q], 3 * ns * sizeof(double),
+                                  cudaMemcpyDefault, R.s));
+    }
+    NCGM_TRY(sync(R));
+  }
   return NCGM_OK;
+}
+
+// the output step's energy table (output.cpp:205-236, printed before the
+// Lagrange recompute), the final orbitals and the mean fields
+int fillOutputs(Run &R, ncgm_hf_outputs *out) {
+  const ncgm_hf_config &C = R.cfg;
+  double e[kEnergyTerms];
+  energyTerms(R, R.tau, R.J9, R.lap, e);
+  NCGM_TRY(sync(R));
+  double *t = out->terms;
+  t[0] = e[12];
+  t[1] = e[0];
+  t[2] = e[1];
+  t[3] = e[2];
+  t[4] = e[3];
+  t[5] = e[4];
+  t[6] = e[5];
+  t[7] = e[8];
+  t[8] = e[9];
+  t[9] = e[6];
+  t[10] = e[7];
+  t[11] = C.use_coulomb ? 0.5 * e[10] : 0.0;
+  t[12] = epair(R, 0);
+  t[13] = epair(R, 1);
+  t[14] = C.use_coulomb ? e[11] : 0.0;
+  t[15] = e[13];
+  out->constraints_energy = R.constraintEnergy;
+  double *const orb[2] = {out->orbitals_n, out->orbitals_p};
+  double *const U[2] = {out->U_n, out->U_p};
+  for (int q = 0; q < 2; ++q) {
+    if (orb[q])
+      NCGM_CUDA(cudaMemcpyAsync(orb[q], R.sp[q].X,
+                                R.N * R.sp[q].orb * sizeof(double2),
+                                cudaMemcpyDefault, R.s));
+    if (U[q])
+      NCGM_CUDA(cudaMemcpyAsync(U[q], R.U[q], R.ns * sizeof(double),
+                                cudaMemcpyDefault, R.s));
+  }
+  return sync(R);
 }
 
 // Wavefunction::TROrder (wavefunction.cpp:581-635)
@@ -1022,7 +1081,8 @@ std::vector<int4> hoOrbitals(int nev) {
 }
 
 int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
-          double *spe_p, double *rho_n, double *rho_p, double *energiesOut) {
+          double *spe_p, double *rho_n, double *rho_p, double *energiesOut,
+          ncgm_hf_outputs *out) {
   const double tStart = now();
   Run R;
   R.cfg = cfg;
@@ -1254,7 +1314,8 @@ int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
     Eint = nE;
     EHF = nH;
   }
-  NCGM_TRY(lagrangeEnergy(R, res.E_int_lagrange));
+  if (out) NCGM_TRY(fillOutputs(R, out));
+  NCGM_TRY(lagrangeEnergy(R, res.E_int_lagrange, out));
   res.iterations = it;
   res.converged = conv;
   res.E_int = Eint;
@@ -1299,7 +1360,48 @@ extern "C" int ncgm_hf_run(const ncgm_hf_config *cfg, ncgm_hf_result *res,
       return NCGM_ERR_ARG;
     }
     std::memset(res, 0, sizeof(*res));
-    return hfRun(*cfg, *res, spe_n, spe_p, rho_n, rho_p, energies);
+    return hfRun(*cfg, *res, spe_n, spe_p, rho_n, rho_p, energies, nullptr);
+  } catch (const std::exception &e) {
+    setError(e.what());
+    return NCGM_ERR_ARG;
+  }
+}
+
+extern "C" int ncgm_hf_run_ex(const ncgm_hf_config *cfg, ncgm_hf_result *res,
+                              double *spe_n, double *spe_p, double *rho_n,
+                              double *rho_p, double *energies,
+                              ncgm_hf_outputs *out) {
+  try {
+    if (!cfg || !res || !out || cfg->n < 4 || cfg->box_size <= 0 ||
+        cfg->A < 2 || cfg->Z < 0 || cfg->Z > cfg->A ||
+        cfg->max_iterations < 0) {
+      setError("ncgm_hf_run_ex: bad configuration");
+      return NCGM_ERR_ARG;
+    }
+    std::memset(res, 0, sizeof(*res));
+    std::memset(out->terms, 0, sizeof(out->terms));
+    return hfRun(*cfg, *res, spe_n, spe_p, rho_n, rho_p, energies, out);
+  } catch (const std::exception &e) {
+    setError(e.what());
+    return NCGM_ERR_ARG;
+  }
+}
+
+extern "C" int ncgm_shell_observables(ncgm_ctx *ctx, const double *Psi,
+                                      int ncols, double *obs) {
+  try {
+    if (!ctx || !Psi || ncols < 1 || !obs) {
+      setError("ncgm_shell_observables: bad argument");
+      return NCGM_ERR_ARG;
+    }
+    const size_t N = ctx->N;
+    double2 *dX = static_cast<double2 *>(ctx->buf(26, N * ncols * sizeof(double2)));
+    void *scr = ctx->buf(27, shellScratchBytes(ctx->n));
+    if (!dX || !scr) return NCGM_ERR_NOMEM;
+    NCGM_CUDA(cudaMemcpyAsync(dX, Psi, N * ncols * sizeof(double2),
+                              cudaMemcpyDefault, ctx->stream));
+    return shellObservables(dX, N, ncols, ctx->n, ctx->a, scr, obs,
+                            ctx->stream);
   } catch (const std::exception &e) {
     setError(e.what());
     return NCGM_ERR_ARG;
@@ -1358,8 +1460,8 @@ extern "C" int ncgm_lagrange_densities(ncgm_ctx *ctx, const double *Phi,
                                 cudaMemcpyDefault, ctx->stream));
     NCGM_TRY(lagrangeDensities(dX, N, ncols, ctx->n, ctx->h,
                                rho ? d + 11 * ns : nullptr, d, d + ns,
-                               rho ? d + 10 * ns : nullptr, d + 12 * ns,
-                               ctx->stream));
+                               rho ? d + 10 * ns : nullptr, nullptr,
+                               d + 12 * ns, ctx->stream));
     NCGM_CUDA(cudaMemcpyAsync(tau, d, ns * sizeof(double), cudaMemcpyDefault,
                               ctx->stream));
     NCGM_CUDA(cudaMemcpyAsync(J9, d + ns, 9 * ns * sizeof(double),

@@ -14,36 +14,14 @@
 //  * energyKernel: the trapezoid-weighted energy integrals of
 //    iteration_data.cpp:153-271 and iteration_data_integrals.cpp:95-262.
 // All FP64: these feed the fixed point whose energies are compared at keV.
+#include "fd_deriv.cuh"
 #include "k_density.cuh"
 
 namespace ncgm {
 
 namespace {
 
-template <class T, class Get>
-__device__ __forceinline__ T d1(const Get &g, int pos, int n, double h) {
-  if (pos == 0) {
-    return (g(pos + 1) - g(pos)) / h;
-  } else if (pos == 1 || pos == n - 2) {
-    return (g(pos + 1) - g(pos - 1)) / (2.0 * h);
-  } else if (pos == n - 1) {
-    return (g(pos) - g(pos - 1)) / h;
-  } else if (pos == 2 || pos == n - 3) {
-    T f_2 = g(pos - 2), f_1 = g(pos - 1), f1 = g(pos + 1), f2 = g(pos + 2);
-    return (-f2 + 8.0 * f1 - 8.0 * f_1 + f_2) / (12.0 * h);
-  } else if (pos == 3 || pos == n - 4) {
-    T f_3 = g(pos - 3), f_2 = g(pos - 2), f_1 = g(pos - 1);
-    T f1 = g(pos + 1), f2 = g(pos + 2), f3 = g(pos + 3);
-    return (-f_3 + 9.0 * f_2 - 45.0 * f_1 + 45.0 * f1 - 9.0 * f2 + f3) /
-           (60.0 * h);
-  } else {
-    T f_4 = g(pos - 4), f_3 = g(pos - 3), f_2 = g(pos - 2), f_1 = g(pos - 1);
-    T f1 = g(pos + 1), f2 = g(pos + 2), f3 = g(pos + 3), f4 = g(pos + 4);
-    return (3.0 * f_4 - 32.0 * f_3 + 168.0 * f_2 - 672.0 * f_1 + 672.0 * f1 -
-            168.0 * f2 + 32.0 * f3 - 3.0 * f4) /
-           (840.0 * h);
-  }
-}
+using fd::d1;
 
 __device__ __forceinline__ double d2(const double *v, size_t base,
                                      size_t stride, int pos, int n, double h) {

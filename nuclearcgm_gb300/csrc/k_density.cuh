@@ -58,12 +58,20 @@ void normalizeColumns(double2 *X, size_t ld, int ncols, int n, double h,
                       double *work, cudaStream_t s);
 
 // Lagrange-mesh recompute of the output step (k_lagrange.cu): tau and J9
-// of the orbitals Phi (both or neither) and the Laplacian of rho (lap may
-// be null), with the Lagrange-mesh derivative matrices. scratch holds
-// lagrangeScratchBytes(n) device bytes. Synchronises s.
+// of the orbitals Phi (both or neither), the Laplacian of rho and its
+// gradient (n^3 x 3; lap and grad3 may be null), with the Lagrange-mesh
+// derivative matrices. scratch holds lagrangeScratchBytes(n) device bytes.
+// Synchronises s.
 size_t lagrangeScratchBytes(int n);
 int lagrangeDensities(const double2 *Phi, size_t ld, int M, int n, double h,
                       const double *rho, double *tau, double *J9, double *lap,
-                      void *scratch, cudaStream_t s);
+                      double *grad3, void *scratch, cudaStream_t s);
+// Shell observables of ncols spinor columns (k_shells.cu): per column
+// [int psi conj(L^2 psi), int psi conj(J^2 psi), int psi conj(Jz Jz psi),
+// Re sum psi(-r)^* psi(r), int psi conj(L.S psi)] (real parts).
+// scratch holds shellScratchBytes(n) device bytes. Synchronises s.
+size_t shellScratchBytes(int n);
+int shellObservables(const double2 *Psi, size_t ld, int ncols, int n,
+                     double a, void *scratch, double *obs, cudaStream_t s);
 
 } // namespace ncgm

@@ -115,12 +115,20 @@ __global__ void lagrangeTauJKernel(const double2 *__restrict__ Phi, size_t ld,
 }
 
 // lap(p) = sum over axes of sum_s D2(s, t_a) v(s along a), D2 = D D;
-// D2t[r * n + c] = D2(c, r) so a thread reads its own row
+// D2t[r * n + c] = D2(c, r) so a thread reads its own row. With g3 also
+// gradLagrangeNoSpin (differential_operators.cpp:156-194): g_a(t) =
+// sum_s D(s, t) v(s along a) from Dt[r * n + c] = D(c, r), n^3 x 3
+// column-major.
 __global__ void lagrangeLapKernel(const double *__restrict__ v, int n,
                                   const double *__restrict__ D2t,
-                                  double *lap) {
+                                  const double *__restrict__ Dt, double *lap,
+                                  double *g3) {
   extern __shared__ double Ds[];
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) Ds[e] = D2t[e];
+  double *Dg = Ds + (size_t)n * n;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    Ds[e] = D2t[e];
+    if (g3) Dg[e] = Dt[e];
+  }
   __syncthreads();
   const size_t ns = (size_t)n * n * n;
   const size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -135,7 +143,18 @@ __global__ void lagrangeLapKernel(const double *__restrict__ v, int n,
     ay += Ds[(size_t)j * n + s] * v[by + s * sy];
     az += Ds[(size_t)k * n + s] * v[bz + s * sz];
   }
-  lap[p] = ax + ay + az;
+  if (lap) lap[p] = ax + ay + az;
+  if (g3) {
+    double gx = 0, gy = 0, gz = 0;
+    for (int s = 0; s < n; ++s) {
+      gx += Dg[(size_t)i * n + s] * v[bx + s];
+      gy += Dg[(size_t)j * n + s] * v[by + s * sy];
+      gz += Dg[(size_t)k * n + s] * v[bz + s * sz];
+    }
+    g3[p] = gx;
+    g3[ns + p] = gy;
+    g3[2 * ns + p] = gz;
+  }
 }
 
 // lagrangeFirstDerivative (differential_operators.cpp:108-129), row-major
@@ -153,14 +172,14 @@ std::vector<double> firstDerivative(int n, double h) {
 
 } // namespace
 
-size_t lagrangeScratchBytes(int n) { return 2 * (size_t)n * n * sizeof(double); }
+size_t lagrangeScratchBytes(int n) { return 3 * (size_t)n * n * sizeof(double); }
 
 int lagrangeDensities(const double2 *Phi, size_t ld, int M, int n, double h,
                       const double *rho, double *tau, double *J9, double *lap,
-                      void *scratch, cudaStream_t s) {
+                      double *grad3, void *scratch, cudaStream_t s) {
   const size_t smem = (size_t)n * n * sizeof(double);
-  if (smem > 200 * 1024) {
-    setError("Lagrange recompute: lattice above 160 points per axis");
+  if (2 * smem > 200 * 1024) {
+    setError("Lagrange recompute: lattice above 113 points per axis");
     return NCGM_ERR_ARG;
   }
   static const bool attr = [] {
@@ -182,10 +201,14 @@ int lagrangeDensities(const double2 *Phi, size_t ld, int M, int n, double h,
       for (int u = 0; u < n; ++u) acc += D[(size_t)a * n + u] * D[(size_t)u * n + b];
       D2t[(size_t)b * n + a] = acc;
     }
+  std::vector<double> Dt((size_t)n * n);
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c) Dt[(size_t)r * n + c] = D[(size_t)c * n + r];
   double *dD = static_cast<double *>(scratch);
-  double *dD2 = dD + (size_t)n * n;
+  double *dD2 = dD + (size_t)n * n, *dDt = dD2 + (size_t)n * n;
   NCGM_CUDA(cudaMemcpyAsync(dD, D.data(), smem, cudaMemcpyHostToDevice, s));
   NCGM_CUDA(cudaMemcpyAsync(dD2, D2t.data(), smem, cudaMemcpyHostToDevice, s));
+  NCGM_CUDA(cudaMemcpyAsync(dDt, Dt.data(), smem, cudaMemcpyHostToDevice, s));
   const size_t ns = (size_t)n * n * n;
   const unsigned blocks = (unsigned)((ns + 127) / 128);
   if (tau && J9) {
@@ -197,7 +220,9 @@ int lagrangeDensities(const double2 *Phi, size_t ld, int M, int n, double h,
       NCGM_CUDA(cudaMemsetAsync(J9, 0, 9 * ns * sizeof(double), s));
     }
   }
-  if (rho && lap) lagrangeLapKernel<<<blocks, 128, smem, s>>>(rho, n, dD2, lap);
+  if (rho && (lap || grad3))
+    lagrangeLapKernel<<<blocks, 128, 2 * smem, s>>>(rho, n, dD2, dDt, lap,
+                                                     grad3);
   NCGM_CUDA(cudaGetLastError());
   // the host vectors must outlive the copies
   NCGM_CUDA(cudaStreamSynchronize(s));

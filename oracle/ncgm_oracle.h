@@ -86,6 +86,12 @@ void orc_ho_guess(int n, double a, int nev, double b, double beta,
 int orc_hf_run(const ncgm_hf_config *cfg, ncgm_hf_result *res, double *spe_n,
                double *spe_p, double *rho_n, double *rho_p, double *energies,
                int verbose);
+int orc_hf_run_ex(const ncgm_hf_config *cfg, ncgm_hf_result *res,
+                  double *spe_n, double *spe_p, double *rho_n, double *rho_p,
+                  double *energies, ncgm_hf_outputs *out, int verbose);
+/* obs: ncols x 5 as ncgm_shell_observables */
+void orc_shell_observables(int n, double a, const double *psi, int ncols,
+                           double *obs);
 
 #ifdef __cplusplus
 }

@@ -56,6 +56,8 @@ def lib():
             "orc_poisson": ([i, d, vp, i, vp, vp], i),
             "orc_ho_guess": ([i, d, i, d, d, vp], None),
             "orc_hf_run": ([vp, vp, vp, vp, vp, vp, vp, i], i),
+            "orc_hf_run_ex": ([vp, vp, vp, vp, vp, vp, vp, vp, i], i),
+            "orc_shell_observables": ([i, d, vp, i, vp], None),
         }
         for name, (a, r) in sig.items():
             f = getattr(_lib, name)
@@ -250,6 +252,46 @@ def ho_guess(n, a, nev, b, beta=0.0):
     out = np.zeros((2 * n ** 3, nev), np.complex128, order="F")
     lib().orc_ho_guess(n, a, nev, b, beta, _p(out))
     return out
+
+
+def shell_observables(n, a, psi):
+    """orc_shell_observables: (ncols, 5) as ncgm_shell_observables."""
+    psi = _cmat(psi)
+    if psi.ndim == 1:
+        psi = psi.reshape(-1, 1, order="F")
+    obs = np.zeros((psi.shape[1], 5))
+    lib().orc_shell_observables(n, a, _p(psi), psi.shape[1], _p(obs))
+    return obs
+
+
+def hf_run_ex(cfg, verbose=False):
+    """orc_hf_run_ex: hf_run plus the output step's arrays and energy table
+    (the keys of nuclearcgm_gb300.hf_run(cfg, outputs=True))."""
+    from nuclearcgm_gb300 import abi, config
+    res = abi.HFResult()
+    on, op = config.orbital_counts(cfg)
+    ns = cfg.n ** 3
+    N = 2 * ns
+    arr = {"spe_n": np.zeros(on), "spe_p": np.zeros(op),
+           "rho_n": np.zeros(ns), "rho_p": np.zeros(ns)}
+    en = np.zeros((max(cfg.max_iterations, 1), 2))
+    extra = {"orbitals_n": np.zeros((N, on), np.complex128, order="F"),
+             "orbitals_p": np.zeros((N, op), np.complex128, order="F"),
+             "tau_n": np.zeros(ns), "tau_p": np.zeros(ns),
+             "grad_rho_n": np.zeros(3 * ns), "grad_rho_p": np.zeros(3 * ns),
+             "U_n": np.zeros(ns), "U_p": np.zeros(ns)}
+    out = abi.HFOutputs(**{k: v.ctypes.data for k, v in extra.items()})
+    lib().orc_hf_run_ex(C.addressof(cfg), C.addressof(res),
+                        _p(arr["spe_n"]), _p(arr["spe_p"]), _p(arr["rho_n"]),
+                        _p(arr["rho_p"]), _p(en), C.addressof(out),
+                        int(verbose))
+    for q in ("n", "p"):
+        extra["grad_rho_" + q] = extra["grad_rho_" + q].reshape(3, ns).T
+    arr.update(extra)
+    arr["terms"] = np.array(out.terms[:])
+    arr["constraints_energy"] = out.constraints_energy
+    arr["energies"] = en[:res.iterations]
+    return res, arr
 
 
 def hf_run(cfg, verbose=False):

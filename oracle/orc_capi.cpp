@@ -206,4 +206,18 @@ int orc_hf_run(const ncgm_hf_config *cfg, ncgm_hf_result *res, double *spe_n,
   return hfRun(*cfg, *res, spe_n, spe_p, rho_n, rho_p, energies, verbose);
 }
 
+int orc_hf_run_ex(const ncgm_hf_config *cfg, ncgm_hf_result *res,
+                  double *spe_n, double *spe_p, double *rho_n, double *rho_p,
+                  double *energies, ncgm_hf_outputs *out, int verbose) {
+  std::memset(res, 0, sizeof(*res));
+  std::memset(out->terms, 0, sizeof(out->terms));
+  return hfRun(*cfg, *res, spe_n, spe_p, rho_n, rho_p, energies, verbose, out);
+}
+void orc_shell_observables(int n, double a, const double *psi, int ncols,
+                           double *obs) {
+  Grid g(n, a);
+  for (int c = 0; c < ncols; ++c)
+    shellObservables(g, asC(psi) + (std::size_t)c * g.N(), obs + 5 * c);
+}
+
 } // extern "C"

@@ -6,6 +6,7 @@
 
 #include <chrono>
 #include <cstdio>
+#include <cstring>
 #include <memory>
 #include <tuple>
 
@@ -1185,9 +1186,56 @@ static void quadDef(const Grid &g, const State &st, int A, double &beta,
   beta = 4 * M_PI * a20 / (3 * A * R * R);
 }
 
+// the "Density Functional contributions" table of Output::shellsToFile
+// (output.cpp:205-236), in the order of ncgm_hf_outputs.terms
+static void energyTable(const Grid &g, const ncgm_hf_config &cfg,
+                        const State &st, double *t) {
+  const std::size_t ns = g.ns();
+  const ncgm_edf &P = cfg.edf;
+  Vec f[14];
+  for (auto &v : f) v.assign(ns, 0.0);
+  for (std::size_t i = 0; i < ns; ++i) {
+    const double r0 = st.rhoN[i] + st.rhoP[i], r1 = st.rhoN[i] - st.rhoP[i];
+    const double t0 = st.tauN[i] + st.tauP[i], t1 = st.tauN[i] - st.tauP[i];
+    const double l0 = st.n2N[i] + st.n2P[i], l1 = st.n2N[i] - st.n2P[i];
+    const double rs = std::pow(r0, P.sigma);
+    double j0 = 0, j1 = 0;
+    for (int a = 0; a < 3; ++a) {
+      const double s0 = st.JvN[a * ns + i] + st.JvP[a * ns + i];
+      const double s1 = st.JvN[a * ns + i] - st.JvP[a * ns + i];
+      j0 += s0 * s0;
+      j1 += s1 * s1;
+    }
+    f[0][i] = 0.5 * kHbar * kHbar * st.tauN[i] / st.massCorr +
+              0.5 * kHbar * kHbar * st.tauP[i] / st.massCorr;
+    f[1][i] = (P.C0rr * 1.0 + P.C0Drr * rs) * (r0 * r0);
+    f[2][i] = (P.C1rr * 1.0 + P.C1Drr * rs) * (r1 * r1);
+    f[3][i] = P.C0rdr * (r0 * l0);
+    f[4][i] = P.C1rdr * (l1 * r1);
+    f[5][i] = P.C0rt * (t0 * r0);
+    f[6][i] = P.C1rt * (t1 * r1);
+    f[7][i] = P.C0nJ * ((st.divJN[i] + st.divJP[i]) * r0);
+    f[8][i] = P.C1nJ * ((st.divJN[i] - st.divJP[i]) * r1);
+    f[9][i] = P.C0J2 * j0;
+    f[10][i] = P.C1J2 * j1;
+    f[11][i] = cfg.use_coulomb ? st.rhoP[i] * st.UCDir[i] : 0.0;
+    f[12][i] = std::pow(st.rhoP[i], 4.0 / 3.0) * (-3.0 * kE2 / 4.0) *
+               std::pow(3.0 / M_PI, 1.0 / 3.0);
+    f[13][i] = -0.5 * P.sigma *
+               (P.C0Drr * std::pow(r0, P.sigma + 2) +
+                P.C1Drr * std::pow(r0, P.sigma) * (r1 * r1));
+  }
+  for (int q = 0; q < 11; ++q) t[q] = integral(g, f[q].data());
+  t[11] = cfg.use_coulomb ? 0.5 * integral(g, f[11].data()) : 0.0;
+  t[12] = epair(cfg, st, true);
+  t[13] = epair(cfg, st, false);
+  t[14] = cfg.use_coulomb ? integral(g, f[12].data()) : 0.0;
+  t[15] = integral(g, f[13].data());
+}
+
 int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
           double *spe_p, double *rho_n, double *rho_p, double *energies,
-          int verbose) {
+          int verbose, ncgm_hf_outputs *out) {
   double tStart = now();
   Grid g(cfg.n, cfg.box_size / 2.0);
   const int A = cfg.A, Z = cfg.Z, N = A - Z;
@@ -1318,6 +1366,22 @@ int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
     Eint = nE;
     EHF = nH;
   }
+  if (out) {
+    energyTable(g, cfg, st, out->terms);
+    {
+      Vec rho(g.ns());
+      for (std::size_t i = 0; i < g.ns(); ++i) rho[i] = st.rhoN[i] + st.rhoP[i];
+      double ce = 0;
+      for (auto &c : cons) ce += constraintEvaluate(g, c, rho);
+      out->constraints_energy = ce;
+    }
+    if (out->orbitals_n)
+      std::memcpy(out->orbitals_n, n.X.d.data(), sizeof(cd) * n.X.d.size());
+    if (out->orbitals_p)
+      std::memcpy(out->orbitals_p, p.X.d.data(), sizeof(cd) * p.X.d.size());
+    if (out->U_n) std::copy(st.UN.begin(), st.UN.end(), out->U_n);
+    if (out->U_p) std::copy(st.UP.begin(), st.UP.end(), out->U_p);
+  }
   // Output::shellsToFile: tau, J and the Laplacian of rho recomputed with
   // the Lagrange-mesh derivatives from the final orbitals, then E_INT again
   // ("EintLag", src/system/output.cpp:252-256; iteration_data.cpp:346-382).
@@ -1335,6 +1399,18 @@ int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
     L.n2N = lapLagrangeNoSpin(g, st.rhoN);
     L.n2P = lapLagrangeNoSpin(g, st.rhoP);
     res.E_int_lagrange = kineticEnergy(g, L) + totalEnergyIntegral(g, cfg, L);
+    if (out) {
+      if (out->tau_n) std::copy(L.tauN.begin(), L.tauN.end(), out->tau_n);
+      if (out->tau_p) std::copy(L.tauP.begin(), L.tauP.end(), out->tau_p);
+      if (out->grad_rho_n) {
+        const Vec gN = gradLagrangeNoSpin(g, st.rhoN);
+        std::copy(gN.begin(), gN.end(), out->grad_rho_n);
+      }
+      if (out->grad_rho_p) {
+        const Vec gP = gradLagrangeNoSpin(g, st.rhoP);
+        std::copy(gP.begin(), gP.end(), out->grad_rho_p);
+      }
+    }
   }
   res.iterations = it;
   res.converged = conv;

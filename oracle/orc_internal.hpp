@@ -67,6 +67,10 @@ std::vector<double> kineticDensityLagrange(const Grid &g, const CMat &psi);
 std::vector<double> soDensityLagrange(const Grid &g, const CMat &psi);
 std::vector<double> lapLagrangeNoSpin(const Grid &g,
                                       const std::vector<double> &v);
+std::vector<double> gradLagrangeNoSpin(const Grid &g,
+                                       const std::vector<double> &v);
+// Shell::l/j/mj/P quantities and <L.S> of one spinor
+void shellObservables(const Grid &g, const cd *psi, double obs[5]);
 void normalize(const Grid &g, CMat &psi);
 CMat timeReverse(const Grid &g, const CMat &psi);
 CMat TROrder(const Grid &g, const CMat &psi);
@@ -97,5 +101,5 @@ CMat hoGuess(const Grid &g, int nev, double b, double beta);
 namespace orc {
 int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
           double *spe_p, double *rho_n, double *rho_p, double *energies,
-          int verbose);
+          int verbose, ncgm_hf_outputs *out = nullptr);
 }

@@ -388,6 +388,131 @@ std::vector<double> lapLagrangeNoSpin(const Grid &g,
   return out;
 }
 
+// Operators::gradLagrangeNoSpin (differential_operators.cpp:156-194): D's
+// first index contracted with each axis, no sign change; n^3 x 3
+// column-major
+std::vector<double> gradLagrangeNoSpin(const Grid &g,
+                                       const std::vector<double> &v) {
+  const int n = g.n;
+  const std::vector<double> D = lagrangeD1(n, g.h);
+  const std::size_t ns = g.ns();
+  std::vector<double> out(3 * ns, 0.0);
+  for (std::size_t p = 0; p < ns; ++p) {
+    const int i = (int)(p % n), j = (int)((p / n) % n), k = (int)(p / ((std::size_t)n * n));
+    double gx = 0, gy = 0, gz = 0;
+    for (int s = 0; s < n; ++s) {
+      gx += D[(std::size_t)s * n + i] * v[g.idxNS(s, j, k)];
+      gy += D[(std::size_t)s * n + j] * v[g.idxNS(i, s, k)];
+      gz += D[(std::size_t)s * n + k] * v[g.idxNS(i, j, s)];
+    }
+    out[p] = gx;
+    out[ns + p] = gy;
+    out[2 * ns + p] = gz;
+  }
+  return out;
+}
+
+// ---------------------------------------------------------------------------
+// Shell observables (src/util/shell.cpp:22-51, angular_momentum.cpp)
+// ---------------------------------------------------------------------------
+
+// L_a psi = -i hbar (r x grad)_a psi for a = x, y, z (:206-267)
+static void angularL(const Grid &g, const cd *psi, std::vector<cd> L[3]) {
+  std::vector<cd> gr[3];
+  gradSpinor(g, psi, gr);
+  const cd mih(0.0, -kHbar);
+  for (int a = 0; a < 3; ++a) L[a].assign(g.N(), cd(0, 0));
+  for (int k = 0; k < g.n; ++k)
+    for (int j = 0; j < g.n; ++j)
+      for (int i = 0; i < g.n; ++i)
+        for (int s = 0; s < 2; ++s) {
+          const std::size_t r = g.idx(i, j, k, s);
+          const double x = g.xs[i], y = g.xs[j], z = g.xs[k];
+          L[0][r] = mih * (y * gr[2][r] - z * gr[1][r]);
+          L[1][r] = mih * (z * gr[0][r] - x * gr[2][r]);
+          L[2][r] = mih * (x * gr[1][r] - y * gr[0][r]);
+        }
+}
+
+// Operators::integral of a spinor-length complex vector (trapezoid weights
+// on both components, integral_operators.cpp:4-32)
+static cd integralSpinor(const Grid &g, const std::vector<cd> &f) {
+  const double hhh = g.h * g.h * g.h;
+  cd acc(0, 0);
+  for (int k = 0; k < g.n; ++k)
+    for (int j = 0; j < g.n; ++j)
+      for (int i = 0; i < g.n; ++i)
+        for (int s = 0; s < 2; ++s) {
+          double w = 1.0;
+          if (i == 0 || i == g.n - 1) w *= 0.5;
+          if (j == 0 || j == g.n - 1) w *= 0.5;
+          if (k == 0 || k == g.n - 1) w *= 0.5;
+          acc += f[g.idx(i, j, k, s)] * hhh * w;
+        }
+  return acc;
+}
+
+// obs = [Re int psi conj(L^2 psi), Re int psi conj(J^2 psi),
+//        Re int psi conj(Jz Jz psi), Re psi(-r)^* . psi, Re int psi conj(LS psi)]
+void shellObservables(const Grid &g, const cd *psi, double obs[5]) {
+  const std::size_t N = g.N();
+  std::vector<cd> L[3], LL[3];
+  angularL(g, psi, L);
+  std::vector<cd> L2(N, cd(0, 0));
+  for (int a = 0; a < 3; ++a) {
+    angularL(g, L[a].data(), LL);
+    for (std::size_t r = 0; r < N; ++r) L2[r] += LL[a][r];
+  }
+  // S_z = hbar/2 sigma_z; J_z = L_z + S_z (:185-205, 269-272)
+  std::vector<cd> Jz(N), JJ(N);
+  for (std::size_t r = 0; r < N; ++r)
+    Jz[r] = L[2][r] + ((r % 2 == 0) ? 0.5 : -0.5) * kHbar * psi[r];
+  angularL(g, Jz.data(), LL);
+  for (std::size_t r = 0; r < N; ++r)
+    JJ[r] = LL[2][r] + ((r % 2 == 0) ? 0.5 : -0.5) * kHbar * Jz[r];
+  // L.S psi (:118-183): prefactor -i hbar^2 / 2 on (r x grad) without -i hbar
+  std::vector<cd> LS(N);
+  {
+    const cd I(0, 1), pref = -I * kHbar * kHbar * 0.5, mih(0.0, -kHbar);
+    for (std::size_t q = 0; q < g.ns(); ++q) {
+      // L[a] = -i hbar L'_a, so L'_a = L[a] / (-i hbar)
+      const cd lx0 = L[0][2 * q] / mih, ly0 = L[1][2 * q] / mih,
+               lz0 = L[2][2 * q] / mih;
+      const cd lx1 = L[0][2 * q + 1] / mih, ly1 = L[1][2 * q + 1] / mih,
+               lz1 = L[2][2 * q + 1] / mih;
+      LS[2 * q] = pref * (lz0 + (lx1 - I * ly1));
+      LS[2 * q + 1] = pref * ((lx0 + I * ly0) - lz1);
+    }
+  }
+  std::vector<cd> f(N);
+  auto expect = [&](const std::vector<cd> &Op) {
+    for (std::size_t r = 0; r < N; ++r) f[r] = psi[r] * std::conj(Op[r]);
+    return integralSpinor(g, f).real();
+  };
+  double nrm = 0;
+  {
+    for (std::size_t r = 0; r < N; ++r) f[r] = psi[r] * std::conj(psi[r]);
+    nrm = integralSpinor(g, f).real();
+  }
+  const double l2 = expect(L2), jj = expect(JJ);
+  double ls = 0;
+  for (std::size_t r = 0; r < N; ++r) f[r] = LS[r] * std::conj(psi[r]);
+  ls = integralSpinor(g, f).real();
+  // P psi(r) = psi(-r) (common_operators.cpp:4-22); par.dot(psi)
+  cd par(0, 0);
+  for (int k = 0; k < g.n; ++k)
+    for (int j = 0; j < g.n; ++j)
+      for (int i = 0; i < g.n; ++i)
+        for (int s = 0; s < 2; ++s)
+          par += std::conj(psi[g.idx(g.n - 1 - i, g.n - 1 - j, g.n - 1 - k, s)]) *
+                 psi[g.idx(i, j, k, s)];
+  obs[0] = l2;
+  obs[1] = l2 + 0.75 * kHbar * kHbar * nrm + 2.0 * ls;
+  obs[2] = jj;
+  obs[3] = par.real();
+  obs[4] = ls;
+}
+
 // Wavefunction::normalize (wavefunction.cpp:362-370)
 void normalize(const Grid &g, CMat &psi) {
   std::vector<double> rho(g.ns());

@@ -107,8 +107,24 @@ FP_CG_TOL = 1e-8
 
 
 def test_o16_hf_fp64_fixed_point():
-    _, rg, og, ro, oo = _run_both(O16, cg_tol=FP_CG_TOL)
+    """Also the output step's arrays (ncgm_hf_run_ex against the oracle's
+    restatement): the energy table, the mean fields, the recomputed kinetic
+    densities and the Lagrange-mesh gradients of rho."""
+    cfg = config.from_input(O16)
+    cfg.hf_gcg.cg_tol = FP_CG_TOL
+    rg, og = ng.hf_run(cfg, outputs=True)
+    ro, oo = oracle.hf_run_ex(cfg)
     _fixed_point(rg, og, ro, oo)
+    dT = np.abs(og["terms"] - oo["terms"]).max()
+    dC = abs(og["constraints_energy"] - oo["constraints_energy"])
+    rel = {}
+    for k in ("U_n", "U_p", "tau_n", "tau_p", "grad_rho_n", "grad_rho_p"):
+        rel[k] = np.abs(og[k] - oo[k]).max() / np.abs(oo[k]).max()
+    print("output step: max |d term| %.3e MeV, constraints %.1e, relative "
+          "array differences %s" % (dT, dC, {k: "%.1e" % v
+                                             for k, v in rel.items()}))
+    assert dT < E_TOL and dC < E_TOL
+    assert max(rel.values()) < 1e-5
 
 
 def test_o16_hf_mixed_precision_fixed_point():

@@ -299,3 +299,28 @@ def test_lagrange_densities_from_the_gradient():
                     (P.conj() * (G @ sig[nu].T)).sum(axis=1))
     assert np.abs(tau - tw).max() < 1e-12 * np.abs(tw).max()
     assert np.abs(J9 - Jw).max() < 1e-12 * np.abs(Jw).max()
+
+
+def test_shell_observables_of_a_p3half_state():
+    """(x + iy) exp(-r^2 / 2b^2) spin up is l = 1, j = 3/2, mj = 3/2, odd:
+    <L^2> = 2 hbar^2, <J^2> = 15/4 hbar^2, <Jz Jz> = 9/4 hbar^2,
+    <L.S> = hbar^2 / 2 (finite-difference operators on a 25^3 lattice)."""
+    import math
+    n, a = 25, 7.2
+    h = 2 * a / (n - 1)
+    xs = -a + np.arange(n) * h
+    Z, Y, X = np.meshgrid(xs, xs, xs, indexing="ij")
+    b = 1.7
+    psi = np.zeros(2 * n ** 3, np.complex128)
+    psi[0::2] = ((X + 1j * Y) * np.exp(-(X ** 2 + Y ** 2 + Z ** 2) /
+                                       (2 * b * b))).ravel()
+    psi /= math.sqrt(oracle.integral(n, a, np.abs(psi[0::2]) ** 2))
+    L2, J2, JJ, par, LS = oracle.shell_observables(n, a, psi)[0]
+    hb2 = 197.327053 ** 2
+    assert abs(L2 / hb2 - 2.0) < 1e-3
+    assert abs(J2 / hb2 - 3.75) < 1e-3
+    assert abs(JJ / hb2 - 2.25) < 1e-3
+    assert abs(LS / hb2 - 0.5) < 1e-3
+    assert par < 0
+    from nuclearcgm_gb300 import output
+    assert output.classify([[L2, J2, JJ, par, LS]])[0][:3] == (1.0, 1.5, 1.5)
