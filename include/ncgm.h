@@ -224,6 +224,8 @@ typedef struct ncgm_pairing {
 #define NCGM_PAIRING_HFB 1
 #define NCGM_PAIRING_BCS 2
 
+#define NCGM_MAX_MULTIPOLE 8
+
 typedef struct ncgm_hf_config {
   int n;               /* axisMeshPoints */
   double box_size;     /* boxSize (a = box_size / 2) */
@@ -253,6 +255,13 @@ typedef struct ncgm_hf_config {
   /* learned preconditioner (no reference counterpart; NULL / 0 = off) */
   ncgm_lp *lp;          /* network used when hf_gcg.precond = LEARNED */
   int lp_collect_every; /* > 0: log training pairs every k-th HF iteration */
+  /* general multipole constraints, the input's "constraints" list of
+   * {l, m, target} (input_parser.cpp:189-196): MultipoleConstraint on
+   * X_lm r^l (src/skyrme/multipole_constraint.cpp:7-56), added from HF
+   * iteration 1 (main.cpp:201-207) */
+  int n_multipole;
+  int mp_l[NCGM_MAX_MULTIPOLE], mp_m[NCGM_MAX_MULTIPOLE];
+  double mp_target[NCGM_MAX_MULTIPOLE];
 } ncgm_hf_config;
 
 typedef struct ncgm_hf_result {

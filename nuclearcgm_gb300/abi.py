@@ -44,6 +44,9 @@ class Pairing(C.Structure):
                 ("active", C.c_int)]
 
 
+MAX_MULTIPOLE = 8  # NCGM_MAX_MULTIPOLE
+
+
 class HFConfig(C.Structure):
     _fields_ = [
         ("n", C.c_int), ("box_size", C.c_double), ("A", C.c_int),
@@ -59,7 +62,9 @@ class HFConfig(C.Structure):
         ("constrain_com", C.c_int), ("curve_mode", C.c_int),
         ("mu20", C.c_double), ("constraints_tol", C.c_double),
         ("spe_tol", C.c_double), ("lp", C.c_void_p),
-        ("lp_collect_every", C.c_int)]
+        ("lp_collect_every", C.c_int), ("n_multipole", C.c_int),
+        ("mp_l", C.c_int * MAX_MULTIPOLE), ("mp_m", C.c_int * MAX_MULTIPOLE),
+        ("mp_target", C.c_double * MAX_MULTIPOLE)]
 
 
 class HFResult(C.Structure):

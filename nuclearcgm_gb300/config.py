@@ -108,6 +108,17 @@ def from_input(data: dict, functional: dict | None = None,
     cfg.use_coulomb = int(data.get("coulombInteraction", True))
     cfg.start_hfb_iter = int(data.get("startHFBIter", 3))
     cfg.constrain_com = int(data.get("constrainCOM", False))
+    # "constraints": [{"l", "m", "target"}] (input_parser.cpp:189-196)
+    mps = data.get("constraints", [])
+    if len(mps) > abi.MAX_MULTIPOLE:
+        raise ValueError("at most %d multipole constraints" % abi.MAX_MULTIPOLE)
+    cfg.n_multipole = len(mps)
+    for i, c in enumerate(mps):
+        l, m = int(c["l"]), int(c["m"])
+        if l < 0 or l > 9 or abs(m) > l:
+            raise ValueError("multipole constraint needs 0 <= l <= 9, |m| <= l")
+        cfg.mp_l[i], cfg.mp_m[i] = l, m
+        cfg.mp_target[i] = float(c["target"])
     cfg.constraints_tol = float(data.get("constraintsTol", 1e-3))
     cfg.pairing_threshold = float(data.get("pairingThreshold", 1e-3))
     cfg.density_mix = float(data.get("densityMix", 0.25))

@@ -46,7 +46,60 @@ double now() {
 }
 
 // constraint operators O(r) (xcm/ycm/zcm, x^2-y^2, 2xy, r^3 Y30, Q20)
+// SphericalHarmonics::Y (spherical_harmonics.cpp:14-99): associated
+// Legendre by the upward recurrence (no Condon-Shortley sign inside), the
+// (-1)^|m| factor and e^{i |m| phi}, conjugated with (-1)^|m| for m < 0
+__device__ double2 ylmDev(int l, int m, double theta, double phi) {
+  const int mm = m < 0 ? -m : m;
+  double fl = 1.0, fh = 1.0;
+  for (int i = 2; i <= l - mm; ++i) fl *= i;
+  for (int i = 2; i <= l + mm; ++i) fh *= i;
+  const double norm = sqrt(((2.0 * l + 1.0) / (4.0 * M_PI)) * (fl / fh));
+  const double x = cos(theta);
+  double pmm = 1.0;
+  if (mm > 0) {
+    double fact = 1.0;
+    for (int i = 1; i <= 2 * mm - 1; i += 2) fact *= i;
+    pmm = fact * pow(1.0 - x * x, mm / 2.0);
+  }
+  double leg = pmm;
+  if (l > mm) {
+    double p1 = x * (2 * mm + 1) * pmm, p2 = pmm;
+    leg = p1;
+    for (int ll = mm + 2; ll <= l; ++ll) {
+      const double pll = ((2 * ll - 1) * x * p1 - (ll + mm - 1) * p2) / (ll - mm);
+      p2 = p1;
+      p1 = pll;
+      leg = pll;
+    }
+  }
+  const double sgn = (mm % 2) ? -1.0 : 1.0;
+  const double re = sgn * norm * leg * cos(mm * phi),
+               im = sgn * norm * leg * sin(mm * phi);
+  return m < 0 ? make_double2(sgn * re, -sgn * im) : make_double2(re, im);
+}
+
+// MultipoleConstraint's operator X_lm r^l (multipole_constraint.cpp:24-27):
+// X_lm = sqrt2 Re Y_l,-m (m > 0), sqrt2 Im Y_lm (m < 0), Re Y_l0
+// (spherical_harmonics.cpp:45-58); NaN at the origin, as acos(0/0)
+__device__ double multipoleOp(int l, int m, double x, double y, double z) {
+  const double r = sqrt(x * x + y * y + z * z);
+  const double theta = acos(z / r), phi = atan2(y, x);
+  double X;
+  if (m > 0) X = 2.0 * ylmDev(l, -m, theta, phi).x / sqrt(2.0);
+  else if (m < 0) X = 2.0 * ylmDev(l, m, theta, phi).y / sqrt(2.0);
+  else X = ylmDev(l, 0, theta, phi).x;
+  return X * pow(fabs(r), (double)l);
+}
+
+// multipole constraints carry kind = kMultipoleKind + 100 l + (m + 50)
+constexpr int kMultipoleKind = 1000;
+
 __device__ double constraintOp(int kind, double x, double y, double z) {
+  if (kind >= kMultipoleKind) {
+    const int lm = kind - kMultipoleKind;
+    return multipoleOp(lm / 100, lm % 100 - 50, x, y, z);
+  }
   switch (kind) {
   case 0: return x;
   case 1: return y;
@@ -125,7 +178,7 @@ struct Constraint {
   bool first = true;
   double error() const {
     if (kind <= 2) return 0.0; // COM constraints (xcm_constraint.cpp:13)
-    double t = (kind == 6) ? target : 0.0;
+    double t = (kind == 6 || kind >= kMultipoleKind) ? target : 0.0;
     if (std::abs(t) <= 1e-12) return std::abs(value);
     return std::abs(value / t - 1.0);
   }
@@ -747,7 +800,13 @@ int updateQuantities(Run &R, int iter) {
       for (int b = 0; b < nblk; ++b) Q += part[(size_t)c * nblk + b];
       Constraint &k = R.cons[c];
       double m;
-      if (k.first) {
+      if (k.kind >= kMultipoleKind) {
+        // MultipoleConstraint::getField (multipole_constraint.cpp:18-40):
+        // the multiplier moves every iteration
+        k.lambda += k.gamma * 2.0 * k.C * (Q - k.target);
+        m = k.target - k.lambda / (2.0 * k.C);
+        k.value = Q;
+      } else if (k.first) {
         k.first = false;
         m = (k.kind == 6) ? k.target - k.lambda / (2.0 * k.C) : k.target;
       } else {
@@ -1080,6 +1139,44 @@ std::vector<int4> hoOrbitals(int nev) {
   return orbs;
 }
 
+// main.cpp:201-207: at HF iteration 1 each "constraints" entry becomes a
+// MultipoleConstraint. Its constructor (multipole_constraint.cpp:7-16)
+// evaluates C (Q - target)^2 with C = 1 on the current densities and sets
+// C = 0.01 / that value.
+int addMultipoles(Run &R) {
+  const ncgm_hf_config &C = R.cfg;
+  const int nm = std::min(C.n_multipole, NCGM_MAX_MULTIPOLE);
+  std::vector<int> kinds(nm);
+  for (int i = 0; i < nm; ++i) {
+    if (C.mp_l[i] < 0 || C.mp_l[i] > 9 || std::abs(C.mp_m[i]) > C.mp_l[i]) {
+      setError("hf: multipole constraint needs 0 <= l <= 9, |m| <= l");
+      return NCGM_ERR_ARG;
+    }
+    kinds[i] = kMultipoleKind + 100 * C.mp_l[i] + (C.mp_m[i] + 50);
+  }
+  const int nblk = 120;
+  cudaMemcpyAsync(R.ismall, kinds.data(), sizeof(int) * nm,
+                  cudaMemcpyHostToDevice, R.s);
+  constraintQ<<<nblk, 256, 0, R.s>>>(R.rho[0], R.rho[1], R.n, R.a, R.h,
+                                     R.ismall, nm, R.small);
+  std::vector<double> part((size_t)nm * nblk);
+  cudaMemcpyAsync(part.data(), R.small, sizeof(double) * nm * nblk,
+                  cudaMemcpyDeviceToHost, R.s);
+  NCGM_TRY(sync(R));
+  for (int i = 0; i < nm; ++i) {
+    double Q = 0;
+    for (int b = 0; b < nblk; ++b) Q += part[(size_t)i * nblk + b];
+    Constraint c;
+    c.kind = kinds[i];
+    c.target = C.mp_target[i];
+    c.gamma = 0.3;
+    c.C = 0.01 / std::pow(Q - c.target, 2);
+    c.first = false;
+    R.cons.push_back(c);
+  }
+  return NCGM_OK;
+}
+
 int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
           double *spe_p, double *rho_n, double *rho_p, double *energiesOut,
           ncgm_hf_outputs *out) {
@@ -1209,6 +1306,7 @@ int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
   bool conv = false;
   ncgm_gcg_params hp = cfg.hf_gcg;
   for (it = 0; it < cfg.max_iterations; ++it) {
+    if (it == 1 && cfg.n_multipole > 0) NCGM_TRY(addMultipoles(R));
     NCGM_TRY(updateQuantities(R, it));
     NCGM_TRY(buildCoefficients(R.ctx, 0, R.f[0], R.gf[0], R.U[0],
                                cfg.spin_orbit ? R.W[0] : nullptr, nullptr));

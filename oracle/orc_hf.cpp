@@ -604,7 +604,7 @@ struct Constraint {
   // target, which those classes never set; it is taken as 0.
   double error() const {
     if (kind <= 2) return 0.0;
-    double t = (kind == 6) ? target : 0.0;
+    double t = (kind == 6 || kind >= 1000) ? target : 0.0;
     if (std::abs(t) <= 1e-12) return std::abs(value);
     return std::abs(value / t - 1.0);
   }
@@ -669,7 +669,12 @@ static Vec constraintField(const Grid &g, Constraint &c, const Vec &rho,
                            double energyDiff) {
   double Q = qValue(g, c, rho);
   double mu;
-  if (c.firstIter) {
+  if (c.kind >= 1000) {
+    // MultipoleConstraint::getField (multipole_constraint.cpp:18-40)
+    c.lambda += c.gamma * 2.0 * c.C * (Q - c.target);
+    mu = c.target - c.lambda / (2.0 * c.C);
+    c.value = Q;
+  } else if (c.firstIter) {
     c.firstIter = false;
     mu = (c.kind == 6) ? c.target - c.lambda / (2.0 * c.C) : c.target;
   } else {
@@ -720,6 +725,31 @@ static cd Ylm(int l, int m, double theta, double phi) {
   cd res = std::pow(-1.0, mm) * norm * leg * phase;
   if (m < 0) return std::pow(-1.0, mm) * std::conj(res);
   return res;
+}
+
+// MultipoleConstraint's operator X_lm r^l (multipole_constraint.cpp:24-27)
+// with SphericalHarmonics::X (spherical_harmonics.cpp:45-58)
+static Vec multipoleOperator(const Grid &g, int l, int m) {
+  Vec O(g.ns());
+  for (int k = 0; k < g.n; ++k)
+    for (int j = 0; j < g.n; ++j)
+      for (int i = 0; i < g.n; ++i) {
+        const double x = g.xs[i], y = g.xs[j], z = g.xs[k];
+        const double r = std::sqrt(x * x + y * y + z * z);
+        const double th = std::acos(z / r), ph = std::atan2(y, x);
+        double X;
+        if (m > 0) {
+          const cd Y = Ylm(l, -m, th, ph);
+          X = (Y + std::conj(Y)).real() / std::sqrt(2.0);
+        } else if (m < 0) {
+          const cd Y = Ylm(l, m, th, ph);
+          X = (cd(0, -1) * (Y - std::conj(Y))).real() / std::sqrt(2.0);
+        } else {
+          X = Ylm(l, 0, th, ph).real();
+        }
+        O[g.idxNS(i, j, k)] = X * std::pow(std::abs(r), (double)l);
+      }
+  return O;
 }
 
 CMat hoGuess(const Grid &g, int nev, double omega, double /*beta*/) {
@@ -1288,6 +1318,25 @@ int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
   bool conv = false;
   double lastdE = 0;
   for (it = 0; it < cfg.max_iterations; ++it) {
+    if (it == 1) {
+      // main.cpp:201-207: the input's multipole constraints join at HF
+      // iteration 1; C = 0.01 / (Q - target)^2 on the current densities
+      // (MultipoleConstraint constructor, multipole_constraint.cpp:7-16)
+      Vec rho(g.ns());
+      for (std::size_t i = 0; i < g.ns(); ++i) rho[i] = st.rhoN[i] + st.rhoP[i];
+      for (int q = 0; q < cfg.n_multipole && q < NCGM_MAX_MULTIPOLE; ++q) {
+        Constraint c;
+        c.kind = 1000 + 100 * cfg.mp_l[q] + (cfg.mp_m[q] + 50);
+        c.target = cfg.mp_target[q];
+        c.gamma = 0.3;
+        c.firstIter = false;
+        c.O = multipoleOperator(g, cfg.mp_l[q], cfg.mp_m[q]);
+        c.C = 1.0;
+        const double Q = qValue(g, c, rho);
+        c.C = 0.01 / (c.C * std::pow(Q - c.target, 2));
+        cons.push_back(c);
+      }
+    }
     updateQuantities(g, cfg, st, n, p, it, cons, pt);
     double t0 = now();
     Csr hN = buildSkyrme(g, st.fN.data(), st.gfN.data(), st.UN.data(),

@@ -48,3 +48,21 @@ def test_curve_points_match_mu20_from_beta():
     import math
     R = 1.2 * 24 ** (1 / 3)
     assert pts[0][1] == pytest.approx(-0.3 * 3 * 24 * R * R / 4 / math.pi)
+
+
+def test_multipole_constraints_parsed():
+    from nuclearcgm_gb300 import abi, config
+    data = {"functional": "SLy4", "nucleus": {"A": 16, "Z": 8},
+            "box": {"boxSize": 16.0, "axisMeshPoints": 12},
+            "maxIterations": 10, "energyTol": 1e-3,
+            "constraints": [{"l": 2, "m": 0, "target": 20.0},
+                            {"l": 3, "m": -2, "target": 1.5}]}
+    cfg = config.from_input(data)
+    assert cfg.n_multipole == 2
+    assert (cfg.mp_l[0], cfg.mp_m[0], cfg.mp_target[0]) == (2, 0, 20.0)
+    assert (cfg.mp_l[1], cfg.mp_m[1], cfg.mp_target[1]) == (3, -2, 1.5)
+    import pytest
+    with pytest.raises(ValueError):
+        config.from_input(dict(data, constraints=[{"l": 1, "m": 2,
+                                                   "target": 0.0}]))
+    assert abi.MAX_MULTIPOLE == 8

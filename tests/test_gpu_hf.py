@@ -247,3 +247,26 @@ def test_concurrent_species_match_serial(precision, monkeypatch):
     assert np.array_equal(o_c["spe_n"], o_s["spe_n"])
     assert np.array_equal(o_c["spe_p"], o_s["spe_p"])
     assert np.array_equal(o_c["rho_p"], o_s["rho_p"])
+
+
+@pytest.mark.parametrize("l,m,target", [(2, 0, 3.0), (2, 2, 1.0)])
+def test_multipole_constraint_fixed_point(l, m, target):
+    """A general multipole constraint from the input's "constraints" list
+    (MultipoleConstraint on X_lm r^l, joining at HF iteration 1): the
+    constrained 16O fixed point against the oracle's."""
+    data = {"functional": "SKMstar", "nucleus": {"A": 16, "Z": 8},
+            "box": {"boxSize": 16.5, "axisMeshPoints": 12},
+            "maxIterations": 300, "energyTol": 1e-7,
+            "constraints": [{"l": l, "m": m, "target": target}]}
+    cfg = config.from_input(data)
+    cfg.hf_gcg.cg_tol = FP_CG_TOL
+    rg, og = ng.hf_run(cfg, outputs=True)
+    ro, oo = oracle.hf_run_ex(cfg)
+    print("l %d m %d: E_HF %.6f / %.6f, constraints energy %.3e / %.3e, "
+          "iterations %d / %d" % (l, m, rg.E_HF, ro.E_HF,
+                                  og["constraints_energy"],
+                                  oo["constraints_energy"], rg.iterations,
+                                  ro.iterations))
+    assert abs(rg.E_int - ro.E_int) < E_TOL
+    assert abs(rg.E_HF - ro.E_HF) < E_TOL
+    assert abs(og["constraints_energy"] - oo["constraints_energy"]) < E_TOL

@@ -324,3 +324,21 @@ def test_shell_observables_of_a_p3half_state():
     assert par < 0
     from nuclearcgm_gb300 import output
     assert output.classify([[L2, J2, JJ, par, LS]])[0][:3] == (1.0, 1.5, 1.5)
+
+
+def test_multipole_constraint_joins_at_iteration_one():
+    """A general multipole constraint (MultipoleConstraint) is added at HF
+    iteration 1: iteration 0 is unchanged; from iteration 1 E_HF carries the
+    constraint energy C (Q - target)^2 + lambda (Q - target), about
+    0.01 MeV at first (C = 0.01 / (Q - target)^2)."""
+    from nuclearcgm_gb300 import config
+    data = {"functional": "SLy4", "nucleus": {"A": 16, "Z": 8},
+            "box": {"boxSize": 14.0, "axisMeshPoints": 10},
+            "maxIterations": 3, "energyTol": 0.0}
+    r0, o0 = oracle.hf_run(config.from_input(data))
+    r1, o1 = oracle.hf_run(config.from_input(
+        dict(data, constraints=[{"l": 2, "m": 0, "target": 25.0}])))
+    assert np.array_equal(o0["energies"][0], o1["energies"][0])
+    assert np.all(np.isfinite(o1["energies"]))
+    d = abs(o1["energies"][1, 1] - o0["energies"][1, 1])
+    assert 1e-3 < d < 0.1
