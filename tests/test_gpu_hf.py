@@ -192,6 +192,8 @@ def test_o16_bcs_fixed_point():
     assert abs(rg.E_int - ro.E_int) < E_TOL
     assert abs(rg.E_HF - ro.E_HF) < E_TOL
     assert abs(rg.E_pair_n - ro.E_pair_n) < E_TOL
+    # the Lagrange-mesh recompute with BCS occupations (sqrt(v^2) scaling)
+    assert abs(rg.E_int_lagrange - ro.E_int_lagrange) < E_TOL
     assert abs(rg.lambda_n - ro.lambda_n) < 1e-4
     assert np.abs(og["spe_n"] - oo["spe_n"]).max() < 1e-4
     assert np.abs(og["rho_n"] - oo["rho_n"]).max() < 1e-6
@@ -213,6 +215,8 @@ def test_o16_hfb_fixed_point():
              ro.lambda_n))
     assert rg.last_dE < 1e-4 and ro.last_dE < 1e-4
     assert abs(rg.E_int - ro.E_int) < E_TOL
+    # the Lagrange-mesh recompute on the HFB natural orbitals
+    assert abs(rg.E_int_lagrange - ro.E_int_lagrange) < E_TOL
     # E_HF is not compared: HFEnergy adds the BCS quasiparticle sums
     # (iteration_data.cpp:212-224, bcsN.qpEnergies), which the HFB branch
     # stops updating after iteration startHFBIter - 1, so E_HF keeps the
