@@ -1326,15 +1326,27 @@ int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
     if (twoSpecies && R.ctxP) {
       int stP = NCGM_OK;
       std::string errP;
+      // exceptions stay on their own thread: the proton thread turns them
+      // into a status, and the main thread joins before rethrowing
       std::thread protons([&] {
-        cudaSetDevice(R.ctx->device);
-        stP = gcgRun(R.ctxP, 1, Sp.X, orbP, Sp.cdCols ? Sp.CD : nullptr,
-                     Sp.cdCols, orbP, hp, Sp.Xn, lamP.data(), nullptr);
-        if (stP != NCGM_OK) errP = ncgm_last_error();
+        try {
+          cudaSetDevice(R.ctx->device);
+          stP = gcgRun(R.ctxP, 1, Sp.X, orbP, Sp.cdCols ? Sp.CD : nullptr,
+                       Sp.cdCols, orbP, hp, Sp.Xn, lamP.data(), nullptr);
+          if (stP != NCGM_OK) errP = ncgm_last_error();
+        } catch (const std::exception &e) {
+          stP = NCGM_ERR_ARG;
+          errP = std::string("hf (protons): ") + e.what();
+        }
       });
-      const int stN =
-          gcgRun(R.ctx, 0, Sn.X, orbN, Sn.cdCols ? Sn.CD : nullptr,
-                 Sn.cdCols, orbN, hp, Sn.Xn, lamN.data(), nullptr);
+      int stN = NCGM_OK;
+      try {
+        stN = gcgRun(R.ctx, 0, Sn.X, orbN, Sn.cdCols ? Sn.CD : nullptr,
+                     Sn.cdCols, orbN, hp, Sn.Xn, lamN.data(), nullptr);
+      } catch (...) {
+        protons.join();
+        throw;
+      }
       protons.join();
       if (stN != NCGM_OK) return stN;
       if (stP != NCGM_OK) {
