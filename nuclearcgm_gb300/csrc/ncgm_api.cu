@@ -3,6 +3,8 @@
 // lets a C++ exception cross the boundary.
 #include "ncgm_internal.cuh"
 
+#include <cstdlib>
+
 #include <algorithm>
 
 #include <cstring>
@@ -224,8 +226,14 @@ int ncgm_apply_h(ncgm_ctx *ctx, int species, const double *X, double *Y,
   // consecutive chunks overlap each other and the compute. Every column is
   // computed by the same kernels as in one launch (columns are independent),
   // so the results are identical.
+  // NCGM_PIPE_CHUNK_MB sets the chunk size (default 16 MB)
+  size_t chunkBytes = (size_t)16 << 20;
+  if (const char *e = std::getenv("NCGM_PIPE_CHUNK_MB")) {
+    const long v = std::atol(e);
+    if (v >= 1 && v <= 4096) chunkBytes = (size_t)v << 20;
+  }
   const int chunkCols = std::max<int>(
-      1, (int)std::min<size_t>(ncols, (size_t)(16u << 20) /
+      1, (int)std::min<size_t>(ncols, chunkBytes /
                                           (ctx->N * sizeof(double2))));
   if (!dX && !dY && ncols > chunkCols) {
     const int nch = (ncols + chunkCols - 1) / chunkCols;
