@@ -102,3 +102,31 @@ def test_localisation_bounded():
     g = rng.standard_normal((50, 3)) * 0.01
     C = output.localisation(tau, rho, g)
     assert np.all((C > 0) & (C <= 1))
+
+
+def test_spherical_harmonics_match_scipy():
+    """SphericalHarmonics::Y as the writer restates it equals the standard
+    Y_lm with the Condon-Shortley phase (scipy.special.sph_harm_y)."""
+    sp = pytest.importorskip("scipy.special")
+    if not hasattr(sp, "sph_harm_y"):
+        pytest.skip("scipy without sph_harm_y")
+    rng = np.random.default_rng(2)
+    X, Y, Z = rng.standard_normal((3, 40))
+    r = np.sqrt(X * X + Y * Y + Z * Z)
+    th, ph = np.arccos(Z / r), np.arctan2(Y, X)
+    for l in range(6):
+        for m in range(-l, l + 1):
+            ref = sp.sph_harm_y(l, m, th, ph)
+            assert np.abs(output.ylm(l, m, X, Y, Z) - ref).max() < 1e-13
+
+
+def test_monopole_is_particle_number_over_sqrt_4pi():
+    """Q(0, 0) = int rho Y_00 = A / sqrt(4 pi) for a density normalised to A
+    with the trapezoid rule (even n: no lattice point at the origin)."""
+    n, a = 12, 6.0
+    X, Y, Z, _ = output._coords(n, a)
+    rho = np.exp(-(X * X + Y * Y + Z * Z) / 4.0)
+    rho *= 16.0 / output.integral(rho, n, a)
+    q = output.multipole(0, 0, rho, n, a)
+    assert q.real == pytest.approx(16.0 / math.sqrt(4 * math.pi), rel=1e-12)
+    assert abs(q.imag) < 1e-12
