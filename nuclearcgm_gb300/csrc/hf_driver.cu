@@ -698,8 +698,13 @@ int occupiedOrbitals(Run &R, int q, bool bcsOcc, int &ncols,
     ncols = M;
     return NCGM_OK;
   }
-  Phi = S.X; // phi * nullOcc(N): columns == particle number
-  ncols = M;
+  // phi * nullOcc(particles) (iteration_data.cpp:290-294, 319-323): all
+  // columns without pairing (the basis is the particle number); the first
+  // `particles` columns when HFB pairing was switched off during the run,
+  // as the reference's release build (no size check) computes that product
+  const int particles = q == 0 ? R.cfg.A - R.cfg.Z : R.cfg.Z;
+  Phi = S.X;
+  ncols = std::min(M, std::max(particles, 0));
   return NCGM_OK;
 }
 

@@ -877,7 +877,18 @@ static CMat occupied(const Grid &g, const CMat &phi, const ncgm_hf_config &cfg,
     }
     return out;
   }
-  if (!p.active || cfg.pairing_type == NCGM_PAIRING_NONE) return phi;
+  if (!p.active || cfg.pairing_type == NCGM_PAIRING_NONE) {
+    // phi * nullOcc(particles).asDiagonal() (iteration_data.cpp:290-294,
+    // 319-323). When pairing was switched off during the run the basis is
+    // larger than the particle number; the reference's release build
+    // (-DNDEBUG, no size check) then keeps the first `particles` columns
+    const int particles = neutron ? cfg.A - cfg.Z : cfg.Z;
+    if ((int)phi.cols <= particles) return phi;
+    CMat out(phi.rows, particles);
+    for (int c = 0; c < particles; ++c)
+      for (std::size_t r = 0; r < phi.rows; ++r) out(r, c) = phi(r, c);
+    return out;
+  }
   if (cfg.pairing_type == NCGM_PAIRING_HFB) {
     const UV &h = neutron ? st.hfbN : st.hfbP;
     const int M = (int)h.V.rows;
