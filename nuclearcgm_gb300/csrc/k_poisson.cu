@@ -340,6 +340,27 @@ struct PoissonEigen {
 std::vector<PoissonEigen> g_peig;
 std::mutex g_peigMutex;
 
+// The dynamic shared-memory limit of axisTransformKernel is an attribute of
+// each device: it is raised once on every device that runs the fast solver.
+// False when it cannot be raised (the caller then solves with CG only).
+std::vector<int> g_axisAttrDevs;
+bool axisTransformReady() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  std::lock_guard<std::mutex> lock(g_peigMutex);
+  for (int d : g_axisAttrDevs)
+    if (d == dev) return true;
+  if (cudaFuncSetAttribute(axisTransformKernel,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (80 * 80 + 80) * (int)sizeof(double)) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  g_axisAttrDevs.push_back(dev);
+  return true;
+}
+
 const double *poissonEigen(int n, cudaStream_t s) {
   int dev = 0;
   cudaGetDevice(&dev);
@@ -414,15 +435,8 @@ int poissonSolve(const PoissonArgs &P, cudaStream_t s, int *iterations) {
   const char *fenv = std::getenv("NCGM_POISSON_FAST");
   const double *Wd = (fenv && fenv[0] == '0') ? nullptr : poissonEigen(n, s);
   bool solved = false;
-  if (Wd) {
+  if (Wd && axisTransformReady()) {
     const size_t smem = ((size_t)n * n + n) * sizeof(double);
-    static const bool attr = [] {
-      cudaFuncSetAttribute(axisTransformKernel,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (80 * 80 + 80) * (int)sizeof(double));
-      return true;
-    }();
-    (void)attr;
     const double hh = P.h * P.h;
     for (int ref = 0; ref < 4; ++ref) {
       double hs2[2];
@@ -439,9 +453,13 @@ int poissonSolve(const PoissonArgs &P, cudaStream_t s, int *iterations) {
       axisTransformKernel<<<nblk, 256, smem, s>>>(p, Ap, Wd, n, 0, 1, 0, hh, 0);
       axisTransformKernel<<<nblk, 256, smem, s>>>(Ap, p, Wd, n, 1, 1, 0, hh, 0);
       axisTransformKernel<<<nblk, 256, smem, s>>>(p, P.U, Wd, n, 2, 1, 0, hh, 1);
+      // a failed launch leaves U as it was (all six passes share one
+      // configuration): rebuild the residual from U and finish with CG
+      const bool launched = cudaGetLastError() == cudaSuccess;
       negLapKernel<<<nblk, 256, 0, s>>>(P.U, Ap, n, P.h, nullptr);
       cgInitKernel<<<nblk, 256, 0, s>>>(rhs, Ap, r, p, ns, part);
       cgScalarInit<<<1, 32, 0, s>>>(part, nblk, sc);
+      if (!launched) break;
       ++it;
     }
   }
@@ -527,6 +545,7 @@ static __device__ __align__(256) double g_poissonScratch[kNoAllocDoubles];
 
 constexpr int kMaxDevices = 64;
 double *g_scratchAddr[kMaxDevices] = {nullptr};
+std::mutex g_scratchMutex; // first calls on a device from several threads
 
 // device address of the static scratch on the current device (set-up on the
 // first call per device)
@@ -534,6 +553,7 @@ int staticScratch(double **out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return NCGM_ERR_CUDA;
   if (dev < 0 || dev >= kMaxDevices) return NCGM_ERR_ARG;
+  std::lock_guard<std::mutex> lock(g_scratchMutex);
   if (!g_scratchAddr[dev]) {
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_poissonScratch);
@@ -544,8 +564,11 @@ int staticScratch(double **out) {
   return NCGM_OK;
 }
 
-// Same sequence of kernels as poissonSolve, with the host-side reduction
-// buffers on the stack instead of the heap.
+// The CG path of poissonSolve (the separable-inverse refinement, which needs
+// the per-lattice eigenvectors in allocated memory, is not used), with the
+// host-side reduction buffers on the stack instead of the heap. Both stop at
+// the same 1e-13 relative residual, so their results agree to that level,
+// not bit for bit.
 int poissonSolveNoAlloc(const PoissonArgs &P, cudaStream_t s,
                         int *iterations) {
   const int n = P.n;

@@ -342,3 +342,29 @@ def test_multipole_constraint_joins_at_iteration_one():
     assert np.all(np.isfinite(o1["energies"]))
     d = abs(o1["energies"][1, 1] - o0["energies"][1, 1])
     assert 1e-3 < d < 0.1
+
+
+def test_hfb_switched_off_species_occupies_particle_number_states():
+    """After a species' HFB pairing energy drops to zero the run switches
+    its pairing off and occupies phi * nullOcc(particles)
+    (iteration_data.cpp:290-294, 319-323). With a basis larger than the
+    particle number (20 states for 8 nucleons here) the reference's release
+    build keeps the first `particles` columns: the densities must still
+    integrate to N and Z, not to the basis size."""
+    from nuclearcgm_gb300 import config
+    n, box = 10, 16.5
+    data = {"functional": "SKMstar", "nucleus": {"A": 16, "Z": 8},
+            "box": {"boxSize": box, "axisMeshPoints": n},
+            "pairing": {"type": "HFB", "HFbasisSize": 20, "V0": 100.0,
+                        "window": 5.0},
+            "maxIterations": 12, "energyTol": 0.0}
+    res, out = oracle.hf_run(config.from_input(data))
+    assert res.E_pair_n == 0.0 and res.E_pair_p == 0.0
+    h = box / (n - 1)
+    w = np.ones(n)
+    w[0] = w[-1] = 0.5
+    wt = (w[:, None, None] * w[None, :, None] * w[None, None, :]).ravel()
+    for q in ("rho_n", "rho_p"):
+        assert abs((out[q] * wt).sum() * h ** 3 - 8.0) < 1e-8
+    # the 20 basis states are all still solved for
+    assert out["spe_n"].shape == (20,) and np.all(np.diff(out["spe_n"]) >= 0)

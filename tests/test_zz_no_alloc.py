@@ -15,7 +15,10 @@ import nuclearcgm_gb300 as ng
 
 pytestmark = pytest.mark.gpu
 
-REL_TOL = 1e-12  # same kernels and reduction order: agreement to rounding
+# The allocating call is pinned to its CG path (NCGM_POISSON_FAST=0): both
+# entry points then run the same CG kernels in the same order from U = 0 to
+# the same 1e-13 relative residual, so they agree to rounding.
+REL_TOL = 1e-12
 
 
 def _rho(n, a, Z, w, zfac):
@@ -33,8 +36,9 @@ def _rho(n, a, Z, w, zfac):
     return rho * Z / (rho * wt.ravel()).sum() / h ** 3
 
 
-def test_noalloc_poisson_matches_allocating_call_twice():
+def test_noalloc_poisson_matches_allocating_call_twice(monkeypatch):
     torch = pytest.importorskip("torch")
+    monkeypatch.setenv("NCGM_POISSON_FAST", "0")
     lib = ng.load()
     n, a, Z = 24, 11.0, 20
     ctx = ng.Context(ng.Grid(n, a), 2)
