@@ -221,20 +221,14 @@ def _hf_wall(with_cpu):
         out["learned_mixed_gpu_s"] = None
         out["learned_note"] = "no trained weights (nuclearcgm_gb300.train_lp)"
     if with_cpu:
+        # the FP64 CPU oracle on the same input to the same stop rule, timed
         from oracle import oracle
-        from nuclearcgm_gb300 import config as cf
-        t = {}
-        for k in (1, 3):
-            c = cf.from_input(dict(O16_HF, maxIterations=k, energyTol=0.0))
-            t0 = time.perf_counter()
-            oracle.hf_run(c)
-            t[k] = time.perf_counter() - t0
-        per_it = (t[3] - t[1]) / 2
-        its = out["fp64_gpu_iterations"]
-        out["cpu_oracle_s_est"] = round(t[1] + per_it * (its - 1), 3)
-        out["cpu_sample"] = ("oracle HF runs of 1 and 3 iterations (%.2f s, "
-                             "%.2f s); estimate = 1-iteration run + %d x "
-                             "per-iteration time" % (t[1], t[3], its - 1))
+        c = config.from_input(O16_HF)
+        t0 = time.perf_counter()
+        ro, _ = oracle.hf_run(c)
+        out["cpu_oracle_s"] = round(time.perf_counter() - t0, 3)
+        out["cpu_oracle_iterations"] = ro.iterations
+        out["cpu_oracle_E_MeV"] = round(ro.E_HF, 6)
         out["cpu_cores"] = os.cpu_count()
     return out
 
@@ -273,6 +267,38 @@ def _gcg_step(H, X):
     return out
 
 
+# FP64 pipe instructions of the operator per point and column, counted from
+# its arithmetic (stencil_core.cuh pointH): 65 additions, 8 multiplications
+# and 56 FMAs (185 flops)
+FP64_OPS_PER_POINT_COL = 129
+FP64_FLOPS_PER_POINT_COL = 185
+
+
+def _fp64_roofline(lib, ms64):
+    """The FP64 stencil against the FP64 pipe: pipe instructions per second
+    of the apply over FMA instructions per second of the probe kernel
+    (ncgm_measure_fp64_gflops / 2); an addition or a multiplication takes a
+    pipe slot like an FMA."""
+    import ctypes
+    from nuclearcgm_gb300 import workloads
+    pts = N_LAT ** 3 * NCOLS
+    out = {"ms_per_hx": round(ms64, 4),
+           "gbs": round(workloads.hx_bytes(N_LAT, NCOLS, 8) /
+                        (ms64 * 1e-3) / 1e9, 2),
+           "gflops": round(pts * FP64_FLOPS_PER_POINT_COL / (ms64 * 1e-3) /
+                           1e9, 1)}
+    g = ctypes.c_double(0)
+    if lib.ncgm_measure_fp64_gflops(ctypes.byref(g)) == 0 and g.value > 0:
+        ops = pts * FP64_OPS_PER_POINT_COL / (ms64 * 1e-3) / 1e9
+        out["roofline"] = {"bound": "fp64 pipe", "achieved": round(ops, 1),
+                           "peak": round(g.value / 2, 1),
+                           "unit": "G FP64 instructions/s",
+                           "frac": round(ops / (g.value / 2), 4),
+                           "peak_source": "measured (ncgm_measure_fp64_"
+                                          "gflops: %.1f GFLOP/s)" % g.value}
+    return out
+
+
 def run_reference(args):
     ws, rank = _dist()
     if rank != 0:
@@ -280,7 +306,7 @@ def run_reference(args):
     a, f, gradf, U, W, X = _workload()
     cores = os.cpu_count()
     gbs, dt = _cpu_reference(args.steps, min(args.warmup, 2), a, f, gradf, U,
-                             W, X, 1)
+                             W, X, NCOLS)
     line = {
         "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s",
         "impl": "reference", "n_gpus": args.gpus, "steps": args.steps,
@@ -288,13 +314,14 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": "H.X 40^3 lattice, 64 complex 2-spinors, "
-                               "h=0.5 fm (step = 1 of 64 columns)",
-                   "global_batch": 1, "seq_len": 2 * N_LAT ** 3,
+                               "h=0.5 fm",
+                   "global_batch": NCOLS, "seq_len": 2 * N_LAT ** 3,
                    "parallelism": "host threads"},
         "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s",
                          "cores": cores, "kind": "port",
-                         "sample": "1 column of the 64-column block per step,"
-                                   " CSR assembled once (not timed)"},
+                         "sample": "the whole 64-column block per step (FP64 "
+                                   "CSR product), CSR assembled once (not "
+                                   "timed)"},
         "e2e": {"value": round(gbs, 3), "unit": "GB/s",
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -407,10 +434,11 @@ def run_ours(args):
         hf_ca = _hf_wall_ca40()
     cpu = None
     if rank == 0 and not args.no_cpu:
-        gbs_c, dt_c = _cpu_reference(3, 1, a, f, gradf, U, W, X, 4)
+        gbs_c, dt_c = _cpu_reference(3, 1, a, f, gradf, U, W, X, NCOLS)
         cpu = {"value": round(gbs_c, 3), "unit": "GB/s",
                "cores": os.cpu_count(), "kind": "port",
-               "sample": "4 of 64 columns, 3 timed products (FP64 CSR)"}
+               "sample": "the whole 64-column block, 3 timed products "
+                         "(FP64 CSR)"}
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "GB/s",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -432,9 +460,7 @@ def run_ours(args):
         "gpu_launches": args.steps,
         "clocks": clk.summary(),
         "fp32_rel_err_vs_fp64": rel32,
-        "fp64_stencil": {"ms_per_hx": round(ms64, 4),
-                         "gbs": round(workloads.hx_bytes(N_LAT, NCOLS, 8) /
-                                      (ms64 * 1e-3) / 1e9, 2)},
+        "fp64_stencil": _fp64_roofline(lib, ms64),
         "cpu_baseline": cpu,
         "hf_wall_to_1keV": hf,
         "hf_wall_to_1keV_ca40": hf_ca,

@@ -415,6 +415,14 @@ int ncgm_lp_eval(ncgm_lp *lp, int n, double *mean_loss);
 /* network used by ncgm_gcg with precond = NCGM_PRECOND_LEARNED */
 int ncgm_set_lp(ncgm_ctx *ctx, ncgm_lp *lp);
 
+/* ---- measurement ------------------------------------------------------- */
+
+/* FP64 FMA throughput of the current device in GFLOP/s (2 flops per FMA),
+ * timed with CUDA events over one launch of independent FMA chains: the
+ * compute ceiling the FP64 stencil is reported against. A measurement helper
+ * with no counterpart in the reference. */
+int ncgm_measure_fp64_gflops(double *gflops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -148,6 +148,7 @@ SIGNATURES = {
     "ncgm_lp_train": ([_vp, _i, _i, _d, C.c_ulonglong, _vp], _i),
     "ncgm_lp_eval": ([_vp, _i, _vp], _i),
     "ncgm_set_lp": ([_vp, _vp], _i),
+    "ncgm_measure_fp64_gflops": ([_vp], _i),
 }
 
 

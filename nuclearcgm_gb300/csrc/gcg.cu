@@ -181,10 +181,15 @@ static int cholQR2(ncgm_ctx *ctx, const double2 *V, int k, double2 *Q,
     else
       gram(src, N, cols, src, N, cols, N, G, cols, partials, maxChunks, s);
     cholDrop(G, cols, cols, 1e-24, R, T, dKeep, s);
-    if (cudaMemcpyAsync(keep.data(), dKeep, sizeof(int) * cols,
-                        cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
+    cudaError_t e = cudaMemcpyAsync(keep.data(), dKeep, sizeof(int) * cols,
+                                    cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      setError(std::string("ncgm_gcg: orthonormalisation pass ") +
+               std::to_string(pass) + " of " + std::to_string(k) +
+               " columns: " + cudaGetErrorString(e));
       return -1;
+    }
     idx.clear();
     for (int j = 0; j < cols; ++j)
       if (keep[j]) idx.push_back(j);

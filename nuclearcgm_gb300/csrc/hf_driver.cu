@@ -197,10 +197,27 @@ struct BCSRes {
   std::vector<double> u2, v2, Delta, qp;
   double lambda = 0, Epair = 0;
 };
+// HFB amplitudes of one species on the device (M x M, col-major); `ready`
+// once the HFB branch has started (startHFBIter)
 struct HFBRes {
-  std::vector<double> U, V, kappa; // M x M col-major
+  double *U = nullptr, *V = nullptr, *kappa = nullptr;
   int M = 0;
+  bool ready = false;
   double lambda = 0, energy = 0;
+};
+
+// Device workspace of the HFB step, shared by both species (they run one
+// after the other on the main stream); M = the larger basis
+struct HfbWork {
+  int M = 0;
+  double2 *gemmW = nullptr, *gemmParts = nullptr; // kappa / Delta products
+  void *gemmExact = nullptr; // exact-digit scratch (tensor-core form)
+  double *e = nullptr, *ff = nullptr, *Kff = nullptr, *Delta = nullptr,
+         *Uw = nullptr, *Vw = nullptr, *eig = nullptr, *scal = nullptr;
+  double2 *C = nullptr, *G = nullptr, *H = nullptr, *Hwork = nullptr,
+          *Hv = nullptr, *rho = nullptr, *Wm = nullptr, *T = nullptr;
+  int *perm = nullptr, *status = nullptr;
+  static constexpr int kChunks = 64;
 };
 
 struct Species {
@@ -210,7 +227,7 @@ struct Species {
   std::vector<double> e;
   int cdCols = 0;
   BCSRes bcs;
-  HFBRes hfb;
+  HFBRes hfb, hfbNew; // current amplitudes and the next step's candidate
   ncgm_pairing par;
 };
 
@@ -254,6 +271,65 @@ struct Run {
       tcScr = alloc<char>(b + 1024);
     }
     return tcScr;
+  }
+
+  // HFB workspace and both species' amplitude matrices (first use)
+  HfbWork hw;
+  HfbWork *hfbWork() {
+    if (hw.gemmW) return &hw;
+    const int M = std::max(sp[0].orb, sp[1].orb);
+    const size_t MM = (size_t)M * M;
+    HfbWork w;
+    w.M = M;
+    w.gemmParts = alloc<double2>(HfbWork::kChunks * MM);
+    if (tc()) {
+      // both bounds hold for every window size nS <= M
+      const size_t b =
+          std::max(exactGramScratchDoubles(ns, M, M) * sizeof(double),
+                   exactVCScratchBytes(M, M));
+      w.gemmExact = alloc<char>(b + 1024);
+      if (!w.gemmExact) return nullptr;
+    }
+    double *d = alloc<double>(4 * (size_t)M + 4 * MM + 2 * (size_t)M + 16);
+    double2 *c = alloc<double2>(2 * MM + 3 * 4 * MM + 3 * MM);
+    int *iw = alloc<int>(2 * (size_t)M + 16);
+    for (int q = 0; q < 2; ++q)
+      for (HFBRes *h : {&sp[q].hfb, &sp[q].hfbNew}) {
+        const size_t mq = (size_t)sp[q].orb * sp[q].orb;
+        h->U = alloc<double>(mq);
+        h->V = alloc<double>(mq);
+        h->kappa = alloc<double>(mq);
+        if (!h->kappa) return nullptr;
+      }
+    w.gemmW = alloc<double2>(N * (size_t)M);
+    if (!w.gemmParts || !d || !c || !iw || !w.gemmW) return nullptr;
+    w.e = d;
+    w.ff = w.e + M;
+    w.eig = w.ff + M; // 2M
+    w.Kff = w.eig + 2 * (size_t)M;
+    w.Delta = w.Kff + MM;
+    w.Uw = w.Delta + MM;
+    w.Vw = w.Uw + MM;
+    w.scal = w.Vw + MM;
+    w.C = c;
+    w.G = w.C + MM;
+    w.H = w.G + MM;
+    w.Hwork = w.H + 4 * MM;
+    w.Hv = w.Hwork + 4 * MM;
+    w.rho = w.Hv + 4 * MM;
+    w.Wm = w.rho + MM;
+    w.T = w.Wm + MM;
+    w.perm = iw;
+    w.status = iw + 2 * M + 8;
+    hw = w;
+    return &hw;
+  }
+  PairingGemm pairingGemm() const {
+    PairingGemm g;
+    if (tc()) g.exactScratch = hw.gemmExact;
+    g.partials = hw.gemmParts;
+    g.maxChunks = HfbWork::kChunks;
+    return g;
   }
 
   template <class T> T *alloc(size_t count) {
@@ -462,45 +538,31 @@ int solvePairingBCS(Run &R) {
 }
 
 // --- HFB (iteration_data.cpp:605-850) ---------------------------------------
-int heigHost(Run &R, const std::vector<double2> &A, int m, std::vector<double> &w,
-             std::vector<double2> &V) {
-  double2 *dA = R.cplx, *dW = R.cplx + (size_t)m * m, *dV = dW + (size_t)m * m;
-  double *dw = R.small;
-  int *dperm = R.ismall, *dst = R.ismall + m + 8;
-  cudaMemcpyAsync(dA, A.data(), sizeof(double2) * m * m, cudaMemcpyHostToDevice,
-                  R.s);
-  heig(dA, m, m, dW, dV, dw, dperm, dst, R.s);
-  w.resize(m);
-  V.resize((size_t)m * m);
-  int st = 0;
-  cudaMemcpyAsync(w.data(), dw, sizeof(double) * m, cudaMemcpyDeviceToHost, R.s);
-  cudaMemcpyAsync(V.data(), dV, sizeof(double2) * m * m, cudaMemcpyDeviceToHost,
-                  R.s);
-  cudaMemcpyAsync(&st, dst, sizeof(int), cudaMemcpyDeviceToHost, R.s);
-  NCGM_TRY(sync(R));
-  if (st != 0) {
-    setError("hfb: dense eigensolver did not converge");
-    return NCGM_ERR_EIG;
-  }
-  return NCGM_OK;
+// Everything runs on the device; the host keeps the Fermi-level search
+// (which trial lambda comes next) and reads one scalar per trial.
+int readScalar(Run &R, const double *d, double &v) {
+  NCGM_CUDA(cudaMemcpyAsync(&v, d, sizeof(double), cudaMemcpyDeviceToHost,
+                            R.s));
+  return sync(R);
 }
 
-HFBRes nullHFB(int target, const std::vector<double> &e) {
-  HFBRes h;
-  const int M = (int)e.size();
+void nullHFB(Run &R, int M, int target, const std::vector<double> &e,
+             HFBRes &h) {
   h.M = M;
+  h.ready = true;
   h.lambda = e[target - 1];
-  h.U.assign((size_t)M * M, 0.0);
-  h.V.assign((size_t)M * M, 0.0);
-  h.kappa.assign((size_t)M * M, 0.0);
   h.energy = 0.0;
-  for (int i = 0; i < target; ++i) h.V[(size_t)i * M + i] = 1.0;
-  return h;
+  hfbNull(M, target, h.U, h.V, h.kappa, R.s);
 }
 
 int hfbSpecies(Run &R, Species &S, int target, HFBRes &out) {
   const HFBRes &prev = S.hfb;
   const int M = S.orb;
+  HfbWork *w = R.hfbWork();
+  if (!w) {
+    setError("hfb: device allocation failed");
+    return NCGM_ERR_NOMEM;
+  }
   const double window = S.par.window, smooth = window / 10.0;
   auto fac = [&](double en, double lam) {
     double v = 1.0 / (1.0 + std::exp((en - lam - window) / smooth));
@@ -524,30 +586,25 @@ int hfbSpecies(Run &R, Species &S, int target, HFBRes &out) {
   const int nS = end - start + 1;
   // phi_rev = numericalTR(phi)
   timeReverse(S.X, S.TX, R.ns, M, R.N, true, R.s);
-  std::vector<double> Kff((size_t)nS * nS), ffs(nS);
-  for (int b = 0; b < nS; ++b) {
-    ffs[b] = ff[start + b];
-    for (int a = 0; a < nS; ++a)
-      Kff[(size_t)b * nS + a] =
-          prev.kappa[(size_t)(start + b) * M + (start + a)] * ff[start + a] *
-          ff[start + b];
-  }
-  double *dK = R.small, *dff = dK + (size_t)nS * nS, *dDelta = dff + nS,
-         *dkap = R.scratch;
-  cudaMemcpyAsync(dK, Kff.data(), sizeof(double) * nS * nS,
-                  cudaMemcpyHostToDevice, R.s);
-  cudaMemcpyAsync(dff, ffs.data(), sizeof(double) * nS, cudaMemcpyHostToDevice,
-                  R.s);
-  kappaField(S.TX, R.N, start, nS, dK, R.ns, dkap, R.s);
-  deltaMatrix(S.TX, R.N, start, nS, dff, dkap, R.n, R.h, S.par.V0, dDelta, R.s);
-  std::vector<double> Delta((size_t)nS * nS);
-  cudaMemcpyAsync(Delta.data(), dDelta, sizeof(double) * nS * nS,
-                  cudaMemcpyDeviceToHost, R.s);
-  NCGM_TRY(sync(R));
+  // the window's levels and factors, then K_ab f_a f_b from the previous
+  // kappa, kappa(r) and Delta_ab (one N x nS product and one weighted Gram;
+  // exact-digit tensor-core forms in the tensor-core precision form)
+  NCGM_CUDA(cudaMemcpyAsync(w->e, S.e.data() + start, sizeof(double) * nS,
+                            cudaMemcpyHostToDevice, R.s));
+  NCGM_CUDA(cudaMemcpyAsync(w->ff, ff.data() + start, sizeof(double) * nS,
+                            cudaMemcpyHostToDevice, R.s));
+  hfbKff(prev.kappa, M, start, nS, w->ff, w->Kff, R.s);
+  const PairingGemm g = R.pairingGemm();
+  const double2 *Phi0 = S.TX + (size_t)start * R.N;
+  double *dkap = R.scratch;
+  kappaFieldGemm(Phi0, R.N, nS, w->Kff, R.ns, dkap, w->gemmW, w->C, g, R.s);
+  deltaMatrixGemm(Phi0, R.N, nS, w->ff, dkap, R.n, R.h, S.par.V0, w->Delta,
+                  w->gemmW, w->G, g, R.s);
+  hfbNorm2(w->Delta, nS, w->scal, R.s);
   double dn = 0;
-  for (double x : Delta) dn += x * x;
+  NCGM_TRY(readScalar(R, w->scal, dn));
   if (std::sqrt(dn) < 1e-3) {
-    out = nullHFB(target, S.e);
+    nullHFB(R, M, target, S.e, out);
     return NCGM_OK;
   }
   // Fermi level: N(lambda) - target = 0 inside [lambda - 1.7, lambda + 1.7]
@@ -561,30 +618,15 @@ int hfbSpecies(Run &R, Species &S, int target, HFBRes &out) {
   bool haveLo = false, haveHi = false;
   int side = 0; // Illinois: which end was kept last
   const int m2 = 2 * nS;
-  std::vector<double> U((size_t)nS * nS), V((size_t)nS * nS);
-  std::vector<double2> H((size_t)m2 * m2);
-  std::vector<double> w;
-  std::vector<double2> Ev;
   for (int it = 0; it < 100; ++it) {
-    std::fill(H.begin(), H.end(), make_double2(0, 0));
-    for (int i = 0; i < nS; ++i) {
-      H[(size_t)i * m2 + i] = make_double2(S.e[start + i] - cur, 0);
-      H[(size_t)(nS + i) * m2 + nS + i] = make_double2(-(S.e[start + i] - cur), 0);
-    }
-    for (int j = 0; j < nS; ++j)
-      for (int i = 0; i < nS; ++i) {
-        H[(size_t)(nS + j) * m2 + i] = make_double2(Delta[(size_t)j * nS + i], 0);
-        H[(size_t)j * m2 + nS + i] = make_double2(-Delta[(size_t)j * nS + i], 0);
-      }
-    NCGM_TRY(heigHost(R, H, m2, w, Ev));
+    hfbMatrix(w->e, w->Delta, nS, cur, w->H, R.s);
+    heig(w->H, m2, m2, w->Hwork, w->Hv, w->eig, w->perm, w->status, R.s);
+    hfbExtract(w->Hv, nS, w->status, w->Uw, w->Vw, w->scal + 1, R.s);
     double num = 0;
-    for (int k = 0; k < nS; ++k) {
-      int q = k + nS;
-      for (int i = 0; i < nS; ++i) {
-        U[(size_t)k * nS + i] = Ev[(size_t)q * m2 + i].x;
-        V[(size_t)k * nS + i] = Ev[(size_t)q * m2 + nS + i].x;
-        num += V[(size_t)k * nS + i] * V[(size_t)k * nS + i];
-      }
+    NCGM_TRY(readScalar(R, w->scal + 1, num));
+    if (std::isnan(num)) {
+      setError("hfb: dense eigensolver did not converge");
+      return NCGM_ERR_EIG;
     }
     num += start;
     double diff = num - target;
@@ -611,49 +653,34 @@ int hfbSpecies(Run &R, Species &S, int target, HFBRes &out) {
       break;
     cur = next;
   }
-  lambda = cur;
+  // amplitudes on the whole basis, kappa = U V^T and the pairing energy
+  hfbAmplitudes(w->Uw, w->Vw, nS, start, M, out.U, out.V, out.kappa, R.s);
+  hfbPairEnergy(w->Delta, out.kappa, M, start, nS, w->scal + 2, R.s);
   double pe = 0;
-  for (int i = 0; i < nS; ++i)
-    for (int j = 0; j < nS; ++j) {
-      double kij = 0;
-      for (int k = 0; k < nS; ++k) kij += V[(size_t)k * nS + i] * U[(size_t)k * nS + j];
-      pe += Delta[(size_t)j * nS + i] * kij;
-    }
-  pe *= 0.5;
+  NCGM_TRY(readScalar(R, w->scal + 2, pe));
   out.M = M;
-  out.U.assign((size_t)M * M, 0.0);
-  out.V.assign((size_t)M * M, 0.0);
-  for (int j = 0; j < nS; ++j)
-    for (int i = 0; i < nS; ++i) {
-      out.V[(size_t)(start + j) * M + start + i] = V[(size_t)j * nS + i];
-      out.U[(size_t)(start + j) * M + start + i] = U[(size_t)j * nS + i];
-    }
-  for (int i = 0; i < start; ++i) out.V[(size_t)i * M + i] = 1.0;
-  for (int i = end + 1; i < M; ++i) out.U[(size_t)i * M + i] = 1.0;
-  out.kappa.assign((size_t)M * M, 0.0);
-  for (int i = 0; i < M; ++i)
-    for (int j = 0; j < M; ++j) {
-      double sacc = 0;
-      for (int k = 0; k < M; ++k)
-        sacc += out.U[(size_t)k * M + i] * out.V[(size_t)k * M + j];
-      out.kappa[(size_t)j * M + i] = sacc;
-    }
-  out.lambda = lambda;
+  out.ready = true;
+  out.lambda = cur;
   out.energy = pe;
   return NCGM_OK;
 }
 
-// Phi = phi * T (occupation transform) ; T given on host (M x M, col-major)
+// Phi = phi * T (occupation transform), T on the device (M x M, col-major)
+int occupyDev(Run &R, Species &S, const double2 *T) {
+  const int M = S.orb;
+  if (R.tc() && R.tcScratch())
+    gemmVCExact(S.X, R.N, M, T, M, M, S.Phi, R.N, R.N, R.tcScratch(), R.s);
+  else
+    gemmVC(S.X, R.N, M, T, M, M, S.Phi, R.N, R.N, 0.0, R.s);
+  return NCGM_OK;
+}
+
+// Phi = phi * T with T given on the host
 int occupy(Run &R, Species &S, const std::vector<double2> &T) {
   const int M = S.orb;
-  cudaMemcpyAsync(R.cplx, T.data(), sizeof(double2) * M * M,
-                  cudaMemcpyHostToDevice, R.s);
-  if (R.tc() && R.tcScratch())
-    gemmVCExact(S.X, R.N, M, R.cplx, M, M, S.Phi, R.N, R.N, R.tcScratch(),
-                R.s);
-  else
-    gemmVC(S.X, R.N, M, R.cplx, M, M, S.Phi, R.N, R.N, 0.0, R.s);
-  return NCGM_OK;
+  NCGM_CUDA(cudaMemcpyAsync(R.cplx, T.data(), sizeof(double2) * M * M,
+                            cudaMemcpyHostToDevice, R.s));
+  return occupyDev(R, S, R.cplx);
 }
 
 int occupiedOrbitals(Run &R, int q, bool bcsOcc, int &ncols,
@@ -661,6 +688,17 @@ int occupiedOrbitals(Run &R, int q, bool bcsOcc, int &ncols,
   Species &S = R.sp[q];
   const int M = S.orb;
   const bool pairing = R.cfg.pairing_type != NCGM_PAIRING_NONE;
+  // a run that ends before startHFBIter has BCS occupations only: the
+  // output step then occupies with those (no HFB amplitudes exist yet)
+  const bool hfbReady = S.hfb.ready;
+  if (pairing && S.par.active && R.cfg.pairing_type == NCGM_PAIRING_HFB &&
+      !hfbReady) {
+    if (S.bcs.v2.size() != (size_t)M) {
+      setError("hf: no pairing occupations to occupy the orbitals with");
+      return NCGM_ERR_ARG;
+    }
+    bcsOcc = true;
+  }
   if (bcsOcc || (pairing && S.par.active &&
                  R.cfg.pairing_type == NCGM_PAIRING_BCS)) {
     std::vector<double2> T((size_t)M * M, make_double2(0, 0));
@@ -673,27 +711,23 @@ int occupiedOrbitals(Run &R, int q, bool bcsOcc, int &ncols,
   }
   if (pairing && S.par.active && R.cfg.pairing_type == NCGM_PAIRING_HFB) {
     // natural orbitals of rho = V V^T (iteration_data.cpp:326-338)
-    std::vector<double2> rho((size_t)M * M);
-    for (int i = 0; i < M; ++i)
-      for (int j = 0; j < M; ++j) {
-        double sacc = 0;
-        for (int k = 0; k < M; ++k)
-          sacc += S.hfb.V[(size_t)k * M + i] * S.hfb.V[(size_t)k * M + j];
-        rho[(size_t)j * M + i] = make_double2(sacc, 0);
-      }
-    std::vector<double> w;
-    std::vector<double2> Wm;
-    NCGM_TRY(heigHost(R, rho, M, w, Wm));
-    for (auto &x : w)
-      if (x < 1e-12) x = 0.0;
-    std::vector<double2> T((size_t)M * M);
-    for (int j = 0; j < M; ++j)
-      for (int i = 0; i < M; ++i) {
-        double2 v = Wm[(size_t)j * M + i];
-        double sq = std::sqrt(w[j]);
-        T[(size_t)j * M + i] = make_double2(v.x * sq, v.y * sq);
-      }
-    NCGM_TRY(occupy(R, S, T));
+    HfbWork *w = R.hfbWork();
+    if (!w) {
+      setError("hfb: device allocation failed");
+      return NCGM_ERR_NOMEM;
+    }
+    hfbDensityMatrix(S.hfb.V, M, w->rho, R.s);
+    heig(w->rho, M, M, w->Hwork, w->Wm, w->eig, w->perm, w->status, R.s);
+    hfbNatural(w->Wm, w->eig, M, w->T, R.s);
+    int st = 0;
+    NCGM_CUDA(cudaMemcpyAsync(&st, w->status, sizeof(int),
+                              cudaMemcpyDeviceToHost, R.s));
+    NCGM_TRY(occupyDev(R, S, w->T));
+    NCGM_TRY(sync(R));
+    if (st != 0) {
+      setError("hfb: dense eigensolver did not converge (natural orbitals)");
+      return NCGM_ERR_EIG;
+    }
     Phi = S.Phi;
     ncols = M;
     return NCGM_OK;
@@ -719,32 +753,42 @@ int updateQuantities(Run &R, int iter) {
       bcsOcc = true;
     } else {
       if (iter == C.start_hfb_iter) {
+        // kappa_ii+1 = -kappa_i+1i = sqrt(u2 v2) of the BCS pairs, V = 0
+        if (!R.hfbWork()) {
+          setError("hfb: device allocation failed");
+          return NCGM_ERR_NOMEM;
+        }
         for (int q = 0; q < 2; ++q) {
           Species &S = R.sp[q];
           const int M = S.orb;
-          S.hfb.M = M;
-          S.hfb.kappa.assign((size_t)M * M, 0.0);
-          S.hfb.V.assign((size_t)M * M, 0.0);
-          S.hfb.lambda = S.bcs.lambda;
+          std::vector<double> kap((size_t)M * M, 0.0);
           for (int i = 0; i < M - 1; ++i)
             if (i % 2 == 0) {
               double uv = std::sqrt(S.bcs.u2[i] * S.bcs.v2[i]);
-              S.hfb.kappa[(size_t)(i + 1) * M + i] = uv;
-              S.hfb.kappa[(size_t)i * M + i + 1] = -1.0 * uv;
+              kap[(size_t)(i + 1) * M + i] = uv;
+              kap[(size_t)i * M + i + 1] = -1.0 * uv;
             }
+          NCGM_CUDA(cudaMemcpyAsync(S.hfb.kappa, kap.data(),
+                                    sizeof(double) * M * M,
+                                    cudaMemcpyHostToDevice, R.s));
+          NCGM_CUDA(cudaMemsetAsync(S.hfb.U, 0, sizeof(double) * M * M, R.s));
+          NCGM_CUDA(cudaMemsetAsync(S.hfb.V, 0, sizeof(double) * M * M, R.s));
+          S.hfb.M = M;
+          S.hfb.ready = true;
+          S.hfb.lambda = S.bcs.lambda;
         }
       }
       const int targets[2] = {C.A - C.Z, C.Z};
       for (int q = 0; q < 2; ++q) {
         Species &S = R.sp[q];
         if (!S.par.active) continue;
-        HFBRes nw;
+        HFBRes &nw = S.hfbNew;
         NCGM_TRY(hfbSpecies(R, S, targets[q], nw));
         if (std::isnan(nw.energy)) {
         } else if (std::abs(nw.energy) < 1e-12) {
           S.par.active = 0;
         } else {
-          S.hfb = nw;
+          std::swap(S.hfb, S.hfbNew);
         }
       }
     }

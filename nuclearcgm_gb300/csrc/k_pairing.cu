@@ -4,11 +4,13 @@
 //  * BCS with state-dependent G_pq = V0 int rho_p rho_q (BCS::compute_G_pairing
 //    and solveBCS, src/util/bcs.cpp:10-254): the density Gram on the lattice
 //    and the gap/Fermi-level iteration in one CTA;
-//  * HFB pairing field kappa(r), pairing matrix Delta_ab
-//    (kappa_field / delta_matrix, src/util/iteration_data.cpp:467-538);
+//  * HFB pairing field kappa(r) and pairing matrix Delta_ab
+//    (kappa_field / delta_matrix, src/util/iteration_data.cpp:467-538) as
+//    one N x nS product and one weighted Gram over the lattice points;
 //  * spherical harmonic-oscillator spinor guess (harmonic_oscillator_guess,
 //    src/solver/guess.cpp:10-248).
 #include "k_pairing.cuh"
+#include "k_dense.cuh"
 
 #include <cfloat>
 #include <cmath>
@@ -174,60 +176,207 @@ __global__ void bcsKernel(const double *eps, const double *Gp, int np, int A,
   }
 }
 
-// kappa(r) = Re sum_{a,b} f_a f_b K_ab (phi_a(1) phi_b(0) - phi_a(0) phi_b(1))
-__global__ void kappaFieldKernel(const double2 *Phi, size_t ld, int start,
-                                 int nS, const double *Kff, size_t ns,
-                                 double *kappa) {
+// C (nS x nS, complex, col-major) = Kff^T: column a of Q = Phi C is
+// sum_b K_ab phi_b (Kff already carries f_a f_b)
+__global__ void kffTransposeKernel(const double *Kff, int nS, double2 *C) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nS * nS) return;
+  const int b = e % nS, a = e / nS; // C(b, a) = K(a, b) = Kff[b nS + a]
+  C[e] = make_double2(Kff[(size_t)b * nS + a], 0.0);
+}
+
+// kappa(r) = sum_a Re(phi_a(r,1) Q_a(r,0) - phi_a(r,0) Q_a(r,1)), the
+// reference's double sum over (a, b) with the b sum done by the product
+// Q = Phi Kff^T; consecutive threads take consecutive points
+__global__ void kappaReduceKernel(const double2 *Phi, size_t ld,
+                                  const double2 *Q, size_t ldq, int nS,
+                                  size_t ns, double *kappa) {
   const size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (p >= ns) return;
   double acc = 0;
   for (int a = 0; a < nS; ++a) {
-    double2 a0 = Phi[(size_t)(start + a) * ld + 2 * p],
-            a1 = Phi[(size_t)(start + a) * ld + 2 * p + 1];
-    for (int b = 0; b < nS; ++b) {
-      double k = Kff[(size_t)b * nS + a];
-      if (k == 0.0) continue;
-      double2 b0 = Phi[(size_t)(start + b) * ld + 2 * p],
-              b1 = Phi[(size_t)(start + b) * ld + 2 * p + 1];
-      // Re(a1 b0 - a0 b1)
-      double re = (a1.x * b0.x - a1.y * b0.y) - (a0.x * b1.x - a0.y * b1.y);
-      acc += k * re;
-    }
+    const double2 a0 = Phi[(size_t)a * ld + 2 * p],
+                  a1 = Phi[(size_t)a * ld + 2 * p + 1];
+    const double2 q0 = Q[(size_t)a * ldq + 2 * p],
+                  q1 = Q[(size_t)a * ldq + 2 * p + 1];
+    acc += (a1.x * q0.x - a1.y * q0.y) - (a0.x * q1.x - a0.y * q1.y);
   }
   kappa[p] = acc;
 }
 
-// Delta_ab = 0.5 V0 f_a f_b Re int conj(phi_a(0) phi_b(1) - phi_a(1) phi_b(0))
-// kappa ; a < b, Delta antisymmetric. One block per (a,b).
-__global__ void deltaMatrixKernel(const double2 *Phi, size_t ld, int start,
-                                  int nS, const double *ff, const double *kappa,
-                                  int n, double h, double V0, double *Delta) {
-  __shared__ double sh[256];
-  const int a = blockIdx.x, b = blockIdx.y;
-  if (b < a) return;
+// The two spin planes of the Delta Gram: A0 = conj(phi(r, 0)) and
+// B1 = h^3 w(r) kappa(r) phi(r, 1), ns x nS each (ld ns), so that
+// (A0^H B1)_ab = int phi_a(r,0) kappa(r) phi_b(r,1)
+__global__ void deltaOperandsKernel(const double2 *Phi, size_t ld, int nS,
+                                    const double *kappa, int n, double h,
+                                    double2 *A0, double2 *B1) {
   const size_t ns = (size_t)n * n * n;
-  const double2 *pa = Phi + (size_t)(start + a) * ld,
-                *pb = Phi + (size_t)(start + b) * ld;
-  const double hhh = h * h * h;
-  const double fab = ff[a] * ff[b];
+  const size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const int a = blockIdx.y;
+  if (p >= ns || a >= nS) return;
+  const double2 v0 = Phi[(size_t)a * ld + 2 * p],
+                v1 = Phi[(size_t)a * ld + 2 * p + 1];
+  const double d = kappa[p] * h * h * h * trapW(p, n);
+  A0[(size_t)a * ns + p] = make_double2(v0.x, -v0.y);
+  B1[(size_t)a * ns + p] = make_double2(d * v1.x, d * v1.y);
+}
+
+// Delta_ab = 0.5 V0 f_a f_b Re int (phi_a(0) phi_b(1) - phi_a(1) phi_b(0))
+// kappa = 0.5 V0 f_a f_b Re(G_ab - G_ba) with G = A0^H B1 (antisymmetric,
+// zero diagonal)
+__global__ void deltaFromGramKernel(const double2 *G, int nS, const double *ff,
+                                    double V0, double *Delta) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nS * nS) return;
+  const int a = e % nS, b = e / nS;
+  Delta[e] = a == b ? 0.0
+                    : 0.5 * V0 * ff[a] * ff[b] *
+                          (G[(size_t)b * nS + a].x - G[(size_t)a * nS + b].x);
+}
+
+// --- HFB quasiparticle step (iteration_data.cpp:605-850) on the device ----
+// Matrices are col-major; M x M state matrices (U, V, kappa) index the whole
+// basis, nS x nS window matrices the states start .. start + nS - 1.
+
+// Kff(a, b) = kappa(start + a, start + b) f_a f_b
+__global__ void hfbKffKernel(const double *kappa, int M, int start, int nS,
+                             const double *ff, double *Kff) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nS * nS) return;
+  const int a = e % nS, b = e / nS;
+  Kff[e] = kappa[(size_t)(start + b) * M + start + a] * ff[a] * ff[b];
+}
+
+// out[0] = sum of squares of the nS x nS entries (one block)
+__global__ void hfbNorm2Kernel(const double *D, int nS, double *out) {
+  __shared__ double sh[256];
   double acc = 0;
-  for (size_t e = threadIdx.x; e < ns; e += blockDim.x) {
-    double2 a0 = pa[2 * e], a1 = pa[2 * e + 1], b0 = pb[2 * e], b1 = pb[2 * e + 1];
-    // t = (a0 b1) f_a f_b - (a1 b0) f_a f_b
-    double tr = ((a0.x * b1.x - a0.y * b1.y) - (a1.x * b0.x - a1.y * b0.y)) * fab;
-    // Re(conj(t) kappa) = tr * kappa
-    acc += tr * kappa[e] * hhh * trapW(e, n);
+  for (int e = threadIdx.x; e < nS * nS; e += blockDim.x) acc += D[e] * D[e];
+  acc = blockReduce(acc, sh);
+  if (threadIdx.x == 0) out[0] = acc;
+}
+
+// H = [[e - lambda, Delta], [-Delta, -(e - lambda)]] (2nS x 2nS, complex
+// storage of the real symmetric matrix)
+__global__ void hfbMatrixKernel(const double *e, const double *Delta, int nS,
+                                double lambda, double2 *H) {
+  const int m2 = 2 * nS;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= m2 * m2) return;
+  const int i = idx % m2, j = idx / m2;
+  double v = 0.0;
+  if (i < nS && j < nS) {
+    if (i == j) v = e[i] - lambda;
+  } else if (i >= nS && j >= nS) {
+    if (i == j) v = -(e[i - nS] - lambda);
+  } else if (i < nS) {
+    v = Delta[(size_t)(j - nS) * nS + i];
+  } else {
+    v = -Delta[(size_t)j * nS + (i - nS)];
   }
-  double s = blockReduce(acc, sh);
-  if (threadIdx.x == 0) {
-    double v = 0.5 * V0 * s;
-    if (a == b) {
-      Delta[(size_t)a * nS + a] = -v;
-    } else {
-      Delta[(size_t)b * nS + a] = v;
-      Delta[(size_t)a * nS + b] = -v;
-    }
+  H[idx] = make_double2(v, 0.0);
+}
+
+// The positive-energy half of the eigenvectors (ascending eigenvalues:
+// columns nS .. 2nS-1): U = upper block, V = lower block, and
+// num[0] = sum V^2 (NaN when the eigensolver reported failure). One block.
+__global__ void hfbExtractKernel(const double2 *Ev, int nS, const int *status,
+                                 double *Uw, double *Vw, double *num) {
+  __shared__ double sh[256];
+  const int m2 = 2 * nS;
+  double acc = 0;
+  for (int e = threadIdx.x; e < nS * nS; e += blockDim.x) {
+    const int i = e % nS, k = e / nS;
+    const double u = Ev[(size_t)(k + nS) * m2 + i].x,
+                 v = Ev[(size_t)(k + nS) * m2 + nS + i].x;
+    Uw[e] = u;
+    Vw[e] = v;
+    acc += v * v;
   }
+  acc = blockReduce(acc, sh);
+  if (threadIdx.x == 0) num[0] = (*status != 0) ? nan("") : acc;
+}
+
+// U, V on the whole basis: the window blocks, V = 1 below the window and
+// U = 1 above it (iteration_data.cpp: the padded amplitude matrices)
+__global__ void hfbPadKernel(const double *Uw, const double *Vw, int nS,
+                             int start, int M, double *U, double *V) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= M * M) return;
+  const int r = idx % M, c = idx / M;
+  const int end = start + nS - 1;
+  double u = 0.0, v = 0.0;
+  if (r >= start && r <= end && c >= start && c <= end) {
+    const size_t w = (size_t)(c - start) * nS + (r - start);
+    u = Uw[w];
+    v = Vw[w];
+  } else if (r == c) {
+    if (r < start) v = 1.0;
+    if (r > end) u = 1.0;
+  }
+  U[idx] = u;
+  V[idx] = v;
+}
+
+// kappa = U V^T (M x M)
+__global__ void hfbKappaKernel(const double *U, const double *V, int M,
+                               double *kappa) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= M * M) return;
+  const int i = idx % M, j = idx / M;
+  double acc = 0;
+  for (int k = 0; k < M; ++k)
+    acc += U[(size_t)k * M + i] * V[(size_t)k * M + j];
+  kappa[idx] = acc;
+}
+
+// pe[0] = 0.5 sum_ij Delta(i, j) (V U^T)(i, j) over the window, where
+// (V U^T)(i, j) = kappa(start + j, start + i). One block.
+__global__ void hfbPairEnergyKernel(const double *Delta, const double *kappa,
+                                    int M, int start, int nS, double *pe) {
+  __shared__ double sh[256];
+  double acc = 0;
+  for (int e = threadIdx.x; e < nS * nS; e += blockDim.x) {
+    const int i = e % nS, j = e / nS;
+    acc += Delta[e] * kappa[(size_t)(start + i) * M + start + j];
+  }
+  acc = blockReduce(acc, sh);
+  if (threadIdx.x == 0) pe[0] = 0.5 * acc;
+}
+
+// U = 0, V = 1 on the first `target` states, kappa = 0 (the unpaired
+// amplitudes)
+__global__ void hfbNullKernel(int M, int target, double *U, double *V,
+                              double *kappa) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= M * M) return;
+  const int r = idx % M, c = idx / M;
+  U[idx] = 0.0;
+  kappa[idx] = 0.0;
+  V[idx] = (r == c && r < target) ? 1.0 : 0.0;
+}
+
+// rho = V V^T (complex storage for the Hermitian eigensolver)
+__global__ void hfbDensityMatrixKernel(const double *V, int M, double2 *rho) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= M * M) return;
+  const int i = idx % M, j = idx / M;
+  double acc = 0;
+  for (int k = 0; k < M; ++k)
+    acc += V[(size_t)k * M + i] * V[(size_t)k * M + j];
+  rho[idx] = make_double2(acc, 0.0);
+}
+
+// T = W diag(sqrt(w)) with occupations below 1e-12 set to zero (the natural
+// orbitals weighted by their occupation, iteration_data.cpp:326-338)
+__global__ void hfbNaturalKernel(const double2 *W, const double *w, int M,
+                                 double2 *T) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= M * M) return;
+  const int j = idx / M;
+  const double x = w[j] < 1e-12 ? 0.0 : w[j];
+  const double sq = sqrt(x);
+  T[idx] = make_double2(W[idx].x * sq, W[idx].y * sq);
 }
 
 // spherical HO spinor (nr, l, j2, mj2) on the lattice, unnormalised
@@ -373,18 +522,90 @@ void bcsSolve(const double *eps, const double *Gp, int np, int A,
                               work);
 }
 
-void kappaField(const double2 *Phi, size_t ld, int start, int nS,
-                const double *Kff, size_t ns, double *kappa, cudaStream_t s) {
-  kappaFieldKernel<<<(unsigned)((ns + 127) / 128), 128, 0, s>>>(
-      Phi, ld, start, nS, Kff, ns, kappa);
+void kappaFieldGemm(const double2 *Phi, size_t ld, int nS, const double *Kff,
+                    size_t ns, double *kappa, double2 *Q, double2 *C,
+                    const PairingGemm &g, cudaStream_t s) {
+  if (nS <= 0) return;
+  const size_t N = 2 * ns;
+  kffTransposeKernel<<<(nS * nS + 255) / 256, 256, 0, s>>>(Kff, nS, C);
+  if (g.exactScratch)
+    gemmVCExact(Phi, ld, nS, C, nS, nS, Q, N, N, g.exactScratch, s);
+  else
+    gemmVC(Phi, ld, nS, C, nS, nS, Q, N, N, 0.0, s);
+  kappaReduceKernel<<<(unsigned)((ns + 255) / 256), 256, 0, s>>>(
+      Phi, ld, Q, N, nS, ns, kappa);
 }
 
-void deltaMatrix(const double2 *Phi, size_t ld, int start, int nS,
-                 const double *ff, const double *kappa, int n, double h,
-                 double V0, double *Delta, cudaStream_t s) {
-  dim3 grid(nS, nS);
-  deltaMatrixKernel<<<grid, 256, 0, s>>>(Phi, ld, start, nS, ff, kappa, n, h,
-                                         V0, Delta);
+void deltaMatrixGemm(const double2 *Phi, size_t ld, int nS, const double *ff,
+                     const double *kappa, int n, double h, double V0,
+                     double *Delta, double2 *work, double2 *G,
+                     const PairingGemm &g, cudaStream_t s) {
+  if (nS <= 0) return;
+  const size_t ns = (size_t)n * n * n;
+  double2 *A0 = work, *B1 = work + ns * nS;
+  dim3 grid((unsigned)((ns + 255) / 256), nS);
+  deltaOperandsKernel<<<grid, 256, 0, s>>>(Phi, ld, nS, kappa, n, h, A0, B1);
+  if (g.exactScratch)
+    gramTCExact(A0, ns, nS, B1, ns, nS, ns, G, nS,
+                static_cast<double *>(g.exactScratch), s);
+  else
+    gram(A0, ns, nS, B1, ns, nS, ns, G, nS, g.partials, g.maxChunks, s);
+  deltaFromGramKernel<<<(nS * nS + 255) / 256, 256, 0, s>>>(G, nS, ff, V0,
+                                                           Delta);
+}
+
+namespace {
+inline unsigned blocksFor(size_t n) { return (unsigned)((n + 255) / 256); }
+} // namespace
+
+void hfbKff(const double *kappa, int M, int start, int nS, const double *ff,
+            double *Kff, cudaStream_t s) {
+  if (nS <= 0) return;
+  hfbKffKernel<<<blocksFor((size_t)nS * nS), 256, 0, s>>>(kappa, M, start, nS,
+                                                          ff, Kff);
+}
+
+void hfbNorm2(const double *D, int nS, double *out, cudaStream_t s) {
+  hfbNorm2Kernel<<<1, 256, 0, s>>>(D, nS, out);
+}
+
+void hfbMatrix(const double *e, const double *Delta, int nS, double lambda,
+               double2 *H, cudaStream_t s) {
+  hfbMatrixKernel<<<blocksFor(4 * (size_t)nS * nS), 256, 0, s>>>(
+      e, Delta, nS, lambda, H);
+}
+
+void hfbExtract(const double2 *Ev, int nS, const int *status, double *Uw,
+                double *Vw, double *num, cudaStream_t s) {
+  hfbExtractKernel<<<1, 256, 0, s>>>(Ev, nS, status, Uw, Vw, num);
+}
+
+void hfbAmplitudes(const double *Uw, const double *Vw, int nS, int start,
+                   int M, double *U, double *V, double *kappa,
+                   cudaStream_t s) {
+  const unsigned b = blocksFor((size_t)M * M);
+  hfbPadKernel<<<b, 256, 0, s>>>(Uw, Vw, nS, start, M, U, V);
+  hfbKappaKernel<<<b, 256, 0, s>>>(U, V, M, kappa);
+}
+
+void hfbPairEnergy(const double *Delta, const double *kappa, int M, int start,
+                   int nS, double *pe, cudaStream_t s) {
+  hfbPairEnergyKernel<<<1, 256, 0, s>>>(Delta, kappa, M, start, nS, pe);
+}
+
+void hfbNull(int M, int target, double *U, double *V, double *kappa,
+             cudaStream_t s) {
+  hfbNullKernel<<<blocksFor((size_t)M * M), 256, 0, s>>>(M, target, U, V,
+                                                         kappa);
+}
+
+void hfbDensityMatrix(const double *V, int M, double2 *rho, cudaStream_t s) {
+  hfbDensityMatrixKernel<<<blocksFor((size_t)M * M), 256, 0, s>>>(V, M, rho);
+}
+
+void hfbNatural(const double2 *W, const double *w, int M, double2 *T,
+                cudaStream_t s) {
+  hfbNaturalKernel<<<blocksFor((size_t)M * M), 256, 0, s>>>(W, w, M, T);
 }
 
 void hoGuess(const int4 *orbs, int nev, int n, double a, double h, double b,

@@ -677,11 +677,24 @@ int chunkRows(size_t N, int p, int q) {
 
 } // namespace
 
+// Scratch of gramTCExact for any p' <= p, q' <= q columns: column scales
+// 2(p+q) doubles, exponents 2(p+q) ints and chunks x 2p' x 2q' partials. The
+// row chunking gives a product with fewer output tiles more chunks, so a
+// narrower product can need more partials than the widest one; the bound is
+// the largest over every (M tiles, N tiles) count up to those of (p, q), each
+// with its widest p', q'.
 size_t exactGramScratchDoubles(size_t N, int p, int q) {
-  const size_t rows = chunkRows(N, p, q);
-  const size_t chunks = (N + rows - 1) / rows;
-  return chunks * 4 * (size_t)p * q + 4 * (size_t)(p + q) + 8;
-} // (column scales 2(p+q) doubles, exponents 2(p+q) ints, partials)
+  const int mtiles = (2 * p + kM - 1) / kM, ntiles = (2 * q + kN - 1) / kN;
+  size_t part = 0;
+  for (int a = 1; a <= mtiles; ++a)
+    for (int b = 1; b <= ntiles; ++b) {
+      const int pp = std::min(p, a * kM / 2), qq = std::min(q, b * kN / 2);
+      const size_t rows = chunkRows(N, pp, qq);
+      const size_t chunks = (N + rows - 1) / rows;
+      part = std::max(part, chunks * 4 * (size_t)pp * qq);
+    }
+  return part + 4 * (size_t)(p + q) + 8;
+}
 
 int *exactGramErrWord() {
   static int *d = [] {

@@ -274,3 +274,37 @@ def test_multipole_constraint_fixed_point(l, m, target):
     assert abs(rg.E_int - ro.E_int) < E_TOL
     assert abs(rg.E_HF - ro.E_HF) < E_TOL
     assert abs(og["constraints_energy"] - oo["constraints_energy"]) < E_TOL
+
+
+def test_hfb_switch_off_occupies_particle_number_states():
+    """HFB with a basis larger than the particle number (20 states for 8
+    nucleons) and pairing weak enough that both species' pairing energy
+    falls to zero early in the run, as the 120Sn protons' does: from then
+    on each species occupies phi * nullOcc(particles), the first
+    `particles` columns (iteration_data.cpp:290-294, 319-323, as the
+    reference's release build computes that product). The run then settles
+    to the unpaired fixed point with 12 unoccupied states carried along."""
+    data = {"functional": "SKMstar", "nucleus": {"A": 16, "Z": 8},
+            "box": {"boxSize": 16.5, "axisMeshPoints": 12},
+            "pairing": {"type": "HFB", "HFbasisSize": 20, "V0": 100.0,
+                        "window": 5.0},
+            "maxIterations": 300, "energyTol": 0.0}
+    _, rg, og, ro, oo = _run_both(data, cg_tol=FP_CG_TOL)
+    dS = max(np.abs(og["spe_n"][:8] - oo["spe_n"][:8]).max(),
+             np.abs(og["spe_p"][:8] - oo["spe_p"][:8]).max())
+    dR = max(np.abs(og["rho_n"] - oo["rho_n"]).max(),
+             np.abs(og["rho_p"] - oo["rho_p"]).max())
+    print("HFB switched off: E_int %.6f / %.6f, max|dSPE| (occupied) %.2e, "
+          "max|drho| %.2e" % (rg.E_int, ro.E_int, dS, dR))
+    assert rg.E_pair_n == 0.0 and rg.E_pair_p == 0.0
+    assert ro.E_pair_n == 0.0 and ro.E_pair_p == 0.0
+    assert rg.last_dE < 1e-6 and ro.last_dE < 1e-6
+    assert abs(rg.E_int - ro.E_int) < E_TOL
+    assert dS < SPE_TOL
+    assert dR < RHO_TOL
+    n, h = 12, 16.5 / 11
+    w = np.ones(n)
+    w[0] = w[-1] = 0.5
+    wt = (w[:, None, None] * w[None, :, None] * w[None, None, :]).ravel()
+    for q in ("rho_n", "rho_p"):
+        assert abs((og[q] * wt).sum() * h ** 3 - 8.0) < 1e-8
