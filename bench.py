@@ -183,6 +183,61 @@ def _hf_wall_ca40():
     return out
 
 
+def _curve_cfg2():
+    """The 24Mg deformation curve: SkM*, 32^3 lattice, box 20 fm, HF+BCS
+    with 24 states per isospin, 16 beta2 points in [-0.3, 0.5] under the
+    curve-mode constraint set (main.cpp:176-185), each to |dE| < 1 keV.
+    Timed: all 16 points at once (ncgm_hf_run_batch, one stream and
+    context per point) in the FP64 and tensor-core forms, and the points one
+    after the other in the tensor-core form; per-point |dE| of the
+    tensor-core form against its own FP64 run. The CPU leg is the oracle's
+    measured cost per HF iteration at this size (tests/golden fixture
+    generation on the development host) times the FP64 iteration counts."""
+    import numpy as np
+    import nuclearcgm_gb300 as ng
+    from nuclearcgm_gb300 import abi
+    sys.path.insert(0, os.path.join(HERE, "tests", "golden"))
+    import make_fixtures as mf
+    out = {"workload": "24Mg HF+BCS curve, SkM*, 32^3 lattice, box 20 fm, "
+                       "24 states per isospin, 16 beta2 points in "
+                       "[-0.3, 0.5], |dE| < 1 keV per point", "unit": "s"}
+    res = {}
+    for name, prec in (("fp64", abi.FP64), ("tc", abi.FP32_TC)):
+        cfgs = mf.curve_configs(mf.MG24, prec, 1e-3, 500)
+        t0 = time.perf_counter()
+        res[name] = ng.hf_run_batch(cfgs)
+        out["batched_%s_s" % name] = round(time.perf_counter() - t0, 3)
+    cfgs = mf.curve_configs(mf.MG24, abi.FP32_TC, 1e-3, 500)
+    t0 = time.perf_counter()
+    for c in cfgs:
+        ng.hf_run(c)
+    out["serial_tc_s"] = round(time.perf_counter() - t0, 3)
+    e64 = np.array([r.E_HF for r in res["fp64"]])
+    etc = np.array([r.E_HF for r in res["tc"]])
+    out["E_HF_fp64_MeV"] = [round(x, 6) for x in e64]
+    out["beta_fp64"] = [round(r.beta, 5) for r in res["fp64"]]
+    out["iterations_fp64"] = [r.iterations for r in res["fp64"]]
+    out["converged"] = [bool(r.converged) for r in res["fp64"]]
+    out["max_abs_dE_tc_vs_fp64_MeV"] = float(np.abs(etc - e64).max())
+    # the oracle's measured seconds per HF iteration at this size
+    per_it = []
+    for name in ("mg24_skm_n32_p00", "mg24_skm_n32_p07", "mg24_skm_n32_p15"):
+        if os.path.exists(mf.path(name)):
+            fx = mf.load(name)
+            per_it.append(float(fx["oracle_seconds"]) /
+                          int(fx["iterations"]))
+    if per_it:
+        s_it = float(np.mean(per_it))
+        out["cpu_oracle_s_per_iteration"] = round(s_it, 3)
+        out["cpu_oracle_s_est"] = round(
+            s_it * sum(r.iterations for r in res["fp64"]), 1)
+        out["cpu_note"] = ("oracle FP64 seconds per iteration measured while "
+                           "generating the 24Mg fixtures (x86 host, all "
+                           "cores) times the 16 points' FP64 GPU iteration "
+                           "counts")
+    return out
+
+
 def _hf_wall(with_cpu):
     """Wall seconds to |dE| < 1 keV (the driver's stop rule, main.cpp:333-337)
     for the 16O HF ground state (SLy4, 30^3 lattice, box 18 fm, Woods-Saxon
@@ -427,11 +482,12 @@ def run_ours(args):
             traffic = json.load(open(tp)).get("dram_bytes_per_launch")
         except Exception:
             traffic = None
-    hf = gstep = hf_ca = None
+    hf = gstep = hf_ca = curve = None
     if rank == 0 and not args.no_hf:
         gstep = _gcg_step(H, X)
         hf = _hf_wall(not args.no_cpu)
         hf_ca = _hf_wall_ca40()
+        curve = _curve_cfg2()
     cpu = None
     if rank == 0 and not args.no_cpu:
         gbs_c, dt_c = _cpu_reference(3, 1, a, f, gradf, U, W, X, NCOLS)
@@ -464,6 +520,7 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "hf_wall_to_1keV": hf,
         "hf_wall_to_1keV_ca40": hf_ca,
+        "curve_cfg2": curve,
         "gcg_step": gstep,
     }
     if rank == 0:

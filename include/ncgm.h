@@ -287,6 +287,52 @@ typedef struct ncgm_hf_result {
 int ncgm_hf_run(const ncgm_hf_config *cfg, ncgm_hf_result *res, double *spe_n,
                 double *spe_p, double *rho_n, double *rho_p, double *energies);
 
+/* ---- self-consistent state (IterationData) ------------------------------ */
+
+/* The state of one self-consistent run: densities and their mixing history,
+ * mean fields, Coulomb field, constraints and pairing (BCS / HFB) state, for
+ * callers that drive their own HF loop around ncgm_gcg as main() does. */
+typedef struct ncgm_state ncgm_state;
+
+/* Replaces IterationData(input) (include/util/iteration_data.hpp:81-88,
+ * src/util/iteration_data.cpp:9-151) with the constraint set main() builds
+ * (src/main.cpp:164-185) from cfg: lattice, EDF, options, pairing, COM /
+ * curve / multipole constraints. The guess and loop fields of cfg are not
+ * used. */
+int ncgm_state_create(ncgm_state **out, const ncgm_hf_config *cfg);
+int ncgm_state_destroy(ncgm_state *st);
+
+#define NCGM_UPDATE_NORMALIZE 1 /* Wavefunction::normalize first (main.cpp:254) */
+#define NCGM_UPDATE_TRORDER 2   /* Wavefunction::TROrder first when pairing
+                                   (main.cpp:256-263) */
+/* Replaces IterationData::updateQuantities(neutronsPair, protonsPair, iter,
+ * constraints) (include/util/iteration_data.hpp:89-92,
+ * src/util/iteration_data.cpp:852-1125): pairing (BCS, or HFB from
+ * startHFBIter), occupations, densities rho, tau, J, div J with mixing,
+ * grad / Laplacian of rho, mean fields f, grad f, U (+ constraint field), W,
+ * and the Coulomb field of the protons. X*: 2 n^3 x ncols complex, e*: the
+ * eigenvalues (host or device X, host e); ncols must be the configured
+ * orbital counts. iter: the HF iteration (constraints join at 1). flags:
+ * NCGM_UPDATE_* steps of main() applied to the eigenvectors first. */
+int ncgm_state_update(ncgm_state *st, const double *Xn, const double *en,
+                      int ncols_n, const double *Xp, const double *ep,
+                      int ncols_p, int iter, int flags);
+/* The mean fields of a species after the last update, in the layout of
+ * ncgm_set_fields (host or device outputs; any may be NULL): f, grad f
+ * (n^3 x 3), U with the constraint field, W (n^3 x 3), UC (the Coulomb field
+ * for protons, zeros otherwise). */
+int ncgm_state_fields(ncgm_state *st, int species, double *f, double *gradf,
+                      double *U, double *W, double *UC);
+/* rho and tau of a species (n^3 each, either may be NULL) */
+int ncgm_state_densities(ncgm_state *st, int species, double *rho,
+                         double *tau);
+/* E_int = kinetic + totalEnergyIntegral and E_HF = HFEnergy
+ * (iteration_data.cpp:153-271, main.cpp:300-305) of the current densities
+ * with the new single-particle energies en, ep (host); also records
+ * |Delta E_HF| as IterationData::energyDiff for the constraints. */
+int ncgm_state_energy(ncgm_state *st, const double *en, const double *ep,
+                      double *E_int, double *E_HF);
+
 /* What the reference's output step (Output::shellsToFile,
  * src/system/output.cpp:97-408) reads from the final state. Array pointers
  * may be NULL (not wanted) and may be host or device memory. */

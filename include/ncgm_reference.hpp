@@ -7,7 +7,7 @@
 //   Hamiltonian / buildMatrix     (include/hamiltonian.hpp:16-46)
 //   gcgm_complex_no_B_lock        (include/solver.hpp:43-47)
 //   Utilities::solve              (include/util/utilities.hpp:19-24)
-//   EDF::setFromInteraction       (include/EDF.hpp:20-31)
+//   EDF, setFromInteraction       (include/EDF.hpp:4-31)
 //
 // Matrices are raw column-major complex<double> buffers in the Eigen layout
 // (rows s + 2(i + n(j + n k))). Define NCGM_WITH_EIGEN before including this
@@ -171,6 +171,61 @@ inline ncgm_edf edfFromSkyrme(const ncgm_skyrme &s) {
   check(ncgm_edf_from_skyrme(&s, &e), "ncgm_edf_from_skyrme");
   return e;
 }
+
+// SkyrmeParameters / FunctionalParameters (include/EDF.hpp:4-23): the same
+// fields in the same order as the C structs
+using SkyrmeParameters = ncgm_skyrme;
+using FunctionalParameters = ncgm_edf;
+
+// EDF (include/EDF.hpp:25-31, src/skyrme/EDF.cpp:4-59), built from one
+// functional-file object. `Json` is anything with contains(key) and
+// operator[](key) whose values have get<double>(): nlohmann::json itself, so
+// EDF(functional) reads the reference's functionals/<name>.json objects
+// unchanged. An interaction (a "t0" key) is converted with
+// setFromInteraction (W0_pr defaults to W0; te/to from "te"/"to", else from
+// "aT"/"bT", else zero); otherwise the coupling constants are read directly.
+class EDF {
+public:
+  FunctionalParameters params{};
+
+  template <class Json> explicit EDF(const Json &functional) {
+    auto num = [&](const char *key) {
+      return functional[key].template get<double>();
+    };
+    if (functional.contains("t0")) {
+      SkyrmeParameters p{};
+      p.W0 = num("W0");
+      p.W0_pr = functional.contains("W0_pr") ? num("W0_pr") : p.W0;
+      p.te = p.to = 0.0;
+      if (functional.contains("te")) {
+        p.te = num("te");
+        p.to = num("to");
+      } else if (functional.contains("aT")) {
+        p.to = 4 * num("aT") / 5;
+        p.te = 8 * num("bT") / 5 - p.to;
+      }
+      p.t0 = num("t0");
+      p.t1 = num("t1");
+      p.t2 = num("t2");
+      p.t3 = num("t3");
+      p.x0 = num("x0");
+      p.x1 = num("x1");
+      p.x2 = num("x2");
+      p.x3 = num("x3");
+      p.sigma = num("sigma");
+      setFromInteraction(p);
+    } else {
+      params = FunctionalParameters{
+          num("C0rr"),  num("C1rr"),  num("C0Drr"), num("C1Drr"),
+          num("C0rt"),  num("C1rt"),  num("C0J2"),  num("C1J2"),
+          num("C0rdr"), num("C1rdr"), num("C0nJ"),  num("C1nJ"),
+          num("sigma")};
+    }
+  }
+  void setFromInteraction(const SkyrmeParameters &p) {
+    check(ncgm_edf_from_skyrme(&p, &params), "ncgm_edf_from_skyrme");
+  }
+};
 
 #ifdef NCGM_WITH_EIGEN
 inline Eigen::MatrixXcd apply(const Hamiltonian &H, const Eigen::MatrixXcd &X,

@@ -210,6 +210,79 @@ def solve(H: Hamiltonian, ConjDir, calc: dict, guess, nev=None,
                                   precision)
 
 
+class IterationData:
+    """The self-consistent state of one run (IterationData,
+    include/util/iteration_data.hpp:81-137) for a caller that drives its own
+    HF loop around the GCG, as main() does (src/main.cpp:199-342):
+
+        data = IterationData(cfg)
+        data.update_quantities((Xn, en), (Xp, ep), it)   # densities, fields
+        H_n.set_fields(*data.fields(NEUTRON)[:4]); ...      # Hamiltonians
+        ... solve ...
+        E_int, E_HF = data.energies(new_en, new_ep)
+    """
+
+    def __init__(self, cfg: abi.HFConfig):
+        self.cfg = cfg
+        self.n = cfg.n
+        h = C.c_void_p()
+        _check(load().ncgm_state_create(C.byref(h), C.byref(cfg)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            load().ncgm_state_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def update_quantities(self, neutrons, protons, it,
+                          flags=abi.UPDATE_NORMALIZE | abi.UPDATE_TRORDER):
+        """IterationData::updateQuantities (iteration_data.cpp:852-1125);
+        neutrons / protons: (X, eigenvalues), X in the Eigen layout."""
+        (Xn, en), (Xp, ep) = neutrons, protons
+        Xn = np.asfortranarray(Xn, dtype=np.complex128)
+        Xp = np.asfortranarray(Xp, dtype=np.complex128)
+        en = np.ascontiguousarray(en, dtype=np.float64)
+        ep = np.ascontiguousarray(ep, dtype=np.float64)
+        _check(load().ncgm_state_update(self.h, Xn.ctypes.data, en.ctypes.data,
+                                        Xn.shape[1], Xp.ctypes.data,
+                                        ep.ctypes.data, Xp.shape[1], int(it),
+                                        int(flags)))
+
+    def fields(self, species):
+        """(f, grad f, U, W, UC) in the layout of Hamiltonian.set_fields
+        (UC is None for neutrons)."""
+        ns = self.n ** 3
+        f, U, UC = np.zeros(ns), np.zeros(ns), np.zeros(ns)
+        gf, W = np.zeros(3 * ns), np.zeros(3 * ns)
+        _check(load().ncgm_state_fields(self.h, species, f.ctypes.data,
+                                        gf.ctypes.data, U.ctypes.data,
+                                        W.ctypes.data, UC.ctypes.data))
+        return f, gf, U, W, (UC if species == abi.PROTON else None)
+
+    def densities(self, species):
+        """(rho, tau) of a species."""
+        ns = self.n ** 3
+        rho, tau = np.zeros(ns), np.zeros(ns)
+        _check(load().ncgm_state_densities(self.h, species, rho.ctypes.data,
+                                           tau.ctypes.data))
+        return rho, tau
+
+    def energies(self, en, ep):
+        """(E_int, E_HF) of the current densities with the new levels."""
+        en = np.ascontiguousarray(en, dtype=np.float64)
+        ep = np.ascontiguousarray(ep, dtype=np.float64)
+        a, b = C.c_double(), C.c_double()
+        _check(load().ncgm_state_energy(self.h, en.ctypes.data, ep.ctypes.data,
+                                        C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+
 def hf_run(cfg: abi.HFConfig, outputs: bool = False):
     """Runs the WS guess and HF(B) iteration on the GPU (ncgm_hf_run).
     With outputs, also what the reference's output step reads

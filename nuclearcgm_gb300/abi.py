@@ -149,7 +149,14 @@ SIGNATURES = {
     "ncgm_lp_eval": ([_vp, _i, _vp], _i),
     "ncgm_set_lp": ([_vp, _vp], _i),
     "ncgm_measure_fp64_gflops": ([_vp], _i),
+    "ncgm_state_create": ([C.POINTER(_vp), C.POINTER(HFConfig)], _i),
+    "ncgm_state_destroy": ([_vp], _i),
+    "ncgm_state_update": ([_vp, _vp, _vp, _i, _vp, _vp, _i, _i, _i], _i),
+    "ncgm_state_fields": ([_vp, _i, _vp, _vp, _vp, _vp, _vp], _i),
+    "ncgm_state_densities": ([_vp, _i, _vp, _vp], _i),
+    "ncgm_state_energy": ([_vp, _vp, _vp, _vp, _vp], _i),
 }
+UPDATE_NORMALIZE, UPDATE_TRORDER = 1, 2
 
 
 def bind(lib):

@@ -1226,11 +1226,11 @@ int addMultipoles(Run &R) {
   return NCGM_OK;
 }
 
-int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
-          double *spe_p, double *rho_n, double *rho_p, double *energiesOut,
-          ncgm_hf_outputs *out) {
-  const double tStart = now();
-  Run R;
+// The run's lattice state, contexts and constraint list for cfg
+// (IterationData's constructor, iteration_data.cpp:9-151, and the constraint
+// set-up of main.cpp:164-185). twoContexts: a second context for the protons'
+// concurrent eigenproblem when the species differ (unless NCGM_HF_SERIAL=1).
+int setupRun(Run &R, const ncgm_hf_config &cfg, bool twoContexts) {
   R.cfg = cfg;
   R.n = cfg.n;
   R.a = cfg.box_size / 2.0;
@@ -1254,7 +1254,7 @@ int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
   // two contexts and host threads; NCGM_HF_SERIAL=1 solves them one after
   // the other on one context. Either way each species runs the same kernels
   // on the same inputs, so the results are the same.
-  const bool twoSpecies = cfg.use_coulomb || N != Z;
+  const bool twoSpecies = twoContexts && (cfg.use_coulomb || N != Z);
   {
     const char *ser = std::getenv("NCGM_HF_SERIAL");
     if (twoSpecies && !(ser && ser[0] == '1')) {
@@ -1320,6 +1320,20 @@ int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
     R.cons.push_back(makeConstraint(5, 0.0));
     R.cons.push_back(makeConstraint(6, cfg.mu20));
   }
+  return NCGM_OK;
+}
+
+int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
+          double *spe_p, double *rho_n, double *rho_p, double *energiesOut,
+          ncgm_hf_outputs *out) {
+  const double tStart = now();
+  Run R;
+  NCGM_TRY(setupRun(R, cfg, true));
+  const int A = cfg.A, Z = cfg.Z, N = A - Z;
+  const bool pairing = cfg.pairing_type != NCGM_PAIRING_NONE;
+  const int orbN = R.sp[0].orb, orbP = R.sp[1].orb;
+  const int mx = std::max(orbN, orbP);
+  const bool twoSpecies = cfg.use_coulomb || N != Z;
 
   // --- Woods-Saxon guess (main.cpp:72-111) ---------------------------------
   double t0 = now();
@@ -1727,3 +1741,159 @@ extern "C" int ncgm_hf_run_batch(const ncgm_hf_config *cfgs, int count,
   return first;
 }
 
+
+// ---------------------------------------------------------------------------
+// IterationData as a handle (include/util/iteration_data.hpp:81-137): the
+// densities with their mixing history, the mean fields, the Coulomb field,
+// the constraints and the pairing state of one self-consistent run, updated
+// from eigenpairs the caller solved for (ncgm_state_update =
+// IterationData::updateQuantities, src/util/iteration_data.cpp:852-1125).
+// ---------------------------------------------------------------------------
+struct ncgm_state {
+  ncgm::Run R;
+  bool multipolesAdded = false;
+  double lastEHF = 0.0; // E_HF of the previous ncgm_state_energy call
+};
+
+namespace {
+int checkState(ncgm_state *st, const char *who) {
+  if (!st) {
+    setError(std::string(who) + ": null state");
+    return NCGM_ERR_ARG;
+  }
+  return NCGM_OK;
+}
+} // namespace
+
+extern "C" int ncgm_state_create(ncgm_state **out, const ncgm_hf_config *cfg) {
+  try {
+    if (!out || !cfg || cfg->n < 4 || cfg->box_size <= 0 || cfg->A < 2 ||
+        cfg->Z < 0 || cfg->Z > cfg->A) {
+      setError("ncgm_state_create: bad configuration");
+      return NCGM_ERR_ARG;
+    }
+    *out = nullptr;
+    auto *st = new ncgm_state();
+    const int rc = setupRun(st->R, *cfg, false);
+    if (rc != NCGM_OK) {
+      delete st;
+      return rc;
+    }
+    *out = st;
+    return NCGM_OK;
+  } catch (const std::exception &e) {
+    setError(e.what());
+    return NCGM_ERR_ARG;
+  }
+}
+
+extern "C" int ncgm_state_destroy(ncgm_state *st) {
+  delete st;
+  return NCGM_OK;
+}
+
+extern "C" int ncgm_state_update(ncgm_state *st, const double *Xn,
+                                 const double *en, int ncols_n,
+                                 const double *Xp, const double *ep,
+                                 int ncols_p, int iter, int flags) {
+  try {
+    NCGM_TRY(checkState(st, "ncgm_state_update"));
+    Run &R = st->R;
+    const double *X[2] = {Xn, Xp}, *e[2] = {en, ep};
+    const int cols[2] = {ncols_n, ncols_p};
+    for (int q = 0; q < 2; ++q)
+      if (!X[q] || !e[q] || cols[q] != R.sp[q].orb || iter < 0) {
+        setError("ncgm_state_update: need both species' eigenpairs with " +
+                 std::to_string(R.sp[0].orb) + " and " +
+                 std::to_string(R.sp[1].orb) + " columns, iter >= 0");
+        return NCGM_ERR_ARG;
+      }
+    const bool pairing = R.cfg.pairing_type != NCGM_PAIRING_NONE;
+    for (int q = 0; q < 2; ++q) {
+      Species &S = R.sp[q];
+      NCGM_CUDA(cudaMemcpyAsync(S.X, X[q], sizeof(double2) * R.N * cols[q],
+                                cudaMemcpyDefault, R.s));
+      S.e.assign(e[q], e[q] + cols[q]);
+      // main.cpp:254-263 before the next update
+      if (flags & NCGM_UPDATE_NORMALIZE)
+        normalizeColumns(S.X, R.N, cols[q], R.n, R.h, R.small, R.s);
+      if ((flags & NCGM_UPDATE_TRORDER) && pairing)
+        NCGM_TRY(trOrder(R, S, S.X));
+    }
+    // the input's multipole constraints join at HF iteration 1
+    // (main.cpp:201-207)
+    if (iter >= 1 && R.cfg.n_multipole > 0 && !st->multipolesAdded) {
+      NCGM_TRY(addMultipoles(R));
+      st->multipolesAdded = true;
+    }
+    NCGM_TRY(updateQuantities(R, iter));
+    return sync(R);
+  } catch (const std::exception &e) {
+    setError(e.what());
+    return NCGM_ERR_ARG;
+  }
+}
+
+extern "C" int ncgm_state_fields(ncgm_state *st, int species, double *f,
+                                 double *gradf, double *U, double *W,
+                                 double *UC) {
+  NCGM_TRY(checkState(st, "ncgm_state_fields"));
+  if (species != NCGM_NEUTRON && species != NCGM_PROTON) {
+    setError("ncgm_state_fields: bad species");
+    return NCGM_ERR_ARG;
+  }
+  Run &R = st->R;
+  const int q = species;
+  const size_t b = sizeof(double) * R.ns;
+  if (f) NCGM_CUDA(cudaMemcpyAsync(f, R.f[q], b, cudaMemcpyDefault, R.s));
+  if (gradf)
+    NCGM_CUDA(cudaMemcpyAsync(gradf, R.gf[q], 3 * b, cudaMemcpyDefault, R.s));
+  if (U) NCGM_CUDA(cudaMemcpyAsync(U, R.U[q], b, cudaMemcpyDefault, R.s));
+  if (W) NCGM_CUDA(cudaMemcpyAsync(W, R.W[q], 3 * b, cudaMemcpyDefault, R.s));
+  if (UC) {
+    if (q == NCGM_PROTON && R.cfg.use_coulomb && R.haveCoul)
+      NCGM_CUDA(cudaMemcpyAsync(UC, R.UCoul, b, cudaMemcpyDefault, R.s));
+    else
+      NCGM_CUDA(cudaMemsetAsync(UC, 0, b, R.s));
+  }
+  return sync(R);
+}
+
+extern "C" int ncgm_state_densities(ncgm_state *st, int species, double *rho,
+                                    double *tau) {
+  NCGM_TRY(checkState(st, "ncgm_state_densities"));
+  if (species != NCGM_NEUTRON && species != NCGM_PROTON) {
+    setError("ncgm_state_densities: bad species");
+    return NCGM_ERR_ARG;
+  }
+  Run &R = st->R;
+  const size_t b = sizeof(double) * R.ns;
+  if (rho)
+    NCGM_CUDA(cudaMemcpyAsync(rho, R.rho[species], b, cudaMemcpyDefault, R.s));
+  if (tau)
+    NCGM_CUDA(cudaMemcpyAsync(tau, R.tau[species], b, cudaMemcpyDefault, R.s));
+  return sync(R);
+}
+
+extern "C" int ncgm_state_energy(ncgm_state *st, const double *en,
+                                 const double *ep, double *E_int,
+                                 double *E_HF) {
+  try {
+    NCGM_TRY(checkState(st, "ncgm_state_energy"));
+    Run &R = st->R;
+    if (!en || !ep || !E_int || !E_HF) {
+      setError("ncgm_state_energy: null argument");
+      return NCGM_ERR_ARG;
+    }
+    R.sp[0].e.assign(en, en + R.sp[0].orb);
+    R.sp[1].e.assign(ep, ep + R.sp[1].orb);
+    NCGM_TRY(energies(R, *E_int, *E_HF));
+    // data.energyDiff, read by the constraints' multiplier updates
+    R.energyDiff = std::abs(*E_HF - st->lastEHF);
+    st->lastEHF = *E_HF;
+    return NCGM_OK;
+  } catch (const std::exception &e) {
+    setError(e.what());
+    return NCGM_ERR_ARG;
+  }
+}

@@ -89,6 +89,15 @@ int orc_hf_run(const ncgm_hf_config *cfg, ncgm_hf_result *res, double *spe_n,
 int orc_hf_run_ex(const ncgm_hf_config *cfg, ncgm_hf_result *res,
                   double *spe_n, double *spe_p, double *rho_n, double *rho_p,
                   double *energies, ncgm_hf_outputs *out, int verbose);
+/* The state-update counterpart of ncgm_state_*: `calls` updates from the
+ * same eigenpairs (iterations 0 .. calls-1), then the energies E[0..1] with
+ * the levels en2, ep2; out: per species f, grad f, U, W, UC, rho, tau
+ * (11 n^3). flags: 1 normalise, 2 TROrder (with pairing). */
+int orc_state_run(const ncgm_hf_config *cfg, const double *Xn,
+                  const double *en, int cn, const double *Xp,
+                  const double *ep, int cp, int calls, int flags,
+                  const double *en2, const double *ep2, double *out,
+                  double *E);
 /* obs: ncols x 5 as ncgm_shell_observables */
 void orc_shell_observables(int n, double a, const double *psi, int ncols,
                            double *obs);

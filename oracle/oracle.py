@@ -58,6 +58,8 @@ def lib():
             "orc_hf_run": ([vp, vp, vp, vp, vp, vp, vp, i], i),
             "orc_hf_run_ex": ([vp, vp, vp, vp, vp, vp, vp, vp, i], i),
             "orc_shell_observables": ([i, d, vp, i, vp], None),
+            "orc_state_run": ([vp, vp, vp, i, vp, vp, i, i, i, vp, vp, vp,
+                               vp], i),
         }
         for name, (a, r) in sig.items():
             f = getattr(_lib, name)
@@ -308,3 +310,37 @@ def hf_run(cfg, verbose=False):
     en = en[:res.iterations]
     return res, {"spe_n": spe_n, "spe_p": spe_p, "rho_n": rho_n,
                  "rho_p": rho_p, "energies": en}
+
+
+def state_run(cfg, neutrons, protons, calls, flags=1, new_levels=None):
+    """The state-update counterpart of ncgm_state_* (orc_state_run):
+    `calls` updates of IterationData from the same eigenpairs, then the
+    energies with new_levels (default: the same levels). Returns a dict of
+    per-species f, gradf, U, W, UC, rho, tau (suffix _n / _p) and E_int,
+    E_HF."""
+    (Xn, en), (Xp, ep) = neutrons, protons
+    Xn = np.asfortranarray(Xn, dtype=np.complex128)
+    Xp = np.asfortranarray(Xp, dtype=np.complex128)
+    en = np.ascontiguousarray(en, dtype=np.float64)
+    ep = np.ascontiguousarray(ep, dtype=np.float64)
+    en2, ep2 = (en, ep) if new_levels is None else (
+        np.ascontiguousarray(new_levels[0], dtype=np.float64),
+        np.ascontiguousarray(new_levels[1], dtype=np.float64))
+    ns = cfg.n ** 3
+    out = np.zeros(22 * ns)
+    E = np.zeros(2)
+    rc = lib().orc_state_run(C.byref(cfg), Xn.ctypes.data, en.ctypes.data,
+                             Xn.shape[1], Xp.ctypes.data, ep.ctypes.data,
+                             Xp.shape[1], int(calls), int(flags),
+                             en2.ctypes.data, ep2.ctypes.data,
+                             out.ctypes.data, E.ctypes.data)
+    if rc != 0:
+        raise RuntimeError("orc_state_run failed: %d" % rc)
+    res = {"E_int": E[0], "E_HF": E[1]}
+    o = 0
+    for q in ("n", "p"):
+        for name, k in (("f", 1), ("gradf", 3), ("U", 1), ("W", 3),
+                        ("UC", 1), ("rho", 1), ("tau", 1)):
+            res[name + "_" + q] = out[o:o + k * ns]
+            o += k * ns
+    return res

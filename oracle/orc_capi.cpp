@@ -213,6 +213,14 @@ int orc_hf_run_ex(const ncgm_hf_config *cfg, ncgm_hf_result *res,
   std::memset(out->terms, 0, sizeof(out->terms));
   return hfRun(*cfg, *res, spe_n, spe_p, rho_n, rho_p, energies, verbose, out);
 }
+int orc_state_run(const ncgm_hf_config *cfg, const double *Xn,
+                  const double *en, int cn, const double *Xp,
+                  const double *ep, int cp, int calls, int flags,
+                  const double *en2, const double *ep2, double *out,
+                  double *E) {
+  return stateRun(*cfg, Xn, en, cn, Xp, ep, cp, calls, flags, en2, ep2, out,
+                  E);
+}
 void orc_shell_observables(int n, double a, const double *psi, int ncols,
                            double *obs) {
   Grid g(n, a);

@@ -1496,4 +1496,81 @@ int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
   return NCGM_OK;
 }
 
+
+// IterationData held by a caller that drives its own loop (the device state
+// handle's counterpart; test infrastructure): `calls` updates of the state
+// from the same eigenpairs (HF iterations 0 .. calls-1, so the first sets
+// the densities and later ones mix; iteration_data.cpp:852-1125), then the
+// energies with the new levels en2, ep2 as main() evaluates them
+// (main.cpp:300-305). out, per species (neutrons then protons): f, grad f
+// (3), U, W (3), UC, rho, tau, 11 n^3 values. E: E_int, E_HF.
+int stateRun(const ncgm_hf_config &cfg, const double *Xn, const double *en,
+             int cn, const double *Xp, const double *ep, int cp, int calls,
+             int flags, const double *en2, const double *ep2, double *out,
+             double *E) {
+  Grid g(cfg.n, cfg.box_size / 2.0);
+  const std::size_t ns = g.ns();
+  const bool pairing = cfg.pairing_type != NCGM_PAIRING_NONE;
+  State st;
+  st.massCorr = cfg.com_corr ? kMass * ((double)cfg.A) / ((double)(cfg.A - 1))
+                             : kMass;
+  st.pN = cfg.pair_n;
+  st.pP = cfg.pair_p;
+  if (!pairing) {
+    st.pN.active = 0;
+    st.pP.active = 0;
+  }
+  std::vector<Constraint> cons;
+  if (cfg.constrain_com)
+    for (int k = 0; k < 3; ++k) cons.push_back(makeConstraint(g, k, 0.0));
+  if (cfg.curve_mode) {
+    for (int k = 0; k < 3; ++k) cons.push_back(makeConstraint(g, k, 0.0));
+    cons.push_back(makeConstraint(g, 3, 0.0));
+    cons.push_back(makeConstraint(g, 4, 0.0));
+    cons.push_back(makeConstraint(g, 5, 0.0));
+    cons.push_back(makeConstraint(g, 6, cfg.mu20));
+  }
+  Pair n, p;
+  n.X = CMat(g.N(), cn);
+  p.X = CMat(g.N(), cp);
+  std::memcpy(n.X.d.data(), Xn, sizeof(cd) * n.X.d.size());
+  std::memcpy(p.X.d.data(), Xp, sizeof(cd) * p.X.d.size());
+  n.e.assign(en, en + cn);
+  p.e.assign(ep, ep + cp);
+  PhaseTimes pt;
+  for (int it = 0; it < calls; ++it) {
+    if (flags & 1) {
+      normalize(g, n.X);
+      normalize(g, p.X);
+    }
+    if ((flags & 2) && pairing) {
+      n.X = TROrder(g, n.X);
+      p.X = TROrder(g, p.X);
+    }
+    updateQuantities(g, cfg, st, n, p, it, cons, pt);
+  }
+  n.e.assign(en2, en2 + cn);
+  p.e.assign(ep2, ep2 + cp);
+  E[0] = totalEnergyIntegral(g, cfg, st) + kineticEnergy(g, st);
+  E[1] = HFEnergy(g, cfg, st, cons);
+  const Vec zero(ns, 0.0);
+  const Vec *parts[2][7] = {
+      {&st.fN, &st.gfN, &st.UN, &st.BN, &zero, &st.rhoN, &st.tauN},
+      {&st.fP, &st.gfP, &st.UP, &st.BP,
+       (cfg.use_coulomb && st.haveCoul) ? &st.UCoul : &zero, &st.rhoP,
+       &st.tauP}};
+  double *o = out;
+  for (int q = 0; q < 2; ++q)
+    for (int k = 0; k < 7; ++k) {
+      const std::size_t len = (k == 1 || k == 3) ? 3 * ns : ns;
+      const Vec &v = *parts[q][k];
+      if (v.size() >= len)
+        std::copy(v.begin(), v.begin() + len, o);
+      else
+        std::fill(o, o + len, 0.0);
+      o += len;
+    }
+  return NCGM_OK;
+}
+
 } // namespace orc

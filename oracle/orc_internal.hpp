@@ -102,4 +102,8 @@ namespace orc {
 int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
           double *spe_p, double *rho_n, double *rho_p, double *energies,
           int verbose, ncgm_hf_outputs *out = nullptr);
+int stateRun(const ncgm_hf_config &cfg, const double *Xn, const double *en,
+             int cn, const double *Xp, const double *ep, int cp, int calls,
+             int flags, const double *en2, const double *ep2, double *out,
+             double *E);
 }
