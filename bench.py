@@ -183,6 +183,42 @@ def _hf_wall_ca40():
     return out
 
 
+SN120_HFB = {"functional": "SLy4", "nucleus": {"A": 120, "Z": 50},
+             "box": {"boxSize": 24.0, "axisMeshPoints": 48},
+             "pairing": {"type": "HFB", "HFbasisSize": 160, "V0": 300.0,
+                         "window": 60.0},
+             "maxIterations": 400, "energyTol": 1e-3}
+
+
+def _hf_wall_sn120(forms=("mixed_tc_gpu", "fp64_gpu")):
+    """120Sn HFB ground state: SLy4, 48^3 lattice, box 24 fm, 160
+    quasiparticle states per isospin, zero-range pairing V0 = 300 with a
+    60 MeV window, Coulomb by the Poisson solve, to |dE| < 1 keV (one run
+    per form; minutes each, so only with --sn120)."""
+    import nuclearcgm_gb300 as ng
+    from nuclearcgm_gb300 import abi, config
+    out = {"workload": "120Sn HFB ground state, SLy4, 48^3 lattice, box "
+                       "24 fm, 160 states per isospin, V0 300, 60 MeV "
+                       "window, |dE| < 1 keV", "unit": "s"}
+    precs = {"fp64_gpu": abi.FP64, "mixed_tc_gpu": abi.FP32_TC}
+    for name in forms:
+        cfg = config.from_input(SN120_HFB, precision=precs[name])
+        t0 = time.perf_counter()
+        res, _ = ng.hf_run(cfg)
+        out[name + "_s"] = round(time.perf_counter() - t0, 3)
+        out[name + "_iterations"] = res.iterations
+        out[name + "_converged"] = bool(res.converged)
+        out[name + "_E_MeV"] = round(res.E_HF, 6)
+        out[name + "_E_int_MeV"] = round(res.E_int, 6)
+        out[name + "_E_pair_n_MeV"] = round(res.E_pair_n, 6)
+        out[name + "_E_pair_p_MeV"] = round(res.E_pair_p, 6)
+        out[name + "_phase_s"] = {"gcg": round(res.t_gcg_s, 3),
+                                  "fields": round(res.t_fields_s, 3),
+                                  "poisson": round(res.t_poisson_s, 3),
+                                  "pairing": round(res.t_pairing_s, 3)}
+    return out
+
+
 def _curve_cfg2():
     """The 24Mg deformation curve: SkM*, 32^3 lattice, box 20 fm, HF+BCS
     with 24 states per isospin, 16 beta2 points in [-0.3, 0.5] under the
@@ -488,6 +524,7 @@ def run_ours(args):
         hf = _hf_wall(not args.no_cpu)
         hf_ca = _hf_wall_ca40()
         curve = _curve_cfg2()
+    sn = _hf_wall_sn120() if (rank == 0 and args.sn120) else None
     cpu = None
     if rank == 0 and not args.no_cpu:
         gbs_c, dt_c = _cpu_reference(3, 1, a, f, gradf, U, W, X, NCOLS)
@@ -521,6 +558,7 @@ def run_ours(args):
         "hf_wall_to_1keV": hf,
         "hf_wall_to_1keV_ca40": hf_ca,
         "curve_cfg2": curve,
+        "hf_wall_to_1keV_sn120": sn,
         "gcg_step": gstep,
     }
     if rank == 0:
@@ -538,6 +576,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true",
                     help="skip the CPU-baseline sample on our arm")
+    ap.add_argument("--sn120", action="store_true",
+                    help="also time the 120Sn HFB run to 1 keV (minutes)")
     ap.add_argument("--no-hf", action="store_true",
                     help="skip the HF wall-time-to-convergence record")
     args = ap.parse_args()

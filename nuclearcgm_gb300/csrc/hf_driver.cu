@@ -349,6 +349,29 @@ struct Run {
   }
 };
 
+// NCGM_HF_PHASE_SYNC=1: synchronise both species' streams after every phase
+// of an HF iteration and name the phase in the error, so that a failing
+// kernel is attributed to its phase (diagnostics; off by default)
+bool phaseSyncOn() {
+  static const bool v = [] {
+    const char *e = std::getenv("NCGM_HF_PHASE_SYNC");
+    return e && e[0] == '1';
+  }();
+  return v;
+}
+int phaseSync(Run &R, const char *phase, int it) {
+  if (!phaseSyncOn()) return NCGM_OK;
+  cudaError_t e = cudaStreamSynchronize(R.s);
+  if (e == cudaSuccess && R.ctxP) e = cudaStreamSynchronize(R.ctxP->stream);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    setError(std::string("hf: iteration ") + std::to_string(it) + ", " +
+             phase + ": " + cudaGetErrorString(e));
+    return NCGM_ERR_CUDA;
+  }
+  return NCGM_OK;
+}
+
 int sync(Run &R) {
   cudaError_t e = cudaStreamSynchronize(R.s);
   if (e != cudaSuccess) {
@@ -1371,6 +1394,7 @@ int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
   for (it = 0; it < cfg.max_iterations; ++it) {
     if (it == 1 && cfg.n_multipole > 0) NCGM_TRY(addMultipoles(R));
     NCGM_TRY(updateQuantities(R, it));
+    NCGM_TRY(phaseSync(R, "densities, fields and pairing", it));
     NCGM_TRY(buildCoefficients(R.ctx, 0, R.f[0], R.gf[0], R.U[0],
                                cfg.spin_orbit ? R.W[0] : nullptr, nullptr));
     // the proton context's stream waits for this iteration's fields and
@@ -1431,6 +1455,7 @@ int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
       std::copy(lamN.begin(), lamN.begin() + orbP, lamP.begin());
     }
     R.tGcg += now() - t0;
+    NCGM_TRY(phaseSync(R, "eigensolver", it));
     // training pairs for the learned preconditioner: the new eigenpairs on
     // this iteration's Hamiltonians, with the shift the next GCG call uses
     if (cfg.lp && cfg.lp_collect_every > 0 && it % cfg.lp_collect_every == 0) {
@@ -1452,16 +1477,19 @@ int hfRun(const ncgm_hf_config &cfg, ncgm_hf_result &res, double *spe_n,
       NCGM_TRY(trOrder(R, Sn, Sn.Xn));
       NCGM_TRY(trOrder(R, Sp, Sp.Xn));
     }
+    NCGM_TRY(phaseSync(R, "normalisation and time-reversal order", it));
     if (it > 0) {
       NCGM_TRY(conjDir(R, Sn));
       NCGM_TRY(conjDir(R, Sp));
     }
+    NCGM_TRY(phaseSync(R, "conjugate directions", it));
     std::swap(Sn.X, Sn.Xn);
     std::swap(Sp.X, Sp.Xn);
     Sn.e = lamN;
     Sp.e = lamP;
     double nE = 0, nH = 0;
     NCGM_TRY(energies(R, nE, nH));
+    NCGM_TRY(phaseSync(R, "energies", it));
     bool cconv = true;
     for (auto &c : R.cons)
       if (c.error() != 0.0) cconv = cconv && (c.error() < cfg.constraints_tol);

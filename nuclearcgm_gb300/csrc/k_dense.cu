@@ -820,6 +820,17 @@ static bool heigFp64Only() {
   return v;
 }
 
+// NCGM_HEIG_MID=1 selects the one-CTA Householder method (heigMid) for the
+// fast path's projected problems up to heigMidMax() instead of the
+// double-float Jacobi (comparisons)
+static bool heigMidOn() {
+  static const bool v = [] {
+    const char *e = std::getenv("NCGM_HEIG_MID");
+    return e && e[0] == '1';
+  }();
+  return v;
+}
+
 void heig(const double2 *A, int lda, int m, double2 *work, double2 *V,
           double *w, int *perm, int *status, cudaStream_t s, bool fast) {
   // the round-robin tables hold up to 256 pairs (m <= 512)
@@ -830,6 +841,16 @@ void heig(const double2 *A, int lda, int m, double2 *work, double2 *V,
     return true;
   }();
   (void)attr;
+  if (fast && m <= heigMidMax() && !heigFp64Only() && heigMidOn()) {
+    // stream-ordered scratch, as the multi-kernel solver below
+    void *scr = nullptr;
+    if (cudaMallocAsync(&scr, heigMidScratchBytes(m), s) == cudaSuccess) {
+      heigMid(A, lda, m, V, w, perm, status, scr, s);
+      cudaFreeAsync(scr, s);
+      return;
+    }
+    cudaGetLastError();
+  }
   if (fast && m <= kHeigDfMax && !heigFp64Only()) {
     static const bool dfAttr = [] {
       cudaFuncSetAttribute(heigDfKernel,

@@ -47,10 +47,19 @@ void cholDrop(const double2 *G, int ldg, int m, double dropTol, double2 *R,
 void heigLarge(const double2 *A, int lda, int m, double2 *V, double *w,
                int *perm, int *status, void *scratch, cudaStream_t s);
 size_t heigLargeScratchBytes(int m);
+// The same method with the tridiagonalisation in one CTA and the matrix in
+// shared memory, for m <= heigMidMax() (k_heig_large.cu).
+void heigMid(const double2 *A, int lda, int m, double2 *V, double *w,
+             int *perm, int *status, void *scratch, cudaStream_t s);
+size_t heigMidScratchBytes(int m);
+int heigMidMax();
 // Hermitian eigensolver (lower triangle): w ascending, V eigenvectors (m x m).
-// fast: for m <= 80, double-float sweeps finished by FP64 sweeps (same
-// accuracy, a different rounding path, so degenerate eigenvectors may come
-// out rotated within their eigenspace); otherwise the FP64 Jacobi.
+// fast (the FP32 precision forms): for m <= 80, double-float sweeps finished
+// by FP64 sweeps (same accuracy, a different rounding path, so degenerate
+// eigenvectors may come out rotated within their eigenspace), or with
+// NCGM_HEIG_MID=1 the one-CTA Householder method up to heigMidMax();
+// otherwise the FP64 Jacobi up to m = 80 and the multi-kernel Householder
+// method above it.
 void heig(const double2 *A, int lda, int m, double2 *work, double2 *V,
           double *w, int *perm, int *status, cudaStream_t s,
           bool fast = false);

@@ -333,45 +333,163 @@ __global__ void clusterMgsKernel(const double *w, int m, double *Z) {
   }
 }
 
-__global__ void toComplexKernel(const double *Z, int m, double2 *X) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e < m * m) X[e] = make_double2(Z[e], 0.0);
+// One-CTA tridiagonalisation for m <= kMidMax: the same reflectors as steps
+// hhVector / hhMatvec / hhW / hhUpdate, with the full Hermitian matrix in
+// shared memory and __syncthreads between the phases of a step, so the
+// whole reduction is one launch instead of four per column. The
+// matrix-vector product reads column i of A22 (contiguous in shared memory)
+// and uses A22 v = conj(A22^H) v: the rank-2 updates keep A exactly
+// Hermitian, element (j, i) being computed as the conjugate of (i, j) with
+// the same roundings.
+constexpr int kMidMax = 112; // 112^2 x 16 B = 196 KB of shared memory
+constexpr int kMidT = 512;
+__global__ void __launch_bounds__(kMidT, 1)
+    hhTridiagSmemKernel(const double2 *Ain, int lda, int m, double2 *Vr,
+                        double2 *tau, double *d, double *e) {
+  extern __shared__ double2 Ash[];
+  __shared__ double2 vs[kMidMax], ps[kMidMax];
+  __shared__ double sh[kMidT];
+  __shared__ double2 sc;
+  __shared__ int skip;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int warp = tid / 32, lane = tid % 32, nw = nt / 32;
+  for (int q = tid; q < m * m; q += nt) {
+    const int i = q % m, j = q / m;
+    double2 v;
+    if (i > j) v = Ain[(size_t)j * lda + i];
+    else if (i < j) {
+      const double2 l = Ain[(size_t)i * lda + j];
+      v = make_double2(l.x, -l.y);
+    } else v = make_double2(Ain[(size_t)j * lda + i].x, 0.0);
+    Ash[q] = v;
+  }
+  __syncthreads();
+  for (int k = 0; k + 1 < m; ++k) {
+    const int L = m - k - 1;
+    const double2 *x = Ash + (size_t)k * m + k + 1;
+    double loc = 0;
+    for (int i = 1 + tid; i < L; i += nt)
+      loc += x[i].x * x[i].x + x[i].y * x[i].y;
+    const double xn2 = blockSumD(loc, sh);
+    if (tid == 0) {
+      const double2 al = x[0];
+      d[k] = Ash[(size_t)k * m + k].x;
+      if (xn2 == 0.0 && al.y == 0.0) {
+        tau[k] = make_double2(0.0, 0.0);
+        e[k] = al.x;
+        skip = 1;
+      } else {
+        const double beta =
+            -(al.x >= 0.0 ? 1.0 : -1.0) * sqrt(al.x * al.x + al.y * al.y + xn2);
+        tau[k] = make_double2((beta - al.x) / beta, -al.y / beta);
+        e[k] = beta;
+        const double2 den = make_double2(al.x - beta, al.y);
+        const double dd = den.x * den.x + den.y * den.y;
+        sc = make_double2(den.x / dd, -den.y / dd);
+        skip = 0;
+      }
+    }
+    __syncthreads();
+    const bool sk = skip != 0;
+    const double2 t = tau[k]; // written by thread 0 before the barrier
+    double2 *vg = Vr + (size_t)k * m;
+    for (int i = tid; i < m; i += nt) {
+      double2 r = make_double2(0.0, 0.0);
+      if (!sk && i > k) r = (i == k + 1) ? make_double2(1.0, 0.0)
+                                         : cmulD(x[i - k - 1], sc);
+      vg[i] = r;
+      if (i > k) vs[i - k - 1] = r;
+    }
+    __syncthreads();
+    if (sk || L < 2) continue; // uniform: skip and L are shared
+    // p = tau A22 v, one warp per row; A22[i][j] = conj(A22[j][i]) read
+    // along column i
+    for (int i = warp; i < L; i += nw) {
+      const double2 *col = Ash + (size_t)(k + 1 + i) * m + k + 1;
+      double re = 0, im = 0;
+      for (int j = lane; j < L; j += 32) {
+        const double2 a = col[j], v = vs[j]; // conj(a) v
+        re += a.x * v.x + a.y * v.y;
+        im += a.x * v.y - a.y * v.x;
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        re += __shfl_xor_sync(0xffffffffu, re, o);
+        im += __shfl_xor_sync(0xffffffffu, im, o);
+      }
+      if (lane == 0) ps[i] = cmulD(t, make_double2(re, im));
+    }
+    __syncthreads();
+    // w = p - tau/2 (p^H v) v
+    double re = 0, im = 0;
+    for (int i = tid; i < L; i += nt) {
+      const double2 pv = cconjmulD(ps[i], vs[i]);
+      re += pv.x;
+      im += pv.y;
+    }
+    re = blockSumD(re, sh);
+    im = blockSumD(im, sh);
+    const double2 a2 =
+        cmulD(make_double2(-0.5 * t.x, -0.5 * t.y), make_double2(re, im));
+    for (int i = tid; i < L; i += nt) {
+      const double2 av = cmulD(a2, vs[i]);
+      ps[i].x += av.x;
+      ps[i].y += av.y;
+    }
+    __syncthreads();
+    // A22[i][j] -= v_i conj(w_j) + w_i conj(v_j)
+    for (int q = tid; q < L * L; q += nt) {
+      const int i = q % L, j = q / L;
+      const double2 a = cconjmulD(ps[j], vs[i]);
+      const double2 b = cconjmulD(vs[j], ps[i]);
+      double2 &y = Ash[(size_t)(k + 1 + j) * m + (k + 1 + i)];
+      y.x -= a.x + b.x;
+      y.y -= a.y + b.y;
+    }
+    __syncthreads();
+  }
+  if (tid == 0) d[m - 1] = Ash[(size_t)(m - 1) * m + (m - 1)].x;
 }
 
-// back-transformation step k: y_c = sum_i conj(v_i) X[k+1+i][c] (one warp
-// per column), then X[k+1+i][c] -= tau v_i y_c
-__global__ void btDotKernel(const double2 *X, int m, int k, const double2 *Vr,
-                            double2 *y) {
-  const int c = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-  const int lane = threadIdx.x % 32;
+// X = H_0 H_1 ... H_{m-2} Z for the real tridiagonal eigenvectors Z, one
+// warp per column with the column in shared memory: the reflectors are
+// applied from the last to the first (y = v_k^H x, x -= tau_k v_k y)
+constexpr int kBtWarps = 2;
+__global__ void __launch_bounds__(32 * kBtWarps)
+    btColumnsKernel(const double *Z, int m, const double2 *Vr,
+                    const double2 *tau, double2 *X) {
+  extern __shared__ double2 xs[]; // kBtWarps x m
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int c = blockIdx.x * kBtWarps + warp;
   if (c >= m) return;
-  const int L = m - k - 1;
-  const double2 *v = Vr + (size_t)k * m + k + 1;
-  const double2 *x = X + (size_t)c * m + k + 1;
-  double re = 0, im = 0;
-  for (int i = lane; i < L; i += 32) {
-    const double2 t = cconjmulD(v[i], x[i]);
-    re += t.x;
-    im += t.y;
+  double2 *x = xs + (size_t)warp * m;
+  for (int i = lane; i < m; i += 32)
+    x[i] = make_double2(Z[(size_t)c * m + i], 0.0);
+  __syncwarp();
+  for (int k = m - 2; k >= 0; --k) {
+    const double2 t = tau[k];
+    if (t.x == 0.0 && t.y == 0.0) continue;
+    const int L = m - k - 1;
+    const double2 *v = Vr + (size_t)k * m + k + 1;
+    double2 *xx = x + k + 1;
+    double re = 0, im = 0;
+    for (int i = lane; i < L; i += 32) {
+      const double2 p = cconjmulD(v[i], xx[i]);
+      re += p.x;
+      im += p.y;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      re += __shfl_xor_sync(0xffffffffu, re, o);
+      im += __shfl_xor_sync(0xffffffffu, im, o);
+    }
+    const double2 ty = cmulD(t, make_double2(re, im));
+    for (int i = lane; i < L; i += 32) {
+      const double2 u = cmulD(v[i], ty);
+      xx[i].x -= u.x;
+      xx[i].y -= u.y;
+    }
+    __syncwarp();
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    re += __shfl_xor_sync(0xffffffffu, re, o);
-    im += __shfl_xor_sync(0xffffffffu, im, o);
-  }
-  if (lane == 0) y[c] = make_double2(re, im);
-}
-__global__ void btUpdateKernel(double2 *X, int m, int k, const double2 *Vr,
-                               const double2 *tau, const double2 *y) {
-  const int L = m - k - 1;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int c = blockIdx.y;
-  if (i >= L) return;
-  const double2 t = tau[k];
-  const double2 tv = cmulD(t, Vr[(size_t)k * m + k + 1 + i]);
-  const double2 u = cmulD(tv, y[c]);
-  double2 &x = X[(size_t)c * m + k + 1 + i];
-  x.x -= u.x;
-  x.y -= u.y;
+  for (int i = lane; i < m; i += 32) X[(size_t)c * m + i] = x[i];
 }
 
 __global__ void finishKernel(int m, int *perm, int *status) {
@@ -386,7 +504,7 @@ size_t heigLargeScratchBytes(int m) {
   const size_t mm = (size_t)m * m;
   return 2 * mm * sizeof(double2)                // A, Vr
          + (size_t)kJC * m * sizeof(double2)     // P
-         + 2 * (size_t)m * sizeof(double2)       // Wv, y
+         + (size_t)m * sizeof(double2)           // Wv
          + (size_t)m * sizeof(double2)           // tau
          + 2 * (size_t)m * sizeof(double)        // d, e
          + 4 * mm * sizeof(double) + 1024;       // Z, F (3)
@@ -407,7 +525,6 @@ void heigLarge(const double2 *Ain, int lda, int m, double2 *V, double *w,
   double2 *Vr = reinterpret_cast<double2 *>(take(mm * sizeof(double2)));
   double2 *P = reinterpret_cast<double2 *>(take((size_t)kJC * m * sizeof(double2)));
   double2 *Wv = reinterpret_cast<double2 *>(take(m * sizeof(double2)));
-  double2 *y = reinterpret_cast<double2 *>(take(m * sizeof(double2)));
   double2 *tau = reinterpret_cast<double2 *>(take(m * sizeof(double2)));
   double *d = reinterpret_cast<double *>(take(m * sizeof(double)));
   double *e = reinterpret_cast<double *>(take(m * sizeof(double)));
@@ -428,13 +545,53 @@ void heigLarge(const double2 *Ain, int lda, int m, double2 *V, double *w,
   bisectKernel<<<(m + 63) / 64, 64, 0, s>>>(d, e, m, w);
   invIterKernel<<<(m + 63) / 64, 64, 0, s>>>(d, e, m, w, Z, F);
   clusterMgsKernel<<<m, kT, 0, s>>>(w, m, Z);
-  toComplexKernel<<<gm, kT, 0, s>>>(Z, m, V);
-  for (int k = m - 2; k >= 0; --k) {
-    const int L = m - k - 1;
-    btDotKernel<<<(m + 7) / 8, 256, 0, s>>>(V, m, k, Vr, y);
-    btUpdateKernel<<<dim3((L + 127) / 128, m), 128, 0, s>>>(V, m, k, Vr, tau,
-                                                           y);
-  }
+  btColumnsKernel<<<(m + kBtWarps - 1) / kBtWarps, 32 * kBtWarps,
+                    kBtWarps * (size_t)m * sizeof(double2), s>>>(Z, m, Vr, tau,
+                                                                 V);
+  finishKernel<<<(m + 255) / 256, 256, 0, s>>>(m, perm, status);
+}
+
+size_t heigMidScratchBytes(int m) {
+  const size_t mm = (size_t)m * m;
+  return mm * sizeof(double2) + 256         // Vr
+         + (size_t)m * sizeof(double2) + 256 // tau
+         + 2 * ((size_t)m * sizeof(double) + 256) // d, e
+         + 4 * mm * sizeof(double) + 1024;  // Z, F (3)
+}
+int heigMidMax() { return kMidMax; }
+
+// The Householder method of heigLarge with the tridiagonalisation in one CTA
+// (m <= kMidMax): one launch for the reduction, bisection, inverse
+// iteration, cluster orthogonalisation and the per-column
+// back-transformation.
+void heigMid(const double2 *Ain, int lda, int m, double2 *V, double *w,
+             int *perm, int *status, void *scratch, cudaStream_t s) {
+  const size_t mm = (size_t)m * m;
+  char *p = static_cast<char *>(scratch);
+  auto take = [&](size_t bytes) {
+    char *r = p;
+    p += (bytes + 255) & ~(size_t)255;
+    return r;
+  };
+  double2 *Vr = reinterpret_cast<double2 *>(take(mm * sizeof(double2)));
+  double2 *tau = reinterpret_cast<double2 *>(take(m * sizeof(double2)));
+  double *d = reinterpret_cast<double *>(take(m * sizeof(double)));
+  double *e = reinterpret_cast<double *>(take(m * sizeof(double)));
+  double *Z = reinterpret_cast<double *>(take(mm * sizeof(double)));
+  double *F = reinterpret_cast<double *>(take(3 * mm * sizeof(double)));
+  // the dynamic shared-memory limit is a per-device attribute: set on every
+  // call (a driver call of about a microsecond)
+  cudaFuncSetAttribute(hhTridiagSmemKernel,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       kMidMax * kMidMax * (int)sizeof(double2));
+  hhTridiagSmemKernel<<<1, kMidT, mm * sizeof(double2), s>>>(Ain, lda, m, Vr,
+                                                             tau, d, e);
+  bisectKernel<<<(m + 63) / 64, 64, 0, s>>>(d, e, m, w);
+  invIterKernel<<<(m + 63) / 64, 64, 0, s>>>(d, e, m, w, Z, F);
+  clusterMgsKernel<<<m, kT, 0, s>>>(w, m, Z);
+  btColumnsKernel<<<(m + kBtWarps - 1) / kBtWarps, 32 * kBtWarps,
+                    kBtWarps * (size_t)m * sizeof(double2), s>>>(Z, m, Vr, tau,
+                                                                  V);
   finishKernel<<<(m + 255) / 256, 256, 0, s>>>(m, perm, status);
 }
 

@@ -754,7 +754,7 @@ static Shape tune(ncgm_ctx *ctx, int species, int ncols) {
     for (int yr : {1, 2, 4})
       for (int ring : {8, 16})
         for (int cring : {2, 4, 8})
-          for (int cps : {1, 2}) {
+          for (int cps : {1, 2, 3, 4}) {
             for (int nc : {1, 2})
               trial(Shape{TY, ring, yr, cps, 2, cring, nc});
             trial(Shape{TY, ring, yr, cps, 3, cring, 1});

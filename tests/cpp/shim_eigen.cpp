@@ -73,7 +73,7 @@ int main() {
   F.gradf = gradf.data();
   F.U = U.data();
   ncgm_ref::Hamiltonian H(grid, NCGM_NEUTRON, F);
-  const int nev = 2;
+  const int nev = 8;
   Eigen::MatrixXcd guess((std::ptrdiff_t)grid->get_total_points(), nev);
   for (std::ptrdiff_t r = 0; r < guess.size(); ++r)
     guess.data()[r] =

@@ -83,7 +83,7 @@ def test_eigen_overloads_solve_on_device(tmp_path):
     out = subprocess.run([exe], capture_output=True, text=True,
                          check=True).stdout.split("\n")
     words = out[1].split()
-    assert words[0] == "solved" and words[1] == "2" and words[2] == "2"
+    assert words[0] == "solved" and words[1] == "8" and words[2] == "8"
     # the harmonic-oscillator ground level 3/2 hbar w = 15 MeV
     assert float(words[3]) == pytest.approx(15.0, rel=5e-3)
-    assert words[4] == "2"
+    assert words[4] == "8"

@@ -15,15 +15,17 @@ total energy 1 keV, single-particle energies 1e-5 MeV, densities 1e-7 fm^-3
 max-abs (raw; the stored float32 densities carry < 1e-8 fm^-3 of rounding).
 
 The centre of mass is a near-zero mode of the lattice equations: a run
-that starts exactly symmetric (the oracle, the FP64 and the FP32 forms)
-stays at the symmetric fixed point, but the learned start of the PCG is not
-reflection symmetric and moves the nucleus by ~1e-4 fm, which then relaxes
-only very slowly. That form runs with the reference's own centre-of-mass
-constraint ("constrainCOM": XCMConstraint, src/skyrme/xcm_constraint.cpp:
-14-87, and its y, z forms). Its field 2C(Q - mu)x vanishes at the
-symmetric fixed point (Q = 0, multiplier 0), so the constrained and the
-unconstrained problems share that fixed point and the comparison is with
-the same stored one."""
+that starts exactly symmetric (the oracle and the FP64 form) stays at the
+symmetric fixed point, but any asymmetry of the arithmetic moves the
+nucleus, and the move relaxes only very slowly. The learned start of the
+PCG is not reflection symmetric (a shift of ~1e-4 fm), and the FP32 forms'
+roundings differ between mirror points (~1e-7 fm^-3 in rho after 500
+iterations). The reduced-precision forms therefore run with the
+reference's own centre-of-mass constraint ("constrainCOM": XCMConstraint,
+src/skyrme/xcm_constraint.cpp:14-87, and its y, z forms). Its field
+2C(Q - mu)x vanishes at the symmetric fixed point (Q = 0, multiplier 0), so
+the constrained and the unconstrained problems share that fixed point and
+the comparison is with the same stored one."""
 import os
 import sys
 
@@ -45,8 +47,8 @@ RHO_TOL = 1e-7   # fm^-3, max-abs
 
 # (name, precision, preconditioner, centre-of-mass constraint)
 FORMS = [("fp64", abi.FP64, abi.PRECOND_JACOBI, False),
-         ("fp32", abi.FP32, abi.PRECOND_JACOBI, False),
-         ("fp32_tc", abi.FP32_TC, abi.PRECOND_JACOBI, False),
+         ("fp32", abi.FP32, abi.PRECOND_JACOBI, True),
+         ("fp32_tc", abi.FP32_TC, abi.PRECOND_JACOBI, True),
          ("learned_fp32_tc", abi.FP32_TC, abi.PRECOND_LEARNED, True)]
 
 _LP = {}

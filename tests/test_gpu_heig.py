@@ -1,7 +1,9 @@
 """The projected Hermitian eigensolver (ncgm_heig) against numpy: the
-shared-memory Jacobi (m <= 80, FP64 and double-float rotations) and the
-multi-kernel tridiagonal solver (m > 80), on generic spectra and on
-time-reversal symmetric matrices whose levels are all twofold (Kramers)."""
+shared-memory Jacobi (m <= 80, FP64 and double-float rotations), the
+one-CTA Householder tridiagonalisation (NCGM_HEIG_MID=1, m <= 112, in a
+child process) and the multi-kernel tridiagonal solver (m > 80), on generic
+spectra and on time-reversal symmetric matrices whose levels are all twofold
+(Kramers)."""
 import numpy as np
 import pytest
 
@@ -25,6 +27,7 @@ def _herm(m, rng, kramers):
 
 @pytest.mark.parametrize("m,kramers,precision", [
     (24, False, abi.FP64), (60, True, abi.FP32), (80, False, abi.FP32_TC),
+    (2, False, abi.FP32), (24, True, abi.FP32), (48, False, abi.FP32_TC),
     (81, False, abi.FP64), (150, True, abi.FP64), (192, False, abi.FP32),
     (320, True, abi.FP64), (480, False, abi.FP64)])
 def test_heig_matches_numpy(m, kramers, precision):
@@ -45,3 +48,44 @@ def test_heig_matches_numpy(m, kramers, precision):
           "residual %.1e" % (m, kramers, eig, orth, res))
     assert eig <= 1e-12 and orth <= 1e-10 and res <= 1e-11
     ctx.close()
+
+
+_MID_CHILD = r"""
+import sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+import nuclearcgm_gb300 as ng
+from test_gpu_heig import _herm
+m, kramers, prec = int(sys.argv[2]), sys.argv[3] == "1", int(sys.argv[4])
+A = np.asfortranarray(_herm(m, np.random.default_rng(m + 7 * kramers), kramers))
+m = A.shape[0]
+ctx = ng.Context(ng.Grid(8, 3.0), 2)
+w = np.zeros(m)
+V = np.zeros((m, m), np.complex128, order="F")
+ng._check(ng.load().ncgm_heig(ctx.h, A.ctypes.data, m, w.ctypes.data,
+                              V.ctypes.data, prec))
+ref = np.linalg.eigvalsh(A)
+scale = np.abs(ref).max()
+print(np.abs(w - ref).max() / scale, np.abs(V.conj().T @ V - np.eye(m)).max(),
+      np.abs(A @ V - V * w).max() / scale)
+"""
+
+
+@pytest.mark.parametrize("m,kramers", [(2, False), (24, True), (60, True),
+                                       (80, False), (100, True), (112, False)])
+def test_heig_one_cta_householder(m, kramers):
+    """The one-CTA Householder method (NCGM_HEIG_MID=1 selects it for the
+    FP32 forms; the switch is read once per process, so a child runs it)."""
+    import os
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    env = dict(os.environ, NCGM_HEIG_MID="1")
+    out = subprocess.run([sys.executable, "-c", _MID_CHILD,
+                          os.path.dirname(here), str(m), str(int(kramers)),
+                          str(abi.FP32)], env=env, capture_output=True,
+                         text=True, cwd=here, check=True).stdout.split()
+    eig, orth, res = (float(x) for x in out)
+    print("one-CTA Householder m=%d kramers=%s: eigenvalues %.1e, "
+          "orthonormality %.1e, residual %.1e" % (m, kramers, eig, orth, res))
+    assert eig <= 1e-12 and orth <= 1e-10 and res <= 1e-11
