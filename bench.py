@@ -523,7 +523,7 @@ def run_ours(args):
         gstep = _gcg_step(H, X)
         hf = _hf_wall(not args.no_cpu)
         hf_ca = _hf_wall_ca40()
-        curve = _curve_cfg2()
+    curve = _curve_cfg2() if (rank == 0 and args.curve) else None
     sn = _hf_wall_sn120() if (rank == 0 and args.sn120) else None
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -576,6 +576,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true",
                     help="skip the CPU-baseline sample on our arm")
+    ap.add_argument("--curve", action="store_true",
+                    help="also time the 16-point 24Mg curve (about 8 minutes)")
     ap.add_argument("--sn120", action="store_true",
                     help="also time the 120Sn HFB run to 1 keV (minutes)")
     ap.add_argument("--no-hf", action="store_true",
