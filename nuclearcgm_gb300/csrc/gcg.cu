@@ -264,6 +264,10 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
     vcPart = ctx->buf(31, exactVCScratchBytes(vmax, vmax));
     if (!tcPart || !vcPart) return NCGM_ERR_NOMEM;
   }
+  // the projected eigensolver's workspace (Householder methods)
+  const size_t heigScrB = heigScratchBytes(mx);
+  void *heigScr = ctx->buf(32, heigScrB);
+  if (!heigScr) return NCGM_ERR_NOMEM;
   Carve ar{base};
   double2 *V = ar.take<double2>(N * vmax), *Q = ar.take<double2>(N * vmax),
           *AV = ar.take<double2>(N * vmax), *Q1 = ar.take<double2>(N * vmax);
@@ -334,7 +338,7 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
                   reinterpret_cast<double *>(tcPart), s);
     else
       gram(Xa, N, nx, AV, N, nx, N, Ap, nx, partials, (int)maxChunks, s);
-    heig(Ap, nx, nx, Cw, Ev, dW, dPerm, dStat, s, fp32);
+    heig(Ap, nx, nx, Cw, Ev, dW, dPerm, dStat, s, fp32, heigScr, heigScrB);
     if (tc)
       gemmVCExact(Xa, N, nx, Ev, nx, nx, Xn, N, N, vcPart, s);
     else
@@ -535,7 +539,7 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
                   reinterpret_cast<double *>(tcPart), s);
     else
       gram(Q, N, m, AV, N, m, N, Ap, m, partials, (int)maxChunks, s);
-    heig(Ap, m, m, Cw, Ev, dW, dPerm, dStat, s, fp32);
+    heig(Ap, m, m, Cw, Ev, dW, dPerm, dStat, s, fp32, heigScr, heigScrB);
     const int rr = std::min(nev, m);
     if (tc) {
       gemmVCExact(Q, N, m, Ev, m, rr, Xn, N, N, vcPart, s);

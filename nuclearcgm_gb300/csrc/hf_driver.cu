@@ -217,6 +217,8 @@ struct HfbWork {
   double2 *C = nullptr, *G = nullptr, *H = nullptr, *Hwork = nullptr,
           *Hv = nullptr, *rho = nullptr, *Wm = nullptr, *T = nullptr;
   int *perm = nullptr, *status = nullptr;
+  void *heigScr = nullptr; // the eigensolvers' workspace (up to 2M)
+  size_t heigScrB = 0;
   static constexpr int kChunks = 64;
 };
 
@@ -302,7 +304,10 @@ struct Run {
         if (!h->kappa) return nullptr;
       }
     w.gemmW = alloc<double2>(N * (size_t)M);
-    if (!w.gemmParts || !d || !c || !iw || !w.gemmW) return nullptr;
+    w.heigScrB = heigScratchBytes(2 * M);
+    w.heigScr = alloc<char>(w.heigScrB);
+    if (!w.gemmParts || !d || !c || !iw || !w.gemmW || !w.heigScr)
+      return nullptr;
     w.e = d;
     w.ff = w.e + M;
     w.eig = w.ff + M; // 2M
@@ -643,7 +648,8 @@ int hfbSpecies(Run &R, Species &S, int target, HFBRes &out) {
   const int m2 = 2 * nS;
   for (int it = 0; it < 100; ++it) {
     hfbMatrix(w->e, w->Delta, nS, cur, w->H, R.s);
-    heig(w->H, m2, m2, w->Hwork, w->Hv, w->eig, w->perm, w->status, R.s);
+    heig(w->H, m2, m2, w->Hwork, w->Hv, w->eig, w->perm, w->status, R.s,
+         false, w->heigScr, w->heigScrB);
     hfbExtract(w->Hv, nS, w->status, w->Uw, w->Vw, w->scal + 1, R.s);
     double num = 0;
     NCGM_TRY(readScalar(R, w->scal + 1, num));
@@ -740,7 +746,8 @@ int occupiedOrbitals(Run &R, int q, bool bcsOcc, int &ncols,
       return NCGM_ERR_NOMEM;
     }
     hfbDensityMatrix(S.hfb.V, M, w->rho, R.s);
-    heig(w->rho, M, M, w->Hwork, w->Wm, w->eig, w->perm, w->status, R.s);
+    heig(w->rho, M, M, w->Hwork, w->Wm, w->eig, w->perm, w->status, R.s,
+         false, w->heigScr, w->heigScrB);
     hfbNatural(w->Wm, w->eig, M, w->T, R.s);
     int st = 0;
     NCGM_CUDA(cudaMemcpyAsync(&st, w->status, sizeof(int),

@@ -10,6 +10,7 @@
 //  * heig:      one-CTA cyclic Jacobi Hermitian eigensolver reading the lower
 //               triangle (as SelfAdjointEigenSolver does), ascending order.
 #include "k_dense.cuh"
+#include "df64.cuh"
 
 #include <algorithm>
 #include <cstdlib>
@@ -381,37 +382,6 @@ __global__ void heigKernel(const double2 *Ain, int lda, int m, double2 *Ag,
 // sweeps stop at an off-diagonal norm of 3e-13 relative (the FP64 Jacobi
 // stops at 1e-16); the matrices are then converted in place to FP64 for the
 // output, and only if that level was not reached do FP64 sweeps continue.
-struct dfl {
-  float hi, lo;
-};
-struct dfc {
-  dfl re, im;
-};
-// The operations of the error-free transformations use the _rn intrinsics,
-// which the compiler never contracts into FMAs (a contracted p + e in the
-// product, for instance, loses the low part: 1e-9 instead of 1e-13).
-__device__ __forceinline__ dfl dfAdd(dfl a, dfl b) {
-  const float s = __fadd_rn(a.hi, b.hi);
-  const float v = __fsub_rn(s, a.hi);
-  float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)), __fsub_rn(b.hi, v));
-  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
-  const float h = __fadd_rn(s, e);
-  return {h, __fsub_rn(e, __fsub_rn(h, s))};
-}
-__device__ __forceinline__ dfl dfNeg(dfl a) { return {-a.hi, -a.lo}; }
-__device__ __forceinline__ dfl dfMul(dfl a, dfl b) {
-  const float p = __fmul_rn(a.hi, b.hi);
-  float e = fmaf(a.hi, b.hi, -p);
-  e = fmaf(a.hi, b.lo, e);
-  e = fmaf(a.lo, b.hi, e);
-  const float h = __fadd_rn(p, e);
-  return {h, __fsub_rn(e, __fsub_rn(h, p))};
-}
-__device__ __forceinline__ dfl dfFrom(double x) {
-  const float h = __double2float_rn(x);
-  return {h, __double2float_rn(__dsub_rn(x, (double)h))};
-}
-__device__ __forceinline__ double dfTo(dfl a) { return (double)a.hi + (double)a.lo; }
 // c x - s (w y), s x + c (w y) for complex x, y, w and real c, s
 __device__ __forceinline__ void dfRot(dfc &x, dfc &y, dfl c, dfl s, dfc w) {
   const dfc t = {dfAdd(dfMul(w.re, y.re), dfNeg(dfMul(w.im, y.im))),
@@ -831,8 +801,28 @@ static bool heigMidOn() {
   return v;
 }
 
+size_t heigScratchBytes(int m) {
+  return std::max(heigMidScratchBytes(m), heigLargeScratchBytes(m));
+}
+
 void heig(const double2 *A, int lda, int m, double2 *work, double2 *V,
-          double *w, int *perm, int *status, cudaStream_t s, bool fast) {
+          double *w, int *perm, int *status, cudaStream_t s, bool fast,
+          void *scratch, size_t scratchBytes) {
+  // the Householder methods' scratch: the caller's, or stream-ordered
+  auto withScratch = [&](size_t need, auto &&run) {
+    if (scratch && scratchBytes >= need) {
+      run(scratch);
+      return true;
+    }
+    void *scr = nullptr;
+    if (cudaMallocAsync(&scr, need, s) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    run(scr);
+    cudaFreeAsync(scr, s);
+    return true;
+  };
   // the round-robin tables hold up to 256 pairs (m <= 512)
   constexpr size_t kMaxDyn = 210 * 1024; // + 14 KB static <= 227 KB
   static const bool attr = [] {
@@ -841,16 +831,11 @@ void heig(const double2 *A, int lda, int m, double2 *work, double2 *V,
     return true;
   }();
   (void)attr;
-  if (fast && m <= heigMidMax() && !heigFp64Only() && heigMidOn()) {
-    // stream-ordered scratch, as the multi-kernel solver below
-    void *scr = nullptr;
-    if (cudaMallocAsync(&scr, heigMidScratchBytes(m), s) == cudaSuccess) {
-      heigMid(A, lda, m, V, w, perm, status, scr, s);
-      cudaFreeAsync(scr, s);
-      return;
-    }
-    cudaGetLastError();
-  }
+  if (fast && m <= heigMidMax() && !heigFp64Only() && heigMidOn() &&
+      withScratch(heigMidScratchBytes(m), [&](void *scr) {
+        heigMid(A, lda, m, V, w, perm, status, scr, s);
+      }))
+    return;
   if (fast && m <= kHeigDfMax && !heigFp64Only()) {
     static const bool dfAttr = [] {
       cudaFuncSetAttribute(heigDfKernel,
@@ -864,17 +849,13 @@ void heig(const double2 *A, int lda, int m, double2 *work, double2 *V,
         A, lda, m, V, w, perm, status);
     return;
   }
-  if (m > kHeigDfMax && !heigFp64Only()) {
-    // above the shared-memory tier: the multi-kernel solver over the whole
-    // GPU (stream-ordered scratch; concurrent contexts stay independent)
-    void *scr = nullptr;
-    if (cudaMallocAsync(&scr, heigLargeScratchBytes(m), s) == cudaSuccess) {
-      heigLarge(A, lda, m, V, w, perm, status, scr, s);
-      cudaFreeAsync(scr, s);
-      return;
-    }
-    cudaGetLastError();
-  }
+  // above the shared-memory tier: the multi-kernel solver over the whole
+  // GPU
+  if (m > kHeigDfMax && !heigFp64Only() &&
+      withScratch(heigLargeScratchBytes(m), [&](void *scr) {
+        heigLarge(A, lda, m, V, w, perm, status, scr, s);
+      }))
+    return;
   const size_t mat = (size_t)m * m * sizeof(double2);
   const int sm = 2 * mat <= kMaxDyn ? 2 : (mat <= kMaxDyn ? 1 : 0);
   const size_t smem = sm == 2 ? 2 * mat : (sm == 1 ? mat : 0);

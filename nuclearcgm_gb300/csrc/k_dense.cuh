@@ -60,8 +60,12 @@ int heigMidMax();
 // NCGM_HEIG_MID=1 the one-CTA Householder method up to heigMidMax();
 // otherwise the FP64 Jacobi up to m = 80 and the multi-kernel Householder
 // method above it.
+// scratch (optional, heigScratchBytes(m) bytes): the Householder methods'
+// workspace; without it they take stream-ordered allocations per call.
 void heig(const double2 *A, int lda, int m, double2 *work, double2 *V,
           double *w, int *perm, int *status, cudaStream_t s,
-          bool fast = false);
+          bool fast = false, void *scratch = nullptr,
+          size_t scratchBytes = 0);
+size_t heigScratchBytes(int m);
 
 } // namespace ncgm

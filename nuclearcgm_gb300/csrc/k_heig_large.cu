@@ -11,8 +11,8 @@
 //     (p^H v) v, and the rank-2 update A22 -= v w^H + w v^H over the whole
 //     grid. Reflectors H = I - tau v v^H with real beta (the LAPACK
 //     convention), so the tridiagonal matrix is real.
-//  2. Eigenvalues of the real tridiagonal by bisection on Sturm counts, one
-//     thread per eigenvalue.
+//  2. Eigenvalues of the real tridiagonal by multisection on Sturm counts,
+//     one warp per eigenvalue.
 //  3. Eigenvectors by inverse iteration (tridiagonal LU with partial
 //     pivoting, three solves from a hashed start vector), then modified
 //     Gram-Schmidt inside clusters of equal eigenvalues (Kramers pairs are
@@ -21,10 +21,12 @@
 // A numpy restatement of these steps gives eigenvalues to 2e-15 and
 // orthonormality to 7e-13 relative, also with twofold degenerate spectra.
 #include "k_dense.cuh"
+#include "df64.cuh"
 
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstdint>
 
 namespace ncgm {
@@ -182,7 +184,8 @@ __global__ void lastDiagKernel(const double2 *A, int m, double *d) {
     d[m - 1] = A[(size_t)(m - 1) * m + (m - 1)].x;
 }
 
-// number of eigenvalues of the tridiagonal (d, e) below x
+// number of eigenvalues of the tridiagonal (d, e) below x (the quotient
+// form of the Sturm sequence, with a pivot floor)
 __device__ int sturmCount(const double *d, const double *e, int m, double x,
                           double pivmin) {
   double q = d[0] - x;
@@ -195,13 +198,18 @@ __device__ int sturmCount(const double *d, const double *e, int m, double x,
   return c;
 }
 
-// eigenvalue j (ascending) by bisection; Gershgorin bounds
-__global__ void bisectKernel(const double *d, const double *e, int m,
-                             double *w) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+// eigenvalue j (ascending) by multisection from the Gershgorin bounds, one
+// warp per eigenvalue: each step the 32 lanes count the eigenvalues below
+// 32 equally spaced points of the bracket (Sturm counts), which shrinks it
+// 33-fold, so about 11 steps reach the 2.3e-16 relative tolerance where
+// bisection takes ~55
+__global__ void multisectKernel(const double *d, const double *e, int m,
+                                double *w) {
+  const int j = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const int lane = threadIdx.x % 32;
   if (j >= m) return;
   double lo = 1e300, hi = -1e300, emax = 0;
-  for (int i = 0; i < m; ++i) {
+  for (int i = lane; i < m; i += 32) {
     double r = 0;
     if (i > 0) r += fabs(e[i - 1]);
     if (i + 1 < m) r += fabs(e[i]);
@@ -209,18 +217,31 @@ __global__ void bisectKernel(const double *d, const double *e, int m,
     hi = fmax(hi, d[i] + r);
     if (i + 1 < m) emax = fmax(emax, fabs(e[i]));
   }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    emax = fmax(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+  }
   const double scale = fmax(fabs(lo), fabs(hi));
   const double pivmin = fmax(1e-300, 2.3e-308 * fmax(1.0, emax * emax));
   const double tol = 2.3e-16 * scale;
-  for (int it = 0; it < 256; ++it) {
-    const double mid = 0.5 * (lo + hi);
-    if (hi - lo <= 2.0 * tol || mid == lo || mid == hi) break;
-    if (sturmCount(d, e, m, mid, pivmin) <= j)
-      lo = mid;
-    else
-      hi = mid;
+  for (int it = 0; it < 64; ++it) {
+    if (hi - lo <= 2.0 * tol) break;
+    const double step = (hi - lo) / 33.0;
+    const double x = lo + (lane + 1) * step;
+    const bool below =
+        x > lo && x < hi && sturmCount(d, e, m, x, pivmin) <= j;
+    // the bracket is [x_k, x_{k+1}] for the last lane k whose point has at
+    // most j eigenvalues below it (the counts grow with the lane)
+    const unsigned mask = __ballot_sync(0xffffffffu, below);
+    const int k = mask ? 31 - __clz(mask) : -1;
+    const double nlo = k >= 0 ? lo + (k + 1) * step : lo;
+    const double nhi = k < 31 ? lo + (k + 2) * step : hi;
+    if (nlo == lo && nhi == hi) break; // no representable progress
+    lo = nlo;
+    hi = fmin(nhi, hi);
   }
-  w[j] = 0.5 * (lo + hi);
+  if (lane == 0) w[j] = 0.5 * (lo + hi);
 }
 
 __device__ __forceinline__ double hashUniform(uint64_t x) {
@@ -231,71 +252,79 @@ __device__ __forceinline__ double hashUniform(uint64_t x) {
   return (double)(x >> 11) * (2.0 / 9007199254740992.0) - 1.0;
 }
 
-// inverse iteration for eigenvalue j: three solves of (T - w_j) z = b by
-// Gaussian elimination with partial pivoting; column j of Z. The factor
-// rows live in column j of the scratch arrays F (3 x m x m).
+// inverse iteration for eigenvalue j: three solves of (T - w_j) z = b with
+// one LU factorisation with partial pivoting of the tridiagonal; column j of
+// Z. The factors live in column j of the scratch arrays F (5 x m x m): the
+// reciprocal pivots, the two upper diagonals of U, the multipliers and the
+// row swaps. Divisions (slow on the FP64 pipe) are made once per row in the
+// factorisation; the solves multiply.
 __global__ void invIterKernel(const double *d, const double *e, int m,
                               const double *w, double *Z, double *F) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= m) return;
-  double *bb = F + (size_t)j * m, *c = F + (size_t)m * m + (size_t)j * m,
-         *u2 = F + 2 * (size_t)m * m + (size_t)j * m;
+  // one eigenvalue per block (its FP64 chain on an SM of its own)
+  const int j = blockIdx.x;
+  if (j >= m || threadIdx.x != 0) return;
+  const size_t mm = (size_t)m * m;
+  double *rb = F + (size_t)j * m, *c = F + mm + (size_t)j * m,
+         *u2 = F + 2 * mm + (size_t)j * m, *l = F + 3 * mm + (size_t)j * m,
+         *sw = F + 4 * mm + (size_t)j * m;
   double *z = Z + (size_t)j * m;
   double scale = 0;
   for (int i = 0; i < m; ++i) scale = fmax(scale, fabs(d[i]));
   for (int i = 0; i + 1 < m; ++i) scale = fmax(scale, fabs(e[i]));
   const double eps = 2.3e-16 * fmax(scale, 1e-300);
   const double lam = w[j];
-  // factor T - lam once: rows i hold (bb, c, u2) after elimination; the
-  // multipliers and swaps are recorded in sign of a row flag (l stored in z
-  // scratch is avoided by redoing the elimination on the right-hand side)
-  for (int i = 0; i < m; ++i) {
-    bb[i] = d[i] - lam;
-    c[i] = (i + 1 < m) ? e[i] : 0.0;
-    u2[i] = 0.0;
-    z[i] = hashUniform(((uint64_t)j << 32) ^ (uint64_t)i);
-  }
-  // elimination with the right-hand side carried along (three solves: the
-  // factorisation is repeated, O(m) each)
-  for (int rep = 0; rep < 3; ++rep) {
+  // factorisation: row i of U is (b0, c0, u0) after elimination
+  {
     double b0 = d[0] - lam, c0 = m > 1 ? e[0] : 0.0, u0 = 0.0;
-    double y0 = z[0];
     for (int i = 0; i + 1 < m; ++i) {
-      // row i: (b0, c0, u0 | y0); row i+1: (a1 = e[i], b1, c1 | y1)
       double a1 = e[i], b1 = d[i + 1] - lam, c1 = (i + 2 < m) ? e[i + 1] : 0.0;
-      double y1 = z[i + 1], u1 = 0.0;
-      if (fabs(a1) > fabs(b0)) {
-        // swap rows i and i+1
+      double u1 = 0.0;
+      const bool swap = fabs(a1) > fabs(b0);
+      if (swap) {
         double t;
         t = b0; b0 = a1; a1 = t;
         t = c0; c0 = b1; b1 = t;
         t = u0; u0 = c1; c1 = t;
-        t = y0; y0 = y1; y1 = t;
       }
       if (b0 == 0.0) b0 = eps;
-      const double l = a1 / b0;
-      b1 -= l * c0;
-      c1 -= l * u0;
-      y1 -= l * y0;
-      bb[i] = b0;
+      const double li = a1 / b0;
+      b1 -= li * c0;
+      c1 -= li * u0;
+      rb[i] = 1.0 / b0;
       c[i] = c0;
       u2[i] = u0;
-      z[i] = y0;
+      l[i] = li;
+      sw[i] = swap ? 1.0 : 0.0;
       b0 = b1;
       c0 = c1;
       u0 = u1;
-      y0 = y1;
     }
     if (b0 == 0.0) b0 = eps;
-    bb[m - 1] = b0;
+    rb[m - 1] = 1.0 / b0;
+  }
+  for (int i = 0; i < m; ++i)
+    z[i] = hashUniform(((uint64_t)j << 32) ^ (uint64_t)i);
+  for (int rep = 0; rep < 3; ++rep) {
+    // forward: the recorded swaps and multipliers on the right-hand side
+    double y0 = z[0];
+    for (int i = 0; i + 1 < m; ++i) {
+      double y1 = z[i + 1];
+      if (sw[i] != 0.0) {
+        const double t = y0;
+        y0 = y1;
+        y1 = t;
+      }
+      z[i] = y0;
+      y0 = y1 - l[i] * y0;
+    }
     z[m - 1] = y0;
     // back substitution
     double nrm = 0;
     for (int i = m - 1; i >= 0; --i) {
-      double s = z[i];
-      if (i + 1 < m) s -= c[i] * z[i + 1];
-      if (i + 2 < m) s -= u2[i] * z[i + 2];
-      z[i] = s / bb[i];
+      double sacc = z[i];
+      if (i + 1 < m) sacc -= c[i] * z[i + 1];
+      if (i + 2 < m) sacc -= u2[i] * z[i + 2];
+      z[i] = sacc * rb[i];
       nrm += z[i] * z[i];
     }
     const double inv = 1.0 / sqrt(nrm);
@@ -450,10 +479,158 @@ __global__ void __launch_bounds__(kMidT, 1)
   if (tid == 0) d[m - 1] = Ash[(size_t)(m - 1) * m + (m - 1)].x;
 }
 
+// sum over the block with two barriers: warp shuffles, then the warps'
+// partial sums (red: 32 doubles per value)
+__device__ __forceinline__ double2 blockSum2(double a, double b, double *red) {
+  const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  if (lane == 0) {
+    red[warp] = a;
+    red[32 + warp] = b;
+  }
+  __syncthreads();
+  // one warp sums the warps' partials (FP64 work stays off the other 15
+  // warps: the FP64 pipe retires 2 operations per clock per SM)
+  if (warp == 0) {
+    const int nw = blockDim.x / 32;
+    double ra = lane < nw ? red[lane] : 0.0;
+    double rb = lane < nw ? red[32 + lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      ra += __shfl_xor_sync(0xffffffffu, ra, o);
+      rb += __shfl_xor_sync(0xffffffffu, rb, o);
+    }
+    if (lane == 0) {
+      red[0] = ra;
+      red[32] = rb;
+    }
+  }
+  __syncthreads();
+  const double2 r = make_double2(red[0], red[32]);
+  __syncthreads();
+  return r;
+}
+
+// The same reduction as hhTridiagSmemKernel with the matrix held in
+// double-float (df64) form: the O(L^2) parts of a step (the matrix-vector
+// product and the rank-2 update) run on the FP32 pipe, the O(L) parts (the
+// reflector, p^H v, w) in FP64. About 1e-14 relative accuracy of the
+// tridiagonal form.
+__global__ void __launch_bounds__(kMidT, 1)
+    hhTridiagDfKernel(const double2 *Ain, int lda, int m, double2 *Vr,
+                      double2 *tau, double *d, double *e) {
+  extern __shared__ dfc Adf[];
+  __shared__ dfc vsd[kMidMax], wsd[kMidMax];
+  __shared__ double2 v64[kMidMax], p64[kMidMax];
+  __shared__ double red[64];
+  __shared__ double2 sc;
+  __shared__ int skip;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int warp = tid / 32, lane = tid % 32, nw = nt / 32;
+  for (int q = tid; q < m * m; q += nt) {
+    const int i = q % m, j = q / m;
+    double2 v;
+    if (i > j) v = Ain[(size_t)j * lda + i];
+    else if (i < j) {
+      const double2 l = Ain[(size_t)i * lda + j];
+      v = make_double2(l.x, -l.y);
+    } else v = make_double2(Ain[(size_t)j * lda + i].x, 0.0);
+    Adf[q] = dfcFrom(v);
+  }
+  __syncthreads();
+  for (int k = 0; k + 1 < m; ++k) {
+    const int L = m - k - 1;
+    const dfc *x = Adf + (size_t)k * m + k + 1;
+    double loc = 0;
+    for (int i = 1 + tid; i < L; i += nt) {
+      const double2 xi = dfcTo(x[i]);
+      loc += xi.x * xi.x + xi.y * xi.y;
+    }
+    const double xn2 = blockSum2(loc, 0.0, red).x;
+    if (tid == 0) {
+      const double2 al = dfcTo(x[0]);
+      d[k] = dfTo(Adf[(size_t)k * m + k].re);
+      if (xn2 == 0.0 && al.y == 0.0) {
+        tau[k] = make_double2(0.0, 0.0);
+        e[k] = al.x;
+        skip = 1;
+      } else {
+        const double beta =
+            -(al.x >= 0.0 ? 1.0 : -1.0) * sqrt(al.x * al.x + al.y * al.y + xn2);
+        tau[k] = make_double2((beta - al.x) / beta, -al.y / beta);
+        e[k] = beta;
+        const double2 den = make_double2(al.x - beta, al.y);
+        const double dd = den.x * den.x + den.y * den.y;
+        sc = make_double2(den.x / dd, -den.y / dd);
+        skip = 0;
+      }
+    }
+    __syncthreads();
+    const bool sk = skip != 0;
+    const double2 t = tau[k];
+    double2 *vg = Vr + (size_t)k * m;
+    for (int i = tid; i < m; i += nt) {
+      double2 r = make_double2(0.0, 0.0);
+      if (!sk && i > k) r = (i == k + 1) ? make_double2(1.0, 0.0)
+                                         : cmulD(dfcTo(x[i - k - 1]), sc);
+      vg[i] = r;
+      if (i > k) {
+        v64[i - k - 1] = r;
+        vsd[i - k - 1] = dfcFrom(r);
+      }
+    }
+    __syncthreads();
+    if (sk || L < 2) continue; // uniform: skip and L are shared
+    // p = tau A22 v in df64, one warp per row (column i, conjugated)
+    for (int i = warp; i < L; i += nw) {
+      const dfc *col = Adf + (size_t)(k + 1 + i) * m + k + 1;
+      dfc acc = {{0.f, 0.f}, {0.f, 0.f}};
+      for (int j = lane; j < L; j += 32)
+        acc = dfcAdd(acc, dfcConjMul(col[j], vsd[j]));
+      for (int o = 16; o > 0; o >>= 1) {
+        dfc oth;
+        oth.re.hi = __shfl_xor_sync(0xffffffffu, acc.re.hi, o);
+        oth.re.lo = __shfl_xor_sync(0xffffffffu, acc.re.lo, o);
+        oth.im.hi = __shfl_xor_sync(0xffffffffu, acc.im.hi, o);
+        oth.im.lo = __shfl_xor_sync(0xffffffffu, acc.im.lo, o);
+        acc = dfcAdd(acc, oth);
+      }
+      if (lane == 0) p64[i] = cmulD(t, dfcTo(acc));
+    }
+    __syncthreads();
+    // w = p - tau/2 (p^H v) v (FP64), then its df64 copy
+    double re = 0, im = 0;
+    for (int i = tid; i < L; i += nt) {
+      const double2 pv = cconjmulD(p64[i], v64[i]);
+      re += pv.x;
+      im += pv.y;
+    }
+    const double2 pv = blockSum2(re, im, red);
+    const double2 a2 = cmulD(make_double2(-0.5 * t.x, -0.5 * t.y), pv);
+    for (int i = tid; i < L; i += nt) {
+      const double2 av = cmulD(a2, v64[i]);
+      wsd[i] = dfcFrom(make_double2(p64[i].x + av.x, p64[i].y + av.y));
+    }
+    __syncthreads();
+    // A22[i][j] -= v_i conj(w_j) + w_i conj(v_j)
+    for (int q = tid; q < L * L; q += nt) {
+      const int i = q % L, j = q / L;
+      const dfc u = dfcAdd(dfcMulConj(vsd[i], wsd[j]),
+                           dfcMulConj(wsd[i], vsd[j]));
+      dfc &y = Adf[(size_t)(k + 1 + j) * m + (k + 1 + i)];
+      y = dfcSub(y, u);
+    }
+    __syncthreads();
+  }
+  if (tid == 0) d[m - 1] = dfTo(Adf[(size_t)(m - 1) * m + (m - 1)].re);
+}
+
 // X = H_0 H_1 ... H_{m-2} Z for the real tridiagonal eigenvectors Z, one
 // warp per column with the column in shared memory: the reflectors are
 // applied from the last to the first (y = v_k^H x, x -= tau_k v_k y)
-constexpr int kBtWarps = 2;
+constexpr int kBtWarps = 1; // a column per SM: FP64-pipe bound
 __global__ void __launch_bounds__(32 * kBtWarps)
     btColumnsKernel(const double *Z, int m, const double2 *Vr,
                     const double2 *tau, double2 *X) {
@@ -507,7 +684,7 @@ size_t heigLargeScratchBytes(int m) {
          + (size_t)m * sizeof(double2)           // Wv
          + (size_t)m * sizeof(double2)           // tau
          + 2 * (size_t)m * sizeof(double)        // d, e
-         + 4 * mm * sizeof(double) + 1024;       // Z, F (3)
+         + 6 * mm * sizeof(double) + 1024;       // Z, F (5)
 }
 
 // w ascending, V eigenvectors (m x m, column-major); scratch holds
@@ -529,7 +706,7 @@ void heigLarge(const double2 *Ain, int lda, int m, double2 *V, double *w,
   double *d = reinterpret_cast<double *>(take(m * sizeof(double)));
   double *e = reinterpret_cast<double *>(take(m * sizeof(double)));
   double *Z = reinterpret_cast<double *>(take(mm * sizeof(double)));
-  double *F = reinterpret_cast<double *>(take(3 * mm * sizeof(double)));
+  double *F = reinterpret_cast<double *>(take(5 * mm * sizeof(double)));
   const unsigned gm = (unsigned)((mm + kT - 1) / kT);
   fullCopyKernel<<<gm, kT, 0, s>>>(Ain, lda, m, A);
   for (int k = 0; k + 1 < m; ++k) {
@@ -542,8 +719,8 @@ void heigLarge(const double2 *Ain, int lda, int m, double2 *V, double *w,
                                                             tau);
   }
   lastDiagKernel<<<1, 32, 0, s>>>(A, m, d);
-  bisectKernel<<<(m + 63) / 64, 64, 0, s>>>(d, e, m, w);
-  invIterKernel<<<(m + 63) / 64, 64, 0, s>>>(d, e, m, w, Z, F);
+  multisectKernel<<<m, 32, 0, s>>>(d, e, m, w);
+  invIterKernel<<<m, 32, 0, s>>>(d, e, m, w, Z, F);
   clusterMgsKernel<<<m, kT, 0, s>>>(w, m, Z);
   btColumnsKernel<<<(m + kBtWarps - 1) / kBtWarps, 32 * kBtWarps,
                     kBtWarps * (size_t)m * sizeof(double2), s>>>(Z, m, Vr, tau,
@@ -551,17 +728,26 @@ void heigLarge(const double2 *Ain, int lda, int m, double2 *V, double *w,
   finishKernel<<<(m + 255) / 256, 256, 0, s>>>(m, perm, status);
 }
 
+// NCGM_HEIG_MID_FP64=1 keeps the FP64 reduction (comparisons)
+static bool heigMidFp64() {
+  static const bool v = [] {
+    const char *e = std::getenv("NCGM_HEIG_MID_FP64");
+    return e && e[0] == '1';
+  }();
+  return v;
+}
+
 size_t heigMidScratchBytes(int m) {
   const size_t mm = (size_t)m * m;
   return mm * sizeof(double2) + 256         // Vr
          + (size_t)m * sizeof(double2) + 256 // tau
          + 2 * ((size_t)m * sizeof(double) + 256) // d, e
-         + 4 * mm * sizeof(double) + 1024;  // Z, F (3)
+         + 6 * mm * sizeof(double) + 1024;  // Z, F (5)
 }
 int heigMidMax() { return kMidMax; }
 
 // The Householder method of heigLarge with the tridiagonalisation in one CTA
-// (m <= kMidMax): one launch for the reduction, bisection, inverse
+// (m <= kMidMax): one launch for the reduction, then multisection, inverse
 // iteration, cluster orthogonalisation and the per-column
 // back-transformation.
 void heigMid(const double2 *Ain, int lda, int m, double2 *V, double *w,
@@ -578,16 +764,24 @@ void heigMid(const double2 *Ain, int lda, int m, double2 *V, double *w,
   double *d = reinterpret_cast<double *>(take(m * sizeof(double)));
   double *e = reinterpret_cast<double *>(take(m * sizeof(double)));
   double *Z = reinterpret_cast<double *>(take(mm * sizeof(double)));
-  double *F = reinterpret_cast<double *>(take(3 * mm * sizeof(double)));
+  double *F = reinterpret_cast<double *>(take(5 * mm * sizeof(double)));
   // the dynamic shared-memory limit is a per-device attribute: set on every
   // call (a driver call of about a microsecond)
-  cudaFuncSetAttribute(hhTridiagSmemKernel,
-                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       kMidMax * kMidMax * (int)sizeof(double2));
-  hhTridiagSmemKernel<<<1, kMidT, mm * sizeof(double2), s>>>(Ain, lda, m, Vr,
-                                                             tau, d, e);
-  bisectKernel<<<(m + 63) / 64, 64, 0, s>>>(d, e, m, w);
-  invIterKernel<<<(m + 63) / 64, 64, 0, s>>>(d, e, m, w, Z, F);
+  if (heigMidFp64()) {
+    cudaFuncSetAttribute(hhTridiagSmemKernel,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kMidMax * kMidMax * (int)sizeof(double2));
+    hhTridiagSmemKernel<<<1, kMidT, mm * sizeof(double2), s>>>(Ain, lda, m,
+                                                               Vr, tau, d, e);
+  } else {
+    cudaFuncSetAttribute(hhTridiagDfKernel,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kMidMax * kMidMax * (int)sizeof(dfc));
+    hhTridiagDfKernel<<<1, kMidT, mm * sizeof(dfc), s>>>(Ain, lda, m, Vr, tau,
+                                                         d, e);
+  }
+  multisectKernel<<<m, 32, 0, s>>>(d, e, m, w);
+  invIterKernel<<<m, 32, 0, s>>>(d, e, m, w, Z, F);
   clusterMgsKernel<<<m, kT, 0, s>>>(w, m, Z);
   btColumnsKernel<<<(m + kBtWarps - 1) / kBtWarps, 32 * kBtWarps,
                     kBtWarps * (size_t)m * sizeof(double2), s>>>(Z, m, Vr, tau,
