@@ -42,6 +42,33 @@ __device__ __forceinline__ dfl dfFrom(double x) {
 }
 __device__ __forceinline__ double dfTo(dfl a) { return (double)a.hi + (double)a.lo; }
 __device__ __forceinline__ dfl dfSub(dfl a, dfl b) { return dfAdd(a, dfNeg(b)); }
+// a / b: the FP32 quotient of the leading parts, then one correction from
+// the double-float residual a - b q1 (long division in base 2^24); about
+// 44 correct bits
+__device__ __forceinline__ dfl dfDiv(dfl a, dfl b) {
+  const float r = __frcp_rn(b.hi);
+  const float q1 = __fmul_rn(a.hi, r);
+  // p = b q1 exactly as a double-float, then the residual
+  const float ph = __fmul_rn(b.hi, q1);
+  float pl = fmaf(b.hi, q1, -ph);
+  pl = fmaf(b.lo, q1, pl);
+  const dfl rem = dfAdd(a, dfNeg(dfl{ph, pl}));
+  const float q2 = __fmul_rn(rem.hi, r);
+  const float h = __fadd_rn(q1, q2);
+  return {h, __fsub_rn(q2, __fsub_rn(h, q1))};
+}
+// sqrt(a) for a >= 0: the FP32 root of the leading part, one Newton
+// correction in double-float
+__device__ __forceinline__ dfl dfSqrt(dfl a) {
+  if (a.hi <= 0.f) return {0.f, 0.f};
+  const float s = sqrtf(a.hi);
+  const float sh = __fmul_rn(s, s);
+  float sl = fmaf(s, s, -sh);
+  const dfl rem = dfAdd(a, dfNeg(dfl{sh, sl}));
+  const float c = __fmul_rn(rem.hi, __frcp_rn(2.f * s));
+  const float h = __fadd_rn(s, c);
+  return {h, __fsub_rn(c, __fsub_rn(h, s))};
+}
 __device__ __forceinline__ dfc dfcFrom(double2 v) {
   return {dfFrom(v.x), dfFrom(v.y)};
 }

@@ -630,10 +630,15 @@ __global__ void cholDropSmemKernel(const double2 *G, int ldg, int m,
     __syncthreads();
     const double pv = piv;
     if (pv > 0.0) {
-      const double rjj = sqrt(pv);
+      // sqrt(pv) and its reciprocal in double-float (about 1e-14 relative;
+      // the second CholQR pass absorbs it): an FP64 square root or quotient
+      // takes ~650 cycles on GB300 and these sit on the critical path
+      const dfl sq = dfSqrt(dfFrom(pv));
+      const double rjj = dfTo(sq);
+      const double inv = dfTo(dfDiv(dfl{1.f, 0.f}, sq));
       for (int i = j + 1 + tid; i < m; i += nt) {
         const double2 a = A[(size_t)i * m + j];
-        A[(size_t)i * m + j] = make_double2(a.x / rjj, a.y / rjj);
+        A[(size_t)i * m + j] = make_double2(a.x * inv, a.y * inv);
       }
       if (tid == 0) A[(size_t)j * m + j] = make_double2(rjj, 0.0);
       __syncthreads();
@@ -652,20 +657,47 @@ __global__ void cholDropSmemKernel(const double2 *G, int ldg, int m,
     }
     __syncthreads();
   }
-  // T = R^{-1} on the kept columns, one thread per column of T
+  // T = R^{-1} on the kept columns, one thread per column of T. The
+  // reciprocal diagonal comes first (one quotient per row, in parallel); the
+  // row sums run in four independent partial sums, so the FP64 add chain
+  // (64-cycle latency) is a quarter as long. Dropped rows and columns hold
+  // zeros in R (and T starts at zero), so they add nothing to the sums.
+  for (int i = tid; i < m; i += nt)
+    gd[i] = kp[i] ? 1.0 / A[(size_t)i * m + i].x : 0.0;
+  __syncthreads();
   for (int c = tid; c < m; c += nt) {
     if (!kp[c]) continue;
     for (int i = c; i >= 0; --i) {
       if (!kp[i]) continue;
-      double2 sum = make_double2(i == c ? 1.0 : 0.0, 0.0);
-      for (int k = i + 1; k <= c; ++k) {
-        if (!kp[k]) continue;
-        const double2 t = cmul(A[(size_t)k * m + i], Ts[(size_t)c * m + k]);
-        sum.x -= t.x;
-        sum.y -= t.y;
+      double2 s0 = make_double2(i == c ? 1.0 : 0.0, 0.0);
+      double2 s1 = make_double2(0.0, 0.0), s2 = s1, s3 = s1;
+      int k = i + 1;
+      for (; k + 3 <= c; k += 4) {
+        const double2 t0 = cmul(A[(size_t)k * m + i], Ts[(size_t)c * m + k]);
+        const double2 t1 =
+            cmul(A[(size_t)(k + 1) * m + i], Ts[(size_t)c * m + k + 1]);
+        const double2 t2 =
+            cmul(A[(size_t)(k + 2) * m + i], Ts[(size_t)c * m + k + 2]);
+        const double2 t3 =
+            cmul(A[(size_t)(k + 3) * m + i], Ts[(size_t)c * m + k + 3]);
+        s0.x -= t0.x;
+        s0.y -= t0.y;
+        s1.x -= t1.x;
+        s1.y -= t1.y;
+        s2.x -= t2.x;
+        s2.y -= t2.y;
+        s3.x -= t3.x;
+        s3.y -= t3.y;
       }
-      const double rii = A[(size_t)i * m + i].x;
-      Ts[(size_t)c * m + i] = make_double2(sum.x / rii, sum.y / rii);
+      for (; k <= c; ++k) {
+        const double2 t = cmul(A[(size_t)k * m + i], Ts[(size_t)c * m + k]);
+        s0.x -= t.x;
+        s0.y -= t.y;
+      }
+      const double r = gd[i];
+      Ts[(size_t)c * m + i] = make_double2(
+          ((s0.x + s1.x) + (s2.x + s3.x)) * r,
+          ((s0.y + s1.y) + (s2.y + s3.y)) * r);
     }
   }
   __syncthreads();
@@ -790,13 +822,13 @@ static bool heigFp64Only() {
   return v;
 }
 
-// NCGM_HEIG_MID=1 selects the one-CTA Householder method (heigMid) for the
-// fast path's projected problems up to heigMidMax() instead of the
-// double-float Jacobi (comparisons)
+// NCGM_HEIG_MID=0 keeps the double-float Jacobi for the fast path's
+// projected problems up to m = 80 instead of the one-CTA Householder method
+// (comparisons)
 static bool heigMidOn() {
   static const bool v = [] {
     const char *e = std::getenv("NCGM_HEIG_MID");
-    return e && e[0] == '1';
+    return !(e && e[0] == '0');
   }();
   return v;
 }

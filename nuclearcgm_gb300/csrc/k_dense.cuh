@@ -54,12 +54,11 @@ void heigMid(const double2 *A, int lda, int m, double2 *V, double *w,
 size_t heigMidScratchBytes(int m);
 int heigMidMax();
 // Hermitian eigensolver (lower triangle): w ascending, V eigenvectors (m x m).
-// fast (the FP32 precision forms): for m <= 80, double-float sweeps finished
-// by FP64 sweeps (same accuracy, a different rounding path, so degenerate
-// eigenvectors may come out rotated within their eigenspace), or with
-// NCGM_HEIG_MID=1 the one-CTA Householder method up to heigMidMax();
-// otherwise the FP64 Jacobi up to m = 80 and the multi-kernel Householder
-// method above it.
+// fast (the FP32 precision forms): for m <= heigMidMax(), the one-CTA
+// double-float Householder method (heigMid; with NCGM_HEIG_MID=0 the
+// double-float Jacobi up to m = 80); otherwise the FP64 Jacobi up to m = 80
+// and the multi-kernel Householder method above it. Degenerate eigenvectors
+// may come out rotated within their eigenspace between the methods.
 // scratch (optional, heigScratchBytes(m) bytes): the Householder methods'
 // workspace; without it they take stream-ordered allocations per call.
 void heig(const double2 *A, int lda, int m, double2 *work, double2 *V,

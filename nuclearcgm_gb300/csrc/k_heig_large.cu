@@ -332,6 +332,68 @@ __global__ void invIterKernel(const double *d, const double *e, int m,
   }
 }
 
+// The same multisection with the Sturm counts in double-float arithmetic
+// (heigMid): a quotient costs a few dependent FP32 operations where an FP64
+// division takes ~600 cycles on GB300. The bracket stops at 2^-44 of the
+// spectrum's scale (the double-float resolution), so the eigenvalues are good
+// to about 1e-13 relative. d, e2: the diagonal and the squared off-diagonal
+// in double-float (dfl), staged in shared memory.
+constexpr int kDfSturmMax = 512;
+__global__ void __launch_bounds__(32)
+    multisectDfKernel(const double *d, const double *e, int m, double *w) {
+  __shared__ dfl dd[kDfSturmMax], ee[kDfSturmMax];
+  const int j = blockIdx.x, lane = threadIdx.x;
+  if (j >= m) return;
+  double lo = 1e300, hi = -1e300, emax = 0;
+  for (int i = lane; i < m; i += 32) {
+    double r = 0;
+    if (i > 0) r += fabs(e[i - 1]);
+    if (i + 1 < m) r += fabs(e[i]);
+    lo = fmin(lo, d[i] - r);
+    hi = fmax(hi, d[i] + r);
+    dd[i] = dfFrom(d[i]);
+    if (i + 1 < m) {
+      emax = fmax(emax, fabs(e[i]));
+      const dfl ei = dfFrom(e[i]);
+      ee[i] = dfMul(ei, ei);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    emax = fmax(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+  }
+  __syncwarp();
+  const double scale = fmax(fabs(lo), fabs(hi));
+  const float pivmin = (float)fmax(1e-30, 5.7e-14 * fmax(1.0, emax * emax));
+  const double tol = 5.7e-14 * scale;
+  for (int it = 0; it < 64; ++it) {
+    if (hi - lo <= 2.0 * tol) break;
+    const double step = (hi - lo) / 33.0;
+    const double x = lo + (lane + 1) * step;
+    bool below = false;
+    if (x > lo && x < hi) {
+      const dfl xd = dfFrom(x);
+      dfl q = dfSub(dd[0], xd);
+      int c = q.hi < 0.f ? 1 : 0;
+      for (int i = 1; i < m; ++i) {
+        if (fabsf(q.hi) < pivmin) q = {-pivmin, 0.f};
+        q = dfSub(dfSub(dd[i], xd), dfDiv(ee[i - 1], q));
+        if (q.hi < 0.f) ++c;
+      }
+      below = c <= j;
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, below);
+    const int k = mask ? 31 - __clz(mask) : -1;
+    const double nlo = k >= 0 ? lo + (k + 1) * step : lo;
+    const double nhi = k < 31 ? lo + (k + 2) * step : hi;
+    if (nlo == lo && nhi == hi) break;
+    lo = nlo;
+    hi = fmin(nhi, hi);
+  }
+  if (lane == 0) w[j] = 0.5 * (lo + hi);
+}
+
 // modified Gram-Schmidt inside each cluster of equal eigenvalues (one block
 // per cluster head)
 __global__ void clusterMgsKernel(const double *w, int m, double *Z) {
@@ -515,9 +577,9 @@ __device__ __forceinline__ double2 blockSum2(double a, double b, double *red) {
 
 // The same reduction as hhTridiagSmemKernel with the matrix held in
 // double-float (df64) form: the O(L^2) parts of a step (the matrix-vector
-// product and the rank-2 update) run on the FP32 pipe, the O(L) parts (the
-// reflector, p^H v, w) in FP64. About 1e-14 relative accuracy of the
-// tridiagonal form.
+// product, one thread per row, and the rank-2 update) and the reflector's
+// square root and quotients run on the FP32 pipe; p^H v and w in FP64.
+// About 1e-14 relative accuracy of the tridiagonal form.
 __global__ void __launch_bounds__(kMidT, 1)
     hhTridiagDfKernel(const double2 *Ain, int lda, int m, double2 *Vr,
                       double2 *tau, double *d, double *e) {
@@ -525,10 +587,9 @@ __global__ void __launch_bounds__(kMidT, 1)
   __shared__ dfc vsd[kMidMax], wsd[kMidMax];
   __shared__ double2 v64[kMidMax], p64[kMidMax];
   __shared__ double red[64];
-  __shared__ double2 sc;
+  __shared__ double2 sc, taus;
   __shared__ int skip;
   const int tid = threadIdx.x, nt = blockDim.x;
-  const int warp = tid / 32, lane = tid % 32, nw = nt / 32;
   for (int q = tid; q < m * m; q += nt) {
     const int i = q % m, j = q / m;
     double2 v;
@@ -550,54 +611,64 @@ __global__ void __launch_bounds__(kMidT, 1)
     }
     const double xn2 = blockSum2(loc, 0.0, red).x;
     if (tid == 0) {
-      const double2 al = dfcTo(x[0]);
+      // the reflector in double-float: an FP64 square root or quotient takes
+      // ~650 cycles on GB300's FP64 pipe
+      const dfc al = x[0];
       d[k] = dfTo(Adf[(size_t)k * m + k].re);
-      if (xn2 == 0.0 && al.y == 0.0) {
+      if (xn2 == 0.0 && al.im.hi == 0.f) {
         tau[k] = make_double2(0.0, 0.0);
-        e[k] = al.x;
+        taus = make_double2(0.0, 0.0);
+        e[k] = dfTo(al.re);
         skip = 1;
       } else {
-        const double beta =
-            -(al.x >= 0.0 ? 1.0 : -1.0) * sqrt(al.x * al.x + al.y * al.y + xn2);
-        tau[k] = make_double2((beta - al.x) / beta, -al.y / beta);
-        e[k] = beta;
-        const double2 den = make_double2(al.x - beta, al.y);
-        const double dd = den.x * den.x + den.y * den.y;
-        sc = make_double2(den.x / dd, -den.y / dd);
+        const dfl n2 = dfAdd(dfAdd(dfMul(al.re, al.re), dfMul(al.im, al.im)),
+                             dfFrom(xn2));
+        dfl beta = dfSqrt(n2);
+        if (al.re.hi >= 0.f) beta = dfNeg(beta);
+        const dfl rb = dfDiv(dfl{1.f, 0.f}, beta);
+        const double2 tv = make_double2(dfTo(dfMul(dfSub(beta, al.re), rb)),
+                                        -dfTo(dfMul(al.im, rb)));
+        tau[k] = tv;
+        taus = tv;
+        e[k] = dfTo(beta);
+        const dfl dr = dfSub(al.re, beta);
+        const dfl rdd = dfDiv(dfl{1.f, 0.f},
+                              dfAdd(dfMul(dr, dr), dfMul(al.im, al.im)));
+        sc = make_double2(dfTo(dfMul(dr, rdd)), -dfTo(dfMul(al.im, rdd)));
         skip = 0;
       }
     }
     __syncthreads();
     const bool sk = skip != 0;
-    const double2 t = tau[k];
-    double2 *vg = Vr + (size_t)k * m;
+    const double2 t = taus;
+    // the reflectors go out in double-float form (a dfc is 16 bytes, as a
+    // double2) for the double-float back-transformation
+    dfc *vg = reinterpret_cast<dfc *>(Vr) + (size_t)k * m;
     for (int i = tid; i < m; i += nt) {
       double2 r = make_double2(0.0, 0.0);
       if (!sk && i > k) r = (i == k + 1) ? make_double2(1.0, 0.0)
                                          : cmulD(dfcTo(x[i - k - 1]), sc);
-      vg[i] = r;
+      const dfc rd = dfcFrom(r);
+      vg[i] = rd;
       if (i > k) {
         v64[i - k - 1] = r;
-        vsd[i - k - 1] = dfcFrom(r);
+        vsd[i - k - 1] = rd;
       }
     }
     __syncthreads();
     if (sk || L < 2) continue; // uniform: skip and L are shared
-    // p = tau A22 v in df64, one warp per row (column i, conjugated)
-    for (int i = warp; i < L; i += nw) {
-      const dfc *col = Adf + (size_t)(k + 1 + i) * m + k + 1;
-      dfc acc = {{0.f, 0.f}, {0.f, 0.f}};
-      for (int j = lane; j < L; j += 32)
-        acc = dfcAdd(acc, dfcConjMul(col[j], vsd[j]));
-      for (int o = 16; o > 0; o >>= 1) {
-        dfc oth;
-        oth.re.hi = __shfl_xor_sync(0xffffffffu, acc.re.hi, o);
-        oth.re.lo = __shfl_xor_sync(0xffffffffu, acc.re.lo, o);
-        oth.im.hi = __shfl_xor_sync(0xffffffffu, acc.im.hi, o);
-        oth.im.lo = __shfl_xor_sync(0xffffffffu, acc.im.lo, o);
-        acc = dfcAdd(acc, oth);
+    // p = tau A22 v in df64: a thread per row, over the row (consecutive
+    // threads read consecutive elements of each column), two accumulators
+    for (int i = tid; i < L; i += nt) {
+      const dfc *row = Adf + (size_t)(k + 1) * m + k + 1 + i;
+      dfc a0 = {{0.f, 0.f}, {0.f, 0.f}}, a1 = a0;
+      int j = 0;
+      for (; j + 1 < L; j += 2) {
+        a0 = dfcAdd(a0, dfcMul(row[(size_t)j * m], vsd[j]));
+        a1 = dfcAdd(a1, dfcMul(row[(size_t)(j + 1) * m], vsd[j + 1]));
       }
-      if (lane == 0) p64[i] = cmulD(t, dfcTo(acc));
+      if (j < L) a0 = dfcAdd(a0, dfcMul(row[(size_t)j * m], vsd[j]));
+      p64[i] = cmulD(t, dfcTo(dfcAdd(a0, a1)));
     }
     __syncthreads();
     // w = p - tau/2 (p^H v) v (FP64), then its df64 copy
@@ -667,6 +738,42 @@ __global__ void __launch_bounds__(32 * kBtWarps)
     __syncwarp();
   }
   for (int i = lane; i < m; i += 32) X[(size_t)c * m + i] = x[i];
+}
+
+// btColumnsKernel in double-float arithmetic, for the reflectors of
+// hhTridiagDfKernel (stored as dfc): a warp per column, the column in shared
+// memory as dfc. The dependent chain of a reflector (dot, warp reduction,
+// update) runs on the FP32 pipe instead of the FP64 pipe (64-cycle latency).
+__global__ void __launch_bounds__(32)
+    btColumnsDfKernel(const double *Z, int m, const dfc *Vr,
+                      const double2 *tau, double2 *X) {
+  extern __shared__ dfc xd[];
+  const int c = blockIdx.x, lane = threadIdx.x;
+  if (c >= m) return;
+  for (int i = lane; i < m; i += 32)
+    xd[i] = {dfFrom(Z[(size_t)c * m + i]), {0.f, 0.f}};
+  __syncwarp();
+  for (int k = m - 2; k >= 0; --k) {
+    const double2 t = tau[k];
+    if (t.x == 0.0 && t.y == 0.0) continue;
+    const int L = m - k - 1;
+    const dfc *v = Vr + (size_t)k * m + k + 1;
+    dfc *xx = xd + k + 1;
+    dfc acc = {{0.f, 0.f}, {0.f, 0.f}};
+    for (int i = lane; i < L; i += 32) acc = dfcAdd(acc, dfcConjMul(v[i], xx[i]));
+    for (int o = 16; o > 0; o >>= 1) {
+      dfc oth;
+      oth.re.hi = __shfl_xor_sync(0xffffffffu, acc.re.hi, o);
+      oth.re.lo = __shfl_xor_sync(0xffffffffu, acc.re.lo, o);
+      oth.im.hi = __shfl_xor_sync(0xffffffffu, acc.im.hi, o);
+      oth.im.lo = __shfl_xor_sync(0xffffffffu, acc.im.lo, o);
+      acc = dfcAdd(acc, oth);
+    }
+    const dfc ty = dfcMul(dfcFrom(t), acc);
+    for (int i = lane; i < L; i += 32) xx[i] = dfcSub(xx[i], dfcMul(v[i], ty));
+    __syncwarp();
+  }
+  for (int i = lane; i < m; i += 32) X[(size_t)c * m + i] = dfcTo(xd[i]);
 }
 
 __global__ void finishKernel(int m, int *perm, int *status) {
@@ -780,12 +887,22 @@ void heigMid(const double2 *Ain, int lda, int m, double2 *V, double *w,
     hhTridiagDfKernel<<<1, kMidT, mm * sizeof(dfc), s>>>(Ain, lda, m, Vr, tau,
                                                          d, e);
   }
-  multisectKernel<<<m, 32, 0, s>>>(d, e, m, w);
+  // eigenvalues by double-float multisection; the eigenvectors by FP64
+  // inverse iteration (its backward error sets the orthogonality between
+  // clusters: a double-float solve left 1e-11 there)
+  if (heigMidFp64())
+    multisectKernel<<<m, 32, 0, s>>>(d, e, m, w);
+  else
+    multisectDfKernel<<<m, 32, 0, s>>>(d, e, m, w);
   invIterKernel<<<m, 32, 0, s>>>(d, e, m, w, Z, F);
   clusterMgsKernel<<<m, kT, 0, s>>>(w, m, Z);
-  btColumnsKernel<<<(m + kBtWarps - 1) / kBtWarps, 32 * kBtWarps,
-                    kBtWarps * (size_t)m * sizeof(double2), s>>>(Z, m, Vr, tau,
-                                                                  V);
+  if (heigMidFp64())
+    btColumnsKernel<<<(m + kBtWarps - 1) / kBtWarps, 32 * kBtWarps,
+                      kBtWarps * (size_t)m * sizeof(double2), s>>>(Z, m, Vr,
+                                                                   tau, V);
+  else
+    btColumnsDfKernel<<<m, 32, (size_t)m * sizeof(dfc), s>>>(
+        Z, m, reinterpret_cast<const dfc *>(Vr), tau, V);
   finishKernel<<<(m + 255) / 256, 256, 0, s>>>(m, perm, status);
 }
 

@@ -1,9 +1,9 @@
 """The projected Hermitian eigensolver (ncgm_heig) against numpy: the
-shared-memory Jacobi (m <= 80, FP64 and double-float rotations), the
-one-CTA Householder tridiagonalisation (NCGM_HEIG_MID=1, m <= 112, in a
-child process) and the multi-kernel tridiagonal solver (m > 80), on generic
-spectra and on time-reversal symmetric matrices whose levels are all twofold
-(Kramers)."""
+shared-memory FP64 Jacobi (FP64 form, m <= 80), the one-CTA double-float
+Householder method (FP32 forms, m <= 112), the double-float Jacobi
+(NCGM_HEIG_MID=0, m <= 80, in a child process) and the multi-kernel
+tridiagonal solver (above those sizes), on generic spectra and on
+time-reversal symmetric matrices whose levels are all twofold (Kramers)."""
 import numpy as np
 import pytest
 
@@ -28,6 +28,7 @@ def _herm(m, rng, kramers):
 @pytest.mark.parametrize("m,kramers,precision", [
     (24, False, abi.FP64), (60, True, abi.FP32), (80, False, abi.FP32_TC),
     (2, False, abi.FP32), (24, True, abi.FP32), (48, False, abi.FP32_TC),
+    (100, True, abi.FP32), (112, False, abi.FP32_TC), (114, True, abi.FP32),
     (81, False, abi.FP64), (150, True, abi.FP64), (192, False, abi.FP32),
     (320, True, abi.FP64), (480, False, abi.FP64)])
 def test_heig_matches_numpy(m, kramers, precision):
@@ -72,20 +73,21 @@ print(np.abs(w - ref).max() / scale, np.abs(V.conj().T @ V - np.eye(m)).max(),
 
 
 @pytest.mark.parametrize("m,kramers", [(2, False), (24, True), (60, True),
-                                       (80, False), (100, True), (112, False)])
-def test_heig_one_cta_householder(m, kramers):
-    """The one-CTA Householder method (NCGM_HEIG_MID=1 selects it for the
-    FP32 forms; the switch is read once per process, so a child runs it)."""
+                                       (80, False)])
+def test_heig_double_float_jacobi(m, kramers):
+    """The double-float Jacobi that the FP32 forms used before the one-CTA
+    Householder method (NCGM_HEIG_MID=0 selects it; the switch is read once
+    per process, so a child runs it)."""
     import os
     import subprocess
     import sys
     here = os.path.dirname(os.path.abspath(__file__))
-    env = dict(os.environ, NCGM_HEIG_MID="1")
+    env = dict(os.environ, NCGM_HEIG_MID="0")
     out = subprocess.run([sys.executable, "-c", _MID_CHILD,
                           os.path.dirname(here), str(m), str(int(kramers)),
                           str(abi.FP32)], env=env, capture_output=True,
                          text=True, cwd=here, check=True).stdout.split()
     eig, orth, res = (float(x) for x in out)
-    print("one-CTA Householder m=%d kramers=%s: eigenvalues %.1e, "
+    print("double-float Jacobi m=%d kramers=%s: eigenvalues %.1e, "
           "orthonormality %.1e, residual %.1e" % (m, kramers, eig, orth, res))
     assert eig <= 1e-12 and orth <= 1e-10 and res <= 1e-11
