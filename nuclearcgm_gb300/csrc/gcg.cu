@@ -161,7 +161,8 @@ static int cholQR2(ncgm_ctx *ctx, const double2 *V, int k, double2 *Q,
                    double2 *Q1, double2 *small, double2 *partials,
                    int maxChunks, int *dKeep, int *dIdx, cudaStream_t s,
                    std::vector<int> *keptOrig = nullptr,
-                   float *tcPart = nullptr, void *vcPart = nullptr) {
+                   float *tcPart = nullptr, void *vcPart = nullptr,
+                   bool fast = false) {
   const size_t N = ctx->N;
   double2 *G = small, *R = small + (size_t)k * k, *T = small + 2 * (size_t)k * k,
           *Tk = small + 3 * (size_t)k * k;
@@ -180,7 +181,7 @@ static int cholQR2(ncgm_ctx *ctx, const double2 *V, int k, double2 *Q,
                   reinterpret_cast<double *>(tcPart), s);
     else
       gram(src, N, cols, src, N, cols, N, G, cols, partials, maxChunks, s);
-    cholDrop(G, cols, cols, 1e-24, R, T, dKeep, s);
+    cholDrop(G, cols, cols, 1e-24, R, T, dKeep, s, fast);
     cudaError_t e = cudaMemcpyAsync(keep.data(), dKeep, sizeof(int) * cols,
                                     cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -312,7 +313,7 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
                             cudaMemcpyDeviceToDevice, s));
   std::vector<int> keptInit;
   int nkept = cholQR2(ctx, V, nev, Q, Q1, Gs, partials, (int)maxChunks, dKeep,
-                      dIdx, s, &keptInit, tcPart, vcPart);
+                      dIdx, s, &keptInit, tcPart, vcPart, fp32);
   if (nkept < 0) return NCGM_ERR_CUDA;
   if (nkept == 0) {
     setError("ncgm_gcg: initial block has no independent columns");
@@ -525,7 +526,7 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
     }
     const int vcols = nconv + nact + pc + nact;
     int m = cholQR2(ctx, V, vcols, Q, Q1, Gs, partials, (int)maxChunks, dKeep,
-                    dIdx, s, nullptr, tcPart, vcPart);
+                    dIdx, s, nullptr, tcPart, vcPart, fp32);
     if (m < 0) return NCGM_ERR_CUDA;
     if (m == 0) {
       setError("ncgm_gcg: search space collapsed");

@@ -601,6 +601,13 @@ void gemmVC(const double2 *V, size_t ldv, int m, const double2 *Cm, int ldc,
 // step instead of a serial dot product per element). The drop rule and
 // T = R^{-1} are those of cholDropKernel.
 constexpr int kCholSmemMax = 80; // 2 m^2 double2 <= 200 KB
+// FAST (the FP32 precision forms): the pivot's root and reciprocal in
+// double-float and R^-1 with a reciprocal diagonal and four partial sums
+// (different roundings, about 1e-14 relative; the second CholQR pass absorbs
+// them). The FP64 form keeps FP64 roots and quotients and one running sum,
+// whose roundings leave the reflection symmetry of a symmetric start intact
+// to the level the FP64 fixed-point tests resolve.
+template <bool FAST>
 __global__ void cholDropSmemKernel(const double2 *G, int ldg, int m,
                                    double dropTol, double2 *R, double2 *T,
                                    int *keep) {
@@ -630,17 +637,26 @@ __global__ void cholDropSmemKernel(const double2 *G, int ldg, int m,
     __syncthreads();
     const double pv = piv;
     if (pv > 0.0) {
-      // sqrt(pv) and its reciprocal in double-float (about 1e-14 relative;
-      // the second CholQR pass absorbs it): an FP64 square root or quotient
-      // takes ~650 cycles on GB300 and these sit on the critical path
-      const dfl sq = dfSqrt(dfFrom(pv));
-      const double rjj = dfTo(sq);
-      const double inv = dfTo(dfDiv(dfl{1.f, 0.f}, sq));
-      for (int i = j + 1 + tid; i < m; i += nt) {
-        const double2 a = A[(size_t)i * m + j];
-        A[(size_t)i * m + j] = make_double2(a.x * inv, a.y * inv);
+      if constexpr (FAST) {
+        // sqrt(pv) and its reciprocal in double-float: an FP64 square root
+        // or quotient takes ~650 cycles on GB300 and these sit on the
+        // critical path
+        const dfl sq = dfSqrt(dfFrom(pv));
+        const double rjj = dfTo(sq);
+        const double inv = dfTo(dfDiv(dfl{1.f, 0.f}, sq));
+        for (int i = j + 1 + tid; i < m; i += nt) {
+          const double2 a = A[(size_t)i * m + j];
+          A[(size_t)i * m + j] = make_double2(a.x * inv, a.y * inv);
+        }
+        if (tid == 0) A[(size_t)j * m + j] = make_double2(rjj, 0.0);
+      } else {
+        const double rjj = sqrt(pv);
+        for (int i = j + 1 + tid; i < m; i += nt) {
+          const double2 a = A[(size_t)i * m + j];
+          A[(size_t)i * m + j] = make_double2(a.x / rjj, a.y / rjj);
+        }
+        if (tid == 0) A[(size_t)j * m + j] = make_double2(rjj, 0.0);
       }
-      if (tid == 0) A[(size_t)j * m + j] = make_double2(rjj, 0.0);
       __syncthreads();
       const int w = m - j - 1;
       for (int e = tid; e < w * w; e += nt) {
@@ -657,47 +673,66 @@ __global__ void cholDropSmemKernel(const double2 *G, int ldg, int m,
     }
     __syncthreads();
   }
-  // T = R^{-1} on the kept columns, one thread per column of T. The
-  // reciprocal diagonal comes first (one quotient per row, in parallel); the
-  // row sums run in four independent partial sums, so the FP64 add chain
-  // (64-cycle latency) is a quarter as long. Dropped rows and columns hold
-  // zeros in R (and T starts at zero), so they add nothing to the sums.
-  for (int i = tid; i < m; i += nt)
-    gd[i] = kp[i] ? 1.0 / A[(size_t)i * m + i].x : 0.0;
-  __syncthreads();
-  for (int c = tid; c < m; c += nt) {
-    if (!kp[c]) continue;
-    for (int i = c; i >= 0; --i) {
-      if (!kp[i]) continue;
-      double2 s0 = make_double2(i == c ? 1.0 : 0.0, 0.0);
-      double2 s1 = make_double2(0.0, 0.0), s2 = s1, s3 = s1;
-      int k = i + 1;
-      for (; k + 3 <= c; k += 4) {
-        const double2 t0 = cmul(A[(size_t)k * m + i], Ts[(size_t)c * m + k]);
-        const double2 t1 =
-            cmul(A[(size_t)(k + 1) * m + i], Ts[(size_t)c * m + k + 1]);
-        const double2 t2 =
-            cmul(A[(size_t)(k + 2) * m + i], Ts[(size_t)c * m + k + 2]);
-        const double2 t3 =
-            cmul(A[(size_t)(k + 3) * m + i], Ts[(size_t)c * m + k + 3]);
-        s0.x -= t0.x;
-        s0.y -= t0.y;
-        s1.x -= t1.x;
-        s1.y -= t1.y;
-        s2.x -= t2.x;
-        s2.y -= t2.y;
-        s3.x -= t3.x;
-        s3.y -= t3.y;
+  if constexpr (FAST) {
+    // T = R^{-1} on the kept columns, one thread per column of T. The
+    // reciprocal diagonal comes first (one quotient per row, in parallel);
+    // the row sums run in four independent partial sums, so the FP64 add
+    // chain (64-cycle latency) is a quarter as long. Dropped rows and columns
+    // hold zeros in R and T, so they add nothing to the sums.
+    for (int i = tid; i < m; i += nt)
+      gd[i] = kp[i] ? 1.0 / A[(size_t)i * m + i].x : 0.0;
+    __syncthreads();
+    for (int c = tid; c < m; c += nt) {
+      if (!kp[c]) continue;
+      for (int i = c; i >= 0; --i) {
+        if (!kp[i]) continue;
+        double2 s0 = make_double2(i == c ? 1.0 : 0.0, 0.0);
+        double2 s1 = make_double2(0.0, 0.0), s2 = s1, s3 = s1;
+        int k = i + 1;
+        for (; k + 3 <= c; k += 4) {
+          const double2 t0 = cmul(A[(size_t)k * m + i], Ts[(size_t)c * m + k]);
+          const double2 t1 =
+              cmul(A[(size_t)(k + 1) * m + i], Ts[(size_t)c * m + k + 1]);
+          const double2 t2 =
+              cmul(A[(size_t)(k + 2) * m + i], Ts[(size_t)c * m + k + 2]);
+          const double2 t3 =
+              cmul(A[(size_t)(k + 3) * m + i], Ts[(size_t)c * m + k + 3]);
+          s0.x -= t0.x;
+          s0.y -= t0.y;
+          s1.x -= t1.x;
+          s1.y -= t1.y;
+          s2.x -= t2.x;
+          s2.y -= t2.y;
+          s3.x -= t3.x;
+          s3.y -= t3.y;
+        }
+        for (; k <= c; ++k) {
+          const double2 t = cmul(A[(size_t)k * m + i], Ts[(size_t)c * m + k]);
+          s0.x -= t.x;
+          s0.y -= t.y;
+        }
+        const double r = gd[i];
+        Ts[(size_t)c * m + i] = make_double2(
+            ((s0.x + s1.x) + (s2.x + s3.x)) * r,
+            ((s0.y + s1.y) + (s2.y + s3.y)) * r);
       }
-      for (; k <= c; ++k) {
-        const double2 t = cmul(A[(size_t)k * m + i], Ts[(size_t)c * m + k]);
-        s0.x -= t.x;
-        s0.y -= t.y;
+    }
+  } else {
+    // T = R^{-1} on the kept columns, one thread per column of T
+    for (int c = tid; c < m; c += nt) {
+      if (!kp[c]) continue;
+      for (int i = c; i >= 0; --i) {
+        if (!kp[i]) continue;
+        double2 sum = make_double2(i == c ? 1.0 : 0.0, 0.0);
+        for (int k = i + 1; k <= c; ++k) {
+          if (!kp[k]) continue;
+          const double2 t = cmul(A[(size_t)k * m + i], Ts[(size_t)c * m + k]);
+          sum.x -= t.x;
+          sum.y -= t.y;
+        }
+        const double rii = A[(size_t)i * m + i].x;
+        Ts[(size_t)c * m + i] = make_double2(sum.x / rii, sum.y / rii);
       }
-      const double r = gd[i];
-      Ts[(size_t)c * m + i] = make_double2(
-          ((s0.x + s1.x) + (s2.x + s3.x)) * r,
-          ((s0.y + s1.y) + (s2.y + s3.y)) * r);
     }
   }
   __syncthreads();
@@ -783,7 +818,7 @@ __global__ void cholInvKernel(const double2 *R, int m, const int *keep,
 }
 
 void cholDrop(const double2 *G, int ldg, int m, double dropTol, double2 *R,
-              double2 *T, int *keep, cudaStream_t s) {
+              double2 *T, int *keep, cudaStream_t s, bool fast) {
   if (m > kCholSmemMax) {
     const unsigned gm = (unsigned)(((size_t)m * m + 255) / 256);
     cholCopyKernel<<<gm, 256, 0, s>>>(G, ldg, m, R, T);
@@ -799,14 +834,20 @@ void cholDrop(const double2 *G, int ldg, int m, double dropTol, double2 *R,
   }
   if (m <= kCholSmemMax) {
     static const bool attr = [] {
-      cudaFuncSetAttribute(cholDropSmemKernel,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           2 * kCholSmemMax * kCholSmemMax * (int)sizeof(double2));
+      for (auto k : {cholDropSmemKernel<false>, cholDropSmemKernel<true>})
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             2 * kCholSmemMax * kCholSmemMax *
+                                 (int)sizeof(double2));
       return true;
     }();
     (void)attr;
-    cholDropSmemKernel<<<1, 256, 2 * (size_t)m * m * sizeof(double2), s>>>(
-        G, ldg, m, dropTol, R, T, keep);
+    const size_t smem = 2 * (size_t)m * m * sizeof(double2);
+    if (fast)
+      cholDropSmemKernel<true><<<1, 256, smem, s>>>(G, ldg, m, dropTol, R, T,
+                                                     keep);
+    else
+      cholDropSmemKernel<false><<<1, 256, smem, s>>>(G, ldg, m, dropTol, R, T,
+                                                      keep);
     return;
   }
   cholDropKernel<<<1, 256, 0, s>>>(G, ldg, m, dropTol, R, T, keep);

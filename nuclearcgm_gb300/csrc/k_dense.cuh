@@ -40,8 +40,9 @@ void gemmVC(const double2 *V, size_t ldv, int m, const double2 *C, int ldc,
             int k, double2 *Y, size_t ldy, size_t N, double beta,
             cudaStream_t s);
 // Cholesky of Gram G with MGS-equivalent drop; T = R^{-1}; keep flags.
+// fast: the FP32 forms' variant (double-float pivot roots and reciprocals).
 void cholDrop(const double2 *G, int ldg, int m, double dropTol, double2 *R,
-              double2 *T, int *keep, cudaStream_t s);
+              double2 *T, int *keep, cudaStream_t s, bool fast = false);
 // Multi-kernel Hermitian eigensolver for m > 80 (k_heig_large.cu): Householder
 // tridiagonalisation, bisection, inverse iteration, back-transformation.
 void heigLarge(const double2 *A, int lda, int m, double2 *V, double *w,

@@ -62,8 +62,13 @@ def gcg_step64(precision=abi.FP64):
     ctx.close()
 
 
-CASES = {"tcgram": tcgram, "hf_o16": hf_o16, "hf_ca40_tc": hf_ca40_tc,
-         "gcg_step64": gcg_step64}
+def hf_o16_tc():
+    """Four HF iterations of 16O in the mixed tensor-core form."""
+    hf_o16(abi.FP32_TC)
+
+
+CASES = {"tcgram": tcgram, "hf_o16": hf_o16, "hf_o16_tc": hf_o16_tc,
+         "hf_ca40_tc": hf_ca40_tc, "gcg_step64": gcg_step64}
 
 if __name__ == "__main__":
     CASES[sys.argv[1] if len(sys.argv) > 1 else "tcgram"]()
