@@ -601,13 +601,95 @@ void gemmVC(const double2 *V, size_t ldv, int m, const double2 *Cm, int ldc,
 // step instead of a serial dot product per element). The drop rule and
 // T = R^{-1} are those of cholDropKernel.
 constexpr int kCholSmemMax = 80; // 2 m^2 double2 <= 200 KB
-// FAST (the FP32 precision forms): the pivot's root and reciprocal in
-// double-float and R^-1 with a reciprocal diagonal and four partial sums
-// (different roundings, about 1e-14 relative; the second CholQR pass absorbs
-// them). The FP64 form keeps FP64 roots and quotients and one running sum,
-// whose roundings leave the reflection symmetry of a symmetric start intact
-// to the level the FP64 fixed-point tests resolve.
-template <bool FAST>
+// The FP32 forms' CholQR factor with the matrix held as double-float in
+// shared memory: the O(m^3) trailing updates and R^-1 run on the FP32 pipe
+// (an FP64 FMA has 64-cycle latency and the FP64 pipe 2 per clock per SM on
+// GB300), the pivot test in FP64. About 1e-14 relative accuracy; the second
+// CholQR pass absorbs it. Same drop rule, outputs and layout as
+// cholDropSmemKernel.
+__global__ void cholDropDfKernel(const double2 *G, int ldg, int m,
+                                 double dropTol, double2 *R, double2 *T,
+                                 int *keep) {
+  extern __shared__ dfc cdf[];
+  dfc *A = cdf;              // m x m column-major; upper triangle -> R
+  dfc *Ts = cdf + m * m;     // T
+  __shared__ int kp[kCholSmemMax];
+  __shared__ double gd[kCholSmemMax]; // the Gram diagonal (drop floor)
+  __shared__ dfl rinv[kCholSmemMax];
+  __shared__ int pivOk;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const dfc zero = {{0.f, 0.f}, {0.f, 0.f}};
+  for (int e = tid; e < m * m; e += nt) {
+    const double2 g = G[(size_t)(e / m) * ldg + (e % m)];
+    A[e] = dfcFrom(g);
+    Ts[e] = zero;
+    if (e / m == e % m) gd[e % m] = g.x;
+  }
+  __syncthreads();
+  for (int j = 0; j < m; ++j) {
+    if (tid == 0) {
+      const double d = dfTo(A[(size_t)j * m + j].re);
+      const double floor =
+          fmax(dropTol, 64.0 * 2.220446049250313e-16 * gd[j]);
+      pivOk = (d > floor) ? 1 : 0;
+      kp[j] = pivOk;
+    }
+    __syncthreads();
+    if (pivOk) {
+      const dfl sq = dfSqrt(A[(size_t)j * m + j].re);
+      const dfl inv = dfDiv(dfl{1.f, 0.f}, sq);
+      for (int i = j + 1 + tid; i < m; i += nt) {
+        dfc &a = A[(size_t)i * m + j];
+        a = {dfMul(a.re, inv), dfMul(a.im, inv)};
+      }
+      if (tid == 0) {
+        A[(size_t)j * m + j] = {sq, {0.f, 0.f}};
+        rinv[j] = inv;
+      }
+      __syncthreads();
+      const int w = m - j - 1;
+      for (int e = tid; e < w * w; e += nt) {
+        const int a = j + 1 + e % w, b = j + 1 + e / w;
+        if (a <= b) {
+          const dfc t = dfcConjMul(A[(size_t)a * m + j], A[(size_t)b * m + j]);
+          dfc &x = A[(size_t)b * m + a];
+          x = dfcSub(x, t);
+        }
+      }
+    } else {
+      for (int i = j + tid; i < m; i += nt) A[(size_t)i * m + j] = zero;
+      if (tid == 0) rinv[j] = {0.f, 0.f};
+    }
+    __syncthreads();
+  }
+  // T = R^{-1} on the kept columns, one thread per column; dropped rows and
+  // columns hold zeros in R and T, so they add nothing to the sums
+  for (int c = tid; c < m; c += nt) {
+    if (!kp[c]) continue;
+    for (int i = c; i >= 0; --i) {
+      if (!kp[i]) continue;
+      dfc s0 = {{i == c ? 1.f : 0.f, 0.f}, {0.f, 0.f}}, s1 = zero;
+      int k = i + 1;
+      for (; k + 1 <= c; k += 2) {
+        s0 = dfcSub(s0, dfcMul(A[(size_t)k * m + i], Ts[(size_t)c * m + k]));
+        s1 = dfcSub(s1, dfcMul(A[(size_t)(k + 1) * m + i],
+                               Ts[(size_t)c * m + k + 1]));
+      }
+      if (k <= c)
+        s0 = dfcSub(s0, dfcMul(A[(size_t)k * m + i], Ts[(size_t)c * m + k]));
+      const dfc sum = dfcAdd(s0, s1);
+      Ts[(size_t)c * m + i] = {dfMul(sum.re, rinv[i]), dfMul(sum.im, rinv[i])};
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < m * m; e += nt) {
+    const int row = e % m, col = e / m;
+    R[e] = row <= col ? dfcTo(A[e]) : make_double2(0, 0);
+    T[e] = dfcTo(Ts[e]);
+  }
+  for (int j = tid; j < m; j += nt) keep[j] = kp[j];
+}
+
 __global__ void cholDropSmemKernel(const double2 *G, int ldg, int m,
                                    double dropTol, double2 *R, double2 *T,
                                    int *keep) {
@@ -637,26 +719,12 @@ __global__ void cholDropSmemKernel(const double2 *G, int ldg, int m,
     __syncthreads();
     const double pv = piv;
     if (pv > 0.0) {
-      if constexpr (FAST) {
-        // sqrt(pv) and its reciprocal in double-float: an FP64 square root
-        // or quotient takes ~650 cycles on GB300 and these sit on the
-        // critical path
-        const dfl sq = dfSqrt(dfFrom(pv));
-        const double rjj = dfTo(sq);
-        const double inv = dfTo(dfDiv(dfl{1.f, 0.f}, sq));
-        for (int i = j + 1 + tid; i < m; i += nt) {
-          const double2 a = A[(size_t)i * m + j];
-          A[(size_t)i * m + j] = make_double2(a.x * inv, a.y * inv);
-        }
-        if (tid == 0) A[(size_t)j * m + j] = make_double2(rjj, 0.0);
-      } else {
-        const double rjj = sqrt(pv);
-        for (int i = j + 1 + tid; i < m; i += nt) {
-          const double2 a = A[(size_t)i * m + j];
-          A[(size_t)i * m + j] = make_double2(a.x / rjj, a.y / rjj);
-        }
-        if (tid == 0) A[(size_t)j * m + j] = make_double2(rjj, 0.0);
+      const double rjj = sqrt(pv);
+      for (int i = j + 1 + tid; i < m; i += nt) {
+        const double2 a = A[(size_t)i * m + j];
+        A[(size_t)i * m + j] = make_double2(a.x / rjj, a.y / rjj);
       }
+      if (tid == 0) A[(size_t)j * m + j] = make_double2(rjj, 0.0);
       __syncthreads();
       const int w = m - j - 1;
       for (int e = tid; e < w * w; e += nt) {
@@ -673,66 +741,20 @@ __global__ void cholDropSmemKernel(const double2 *G, int ldg, int m,
     }
     __syncthreads();
   }
-  if constexpr (FAST) {
-    // T = R^{-1} on the kept columns, one thread per column of T. The
-    // reciprocal diagonal comes first (one quotient per row, in parallel);
-    // the row sums run in four independent partial sums, so the FP64 add
-    // chain (64-cycle latency) is a quarter as long. Dropped rows and columns
-    // hold zeros in R and T, so they add nothing to the sums.
-    for (int i = tid; i < m; i += nt)
-      gd[i] = kp[i] ? 1.0 / A[(size_t)i * m + i].x : 0.0;
-    __syncthreads();
-    for (int c = tid; c < m; c += nt) {
-      if (!kp[c]) continue;
-      for (int i = c; i >= 0; --i) {
-        if (!kp[i]) continue;
-        double2 s0 = make_double2(i == c ? 1.0 : 0.0, 0.0);
-        double2 s1 = make_double2(0.0, 0.0), s2 = s1, s3 = s1;
-        int k = i + 1;
-        for (; k + 3 <= c; k += 4) {
-          const double2 t0 = cmul(A[(size_t)k * m + i], Ts[(size_t)c * m + k]);
-          const double2 t1 =
-              cmul(A[(size_t)(k + 1) * m + i], Ts[(size_t)c * m + k + 1]);
-          const double2 t2 =
-              cmul(A[(size_t)(k + 2) * m + i], Ts[(size_t)c * m + k + 2]);
-          const double2 t3 =
-              cmul(A[(size_t)(k + 3) * m + i], Ts[(size_t)c * m + k + 3]);
-          s0.x -= t0.x;
-          s0.y -= t0.y;
-          s1.x -= t1.x;
-          s1.y -= t1.y;
-          s2.x -= t2.x;
-          s2.y -= t2.y;
-          s3.x -= t3.x;
-          s3.y -= t3.y;
-        }
-        for (; k <= c; ++k) {
-          const double2 t = cmul(A[(size_t)k * m + i], Ts[(size_t)c * m + k]);
-          s0.x -= t.x;
-          s0.y -= t.y;
-        }
-        const double r = gd[i];
-        Ts[(size_t)c * m + i] = make_double2(
-            ((s0.x + s1.x) + (s2.x + s3.x)) * r,
-            ((s0.y + s1.y) + (s2.y + s3.y)) * r);
+  // T = R^{-1} on the kept columns, one thread per column of T
+  for (int c = tid; c < m; c += nt) {
+    if (!kp[c]) continue;
+    for (int i = c; i >= 0; --i) {
+      if (!kp[i]) continue;
+      double2 sum = make_double2(i == c ? 1.0 : 0.0, 0.0);
+      for (int k = i + 1; k <= c; ++k) {
+        if (!kp[k]) continue;
+        const double2 t = cmul(A[(size_t)k * m + i], Ts[(size_t)c * m + k]);
+        sum.x -= t.x;
+        sum.y -= t.y;
       }
-    }
-  } else {
-    // T = R^{-1} on the kept columns, one thread per column of T
-    for (int c = tid; c < m; c += nt) {
-      if (!kp[c]) continue;
-      for (int i = c; i >= 0; --i) {
-        if (!kp[i]) continue;
-        double2 sum = make_double2(i == c ? 1.0 : 0.0, 0.0);
-        for (int k = i + 1; k <= c; ++k) {
-          if (!kp[k]) continue;
-          const double2 t = cmul(A[(size_t)k * m + i], Ts[(size_t)c * m + k]);
-          sum.x -= t.x;
-          sum.y -= t.y;
-        }
-        const double rii = A[(size_t)i * m + i].x;
-        Ts[(size_t)c * m + i] = make_double2(sum.x / rii, sum.y / rii);
-      }
+      const double rii = A[(size_t)i * m + i].x;
+      Ts[(size_t)c * m + i] = make_double2(sum.x / rii, sum.y / rii);
     }
   }
   __syncthreads();
@@ -834,20 +856,25 @@ void cholDrop(const double2 *G, int ldg, int m, double dropTol, double2 *R,
   }
   if (m <= kCholSmemMax) {
     static const bool attr = [] {
-      for (auto k : {cholDropSmemKernel<false>, cholDropSmemKernel<true>})
-        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             2 * kCholSmemMax * kCholSmemMax *
-                                 (int)sizeof(double2));
+      cudaFuncSetAttribute(cholDropSmemKernel,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           2 * kCholSmemMax * kCholSmemMax * (int)sizeof(double2));
       return true;
     }();
     (void)attr;
     const size_t smem = 2 * (size_t)m * m * sizeof(double2);
+    static const bool dfAttr = [] {
+      cudaFuncSetAttribute(cholDropDfKernel,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           2 * kCholSmemMax * kCholSmemMax * (int)sizeof(dfc));
+      return true;
+    }();
+    (void)dfAttr;
     if (fast)
-      cholDropSmemKernel<true><<<1, 256, smem, s>>>(G, ldg, m, dropTol, R, T,
-                                                     keep);
+      cholDropDfKernel<<<1, 256, 2 * (size_t)m * m * sizeof(dfc), s>>>(
+          G, ldg, m, dropTol, R, T, keep);
     else
-      cholDropSmemKernel<false><<<1, 256, smem, s>>>(G, ldg, m, dropTol, R, T,
-                                                      keep);
+      cholDropSmemKernel<<<1, 256, smem, s>>>(G, ldg, m, dropTol, R, T, keep);
     return;
   }
   cholDropKernel<<<1, 256, 0, s>>>(G, ldg, m, dropTol, R, T, keep);

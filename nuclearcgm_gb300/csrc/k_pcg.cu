@@ -13,6 +13,7 @@
 
 #include <cfloat>
 #include <cstdlib>
+#include <mutex>
 #include <vector>
 
 namespace ncgm {
@@ -487,25 +488,49 @@ struct ExitPoll {
   int device = -1;
   int *host = nullptr; // pinned, kPollSlots
   cudaEvent_t ev[kPollEvents];
+  cudaEvent_t done = nullptr; // after the last copy of the previous user
 };
-// one pinned slot array and event ring per host thread and device
-ExitPoll *exitPoll() {
-  thread_local std::vector<ExitPoll *> pool;
+// A pool of pinned slot arrays and event rings, per device: a PCG run takes
+// one out and returns it when it ends. The pool outlives short-lived host
+// threads (the HF driver solves the protons on a new thread each iteration),
+// so nothing is allocated per thread.
+std::mutex g_pollMutex;
+std::vector<ExitPoll *> g_pollFree;
+
+ExitPoll *exitPollTake() {
   int dev = 0;
   cudaGetDevice(&dev);
-  for (auto *p : pool)
-    if (p->device == dev) return p;
+  {
+    std::lock_guard<std::mutex> lock(g_pollMutex);
+    for (size_t i = 0; i < g_pollFree.size(); ++i)
+      if (g_pollFree[i]->device == dev) {
+        ExitPoll *p = g_pollFree[i];
+        g_pollFree.erase(g_pollFree.begin() + (long)i);
+        // the previous user's last copies into p->host have landed
+        cudaEventSynchronize(p->done);
+        return p;
+      }
+  }
   auto *p = new ExitPoll;
   p->device = dev;
   if (cudaHostAlloc(reinterpret_cast<void **>(&p->host),
                     sizeof(int) * kPollSlots, cudaHostAllocDefault) !=
       cudaSuccess) {
+    cudaGetLastError();
     delete p;
     return nullptr;
   }
   for (auto &e : p->ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
-  pool.push_back(p);
+  cudaEventCreateWithFlags(&p->done, cudaEventDisableTiming);
   return p;
+}
+
+// back to the pool once the copies queued on s have completed
+void exitPollGive(ExitPoll *p, cudaStream_t s) {
+  if (!p) return;
+  cudaEventRecord(p->done, s);
+  std::lock_guard<std::mutex> lock(g_pollMutex);
+  g_pollFree.push_back(p);
 }
 
 namespace {
@@ -572,7 +597,7 @@ void pcgRun(const PcgPlan<T> &pl, cudaStream_t s) {
   // `it` the host reads the count of step it - kLag (already complete, so
   // the device queue never drains) and stops issuing steps once every
   // column has finished. Later steps would only launch no-op kernels.
-  ExitPoll *poll = pl.ndone ? exitPoll() : nullptr;
+  ExitPoll *poll = pl.ndone ? exitPollTake() : nullptr;
   auto mark = [&](int slot) {
     if (!poll) return;
     cudaMemcpyAsync(poll->host + slot, pl.ndone, sizeof(int),
@@ -631,6 +656,7 @@ void pcgRun(const PcgPlan<T> &pl, cudaStream_t s) {
       step();
     if (it + 1 < kPollSlots) mark(it + 1);
   }
+  exitPollGive(poll, s);
   if (exec) cudaGraphExecDestroy(exec);
   if (graph) cudaGraphDestroy(graph);
   if (pl.AX64)

@@ -28,11 +28,11 @@ def tcgram():
     ctx.close()
 
 
-def hf_o16(precision=abi.FP64):
-    """Four HF iterations of 16O (SLy4, box 18 fm, 30^3)."""
+def hf_o16(precision=abi.FP64, iterations=4):
+    """HF iterations of 16O (SLy4, box 18 fm, 30^3), four by default."""
     data = {"functional": "SLy4", "nucleus": {"A": 16, "Z": 8},
             "box": {"boxSize": 18.0, "axisMeshPoints": 30},
-            "maxIterations": 4, "energyTol": 0.0}
+            "maxIterations": iterations, "energyTol": 0.0}
     res, _ = hf_run(config.from_input(data, precision=precision))
     print("iterations %d wall %.3f s (gcg %.3f, poisson %.3f)" % (
         res.iterations, res.wall_s, res.t_gcg_s, res.t_poisson_s))
@@ -62,13 +62,18 @@ def gcg_step64(precision=abi.FP64):
     ctx.close()
 
 
-def hf_o16_tc():
-    """Four HF iterations of 16O in the mixed tensor-core form."""
-    hf_o16(abi.FP32_TC)
+def hf_o16_tc(iterations=4):
+    """HF iterations of 16O in the mixed tensor-core form."""
+    hf_o16(abi.FP32_TC, iterations)
 
 
 CASES = {"tcgram": tcgram, "hf_o16": hf_o16, "hf_o16_tc": hf_o16_tc,
          "hf_ca40_tc": hf_ca40_tc, "gcg_step64": gcg_step64}
 
 if __name__ == "__main__":
-    CASES[sys.argv[1] if len(sys.argv) > 1 else "tcgram"]()
+    # optional second argument: the HF iteration count of the hf_* cases
+    name = sys.argv[1] if len(sys.argv) > 1 else "tcgram"
+    if len(sys.argv) > 2:
+        CASES[name](iterations=int(sys.argv[2]))
+    else:
+        CASES[name]()

@@ -53,11 +53,11 @@ CASES = {
     "ca40_sly4_n36": (CA40, 400, 1e-8, None),
     # 24Mg, SkM*, 32^3, box 20 fm, HF+BCS with 24 states per isospin, at
     # points 0, 4 and 15 of the curve (beta2 = -0.3, -0.0867, 0.5) with the
-    # curve-mode constraint set (the soft points near beta2 = 0.07 still move
-    # by 2e-5 MeV per iteration after 400 iterations, so none of them is a
-    # fixture)
+    # curve-mode constraint set. The paired points near the spherical shape
+    # converge slowly (point 4 still moves by 2e-5 MeV per iteration after
+    # 400 iterations, point 7 likewise), so point 4 runs 1200.
     "mg24_skm_n32_p00": (MG24, 400, 1e-8, 0),
-    "mg24_skm_n32_p04": (MG24, 400, 1e-8, 4),
+    "mg24_skm_n32_p04": (MG24, 1200, 1e-8, 4),
     "mg24_skm_n32_p15": (MG24, 400, 1e-8, 15),
 }
 
