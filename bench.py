@@ -254,7 +254,11 @@ def _curve_cfg2():
     out["beta_fp64"] = [round(r.beta, 5) for r in res["fp64"]]
     out["iterations_fp64"] = [r.iterations for r in res["fp64"]]
     out["converged"] = [bool(r.converged) for r in res["fp64"]]
+    out["abs_dE_tc_vs_fp64_MeV"] = [float("%.3g" % x)
+                                    for x in np.abs(etc - e64)]
     out["max_abs_dE_tc_vs_fp64_MeV"] = float(np.abs(etc - e64).max())
+    out["iterations_tc"] = [r.iterations for r in res["tc"]]
+    out["converged_tc"] = [bool(r.converged) for r in res["tc"]]
     # the oracle's measured seconds per HF iteration at this size
     per_it = []
     for name in ("mg24_skm_n32_p00", "mg24_skm_n32_p07", "mg24_skm_n32_p15"):
