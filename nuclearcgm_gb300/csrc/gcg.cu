@@ -262,7 +262,7 @@ int gcgRun(ncgm_ctx *ctx, int species, const double2 *Xinit, int xcols,
   if (tc) {
     tcPart = static_cast<float *>(ctx->buf(
         11, sizeof(double) * exactGramScratchDoubles(N, vmax, vmax) + 256));
-    vcPart = ctx->buf(31, exactVCScratchBytes(vmax, vmax));
+    vcPart = ctx->buf(31, exactVCScratchBytes(N, vmax, vmax));
     if (!tcPart || !vcPart) return NCGM_ERR_NOMEM;
   }
   // the projected eigensolver's workspace (Householder methods)
@@ -750,7 +750,10 @@ extern "C" int ncgm_gram(ncgm_ctx *ctx, const double *A, int p,
       return nullptr;
     return d;
   };
-  const double2 *dA = stage(A, p, 26), *dB = stage(B, q, 27);
+  // a Gram of a block with itself stages it once (the tensor-core form then
+  // digitises it once)
+  const double2 *dA = stage(A, p, 26);
+  const double2 *dB = (B == A && q == p) ? dA : stage(B, q, 27);
   if (!dA || !dB) return NCGM_ERR_NOMEM;
   const bool devOut = isDevicePtr(C);
   double2 *dC = devOut ? reinterpret_cast<double2 *>(C)
@@ -820,7 +823,7 @@ extern "C" int ncgm_vc(ncgm_ctx *ctx, const double *V, int m, const double *C,
                              ctx->buf(28, N * (size_t)k * sizeof(double2)));
   if (!dY) return NCGM_ERR_NOMEM;
   if (precision == NCGM_FP32_TC) {
-    void *part = ctx->buf(29, exactVCScratchBytes(m, k));
+    void *part = ctx->buf(29, exactVCScratchBytes(N, m, k));
     if (!part) return NCGM_ERR_NOMEM;
     gemmVCExact(dV, N, m, dC, m, k, dY, N, N, part, s);
   } else {

@@ -269,7 +269,7 @@ struct Run {
     if (!tcScr) {
       int M = std::max(sp[0].orb, sp[1].orb);
       size_t b = std::max(exactGramScratchDoubles(N, M, M) * sizeof(double),
-                          exactVCScratchBytes(M, M));
+                          exactVCScratchBytes(N, M, M));
       tcScr = alloc<char>(b + 1024);
     }
     return tcScr;
@@ -288,7 +288,7 @@ struct Run {
       // both bounds hold for every window size nS <= M
       const size_t b =
           std::max(exactGramScratchDoubles(ns, M, M) * sizeof(double),
-                   exactVCScratchBytes(M, M));
+                   exactVCScratchBytes(N, M, M));
       w.gemmExact = alloc<char>(b + 1024);
       if (!w.gemmExact) return nullptr;
     }

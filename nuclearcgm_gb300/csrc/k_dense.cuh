@@ -20,8 +20,9 @@ void gramTC(const double2 *A, size_t lda, int p, const double2 *B, size_t ldb,
 size_t tcGramPartialFloats(size_t N, int p, int q);
 int *tcGramErrWord();
 // C = A^H B on the tensor cores to ~1e-13 relative: error-free splitting into
-// BF16 integer digits, exact FP32 level sums, FP64 combination
-// (k_tcgram_exact.cu). scratch: exactGramScratchDoubles(N, p, q) doubles.
+// BF16 integer digits (digitised once per operand), exact FP32 level sums,
+// exact 64-bit combination (k_tcgram_exact.cu). scratch:
+// exactGramScratchDoubles(N, p, q) doubles, 16-byte aligned.
 void gramTCExact(const double2 *A, size_t lda, int p, const double2 *B,
                  size_t ldb, int q, size_t N, double2 *C, int ldc,
                  double *scratch, cudaStream_t s);
@@ -29,11 +30,11 @@ size_t exactGramScratchDoubles(size_t N, int p, int q);
 int *exactGramErrWord();
 // Y = V C on the tensor cores with the exact digit products of gramTCExact
 // (~1e-12 relative of the column maxima; k_tcgram_exact.cu). scratch:
-// exactVCScratchBytes(m, k) bytes.
+// exactVCScratchBytes(N, m, k) bytes, 16-byte aligned.
 void gemmVCExact(const double2 *V, size_t ldv, int m, const double2 *C,
                  int ldc, int k, double2 *Y, size_t ldy, size_t N,
                  void *scratch, cudaStream_t s, bool accum = false);
-size_t exactVCScratchBytes(int m, int k);
+size_t exactVCScratchBytes(size_t N, int m, int k);
 // Y = V C + beta Y (V: N x m with m <= 1600, C: m x k; C is staged in
 // shared memory in blocks of columns).
 void gemmVC(const double2 *V, size_t ldv, int m, const double2 *C, int ldc,

@@ -2,6 +2,7 @@
 (the commands in profiles/*.md run these).
 
   python -m nuclearcgm_gb300.profile_cases tcgram      # ncgm_gram, 128 000 x 96
+  python -m nuclearcgm_gb300.profile_cases tcprod      # 40Ca shape: A^H A, V C
   python -m nuclearcgm_gb300.profile_cases hf_o16      # 4 HF iterations, 16O 30^3
   python -m nuclearcgm_gb300.profile_cases hf_ca40_tc  # 6 HF iterations, 40Ca 36^3
   python -m nuclearcgm_gb300.profile_cases gcg_step64  # one GCG step, 40^3 x 64
@@ -25,6 +26,28 @@ def tcgram():
         _check(load().ncgm_gram(ctx.h, A.ctypes.data, p, A.ctypes.data, p,
                                 C.ctypes.data, prec))
     print("max |A^H A - I| = %.2e" % np.abs(C - np.eye(p)).max())
+    ctx.close()
+
+
+def tcprod():
+    """The exact-digit products at the 40Ca tensor-core run's shape
+    (2*36^3 = 93 312 rows, 60 columns): the self-Gram A^H A, then Y = A C
+    with C 60 x 20."""
+    n, p, k = 36, 60, 20
+    N = 2 * n ** 3
+    ctx = Context(Grid(n, 10.5), 4)
+    A = workloads.orthonormal_block(N, p, seed=1)
+    Cm = np.asfortranarray(np.random.default_rng(2).normal(size=(p, k))
+                           + 0j)
+    G = np.zeros((p, p), np.complex128, order="F")
+    Y = np.zeros((N, k), np.complex128, order="F")
+    _check(load().ncgm_gram(ctx.h, A.ctypes.data, p, A.ctypes.data, p,
+                            G.ctypes.data, abi.FP32_TC))
+    _check(load().ncgm_vc(ctx.h, A.ctypes.data, p, Cm.ctypes.data, k,
+                          Y.ctypes.data, abi.FP32_TC))
+    ref = A @ Cm
+    print("max |A^H A - I| = %.2e, max |Y - A C| / max |A C| = %.2e" % (
+        np.abs(G - np.eye(p)).max(), np.abs(Y - ref).max() / np.abs(ref).max()))
     ctx.close()
 
 
@@ -67,7 +90,7 @@ def hf_o16_tc(iterations=4):
     hf_o16(abi.FP32_TC, iterations)
 
 
-CASES = {"tcgram": tcgram, "hf_o16": hf_o16, "hf_o16_tc": hf_o16_tc,
+CASES = {"tcgram": tcgram, "tcprod": tcprod, "hf_o16": hf_o16, "hf_o16_tc": hf_o16_tc,
          "hf_ca40_tc": hf_ca40_tc, "gcg_step64": gcg_step64}
 
 if __name__ == "__main__":

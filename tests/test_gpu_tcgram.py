@@ -70,6 +70,28 @@ def test_exact_digit_gram(n, p, q):
     ctx.close()
 
 
+@pytest.mark.parametrize("n,p", [(12, 5), (16, 70), (30, 32), (24, 100)])
+def test_exact_digit_self_gram(n, p):
+    """A^H A with both operands the same buffer: the block is digitised once
+    and output tiles inside its own digit tile read B from there."""
+    N = 2 * n ** 3
+    ctx = ng.Context(ng.Grid(n, 0.5 * (n - 1) * 0.6), 4)
+    A = workloads.orthonormal_block(N, p, seed=3 * n + p)
+    A[:, 0] *= 1e-6
+    A[:, -1] *= 3.0
+    ref = A.conj().T @ A
+    g = _gram(ctx, A, A, abi.FP32_TC)
+    # the digit error of entry (i, j) scales with |a_i| |a_j| (per-column
+    # scaling), so it is measured against sqrt(G_ii G_jj)
+    d = np.sqrt(np.abs(np.diag(ref)))
+    err = (np.abs(g - ref) / np.outer(d, d)).max()
+    print("n=%d p=%d: exact-digit self Gram max error %.2e (of |a_i| |a_j|)"
+          % (n, p, err))
+    assert err <= 5e-12
+    assert (np.abs(g - g.conj().T) / np.outer(d, d)).max() <= 5e-12
+    ctx.close()
+
+
 def _vc(ctx, V, Cm, precision):
     V = np.asfortranarray(V, np.complex128)
     Cm = np.asfortranarray(Cm, np.complex128)
