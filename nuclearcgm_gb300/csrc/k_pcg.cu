@@ -12,6 +12,7 @@
 #include <type_traits>
 
 #include <cfloat>
+#include <chrono>
 #include <cstdlib>
 #include <mutex>
 #include <vector>
@@ -483,12 +484,13 @@ __global__ void pcgZeroKernel(typename C2<T>::type *Wv, size_t N,
 
 } // namespace
 
-constexpr int kLag = 2, kPollEvents = 4, kPollSlots = 4096;
+constexpr int kLag = 2, kPollSlots = 4096;
 struct ExitPoll {
   int device = -1;
-  int *host = nullptr; // pinned, kPollSlots
-  cudaEvent_t ev[kPollEvents];
-  cudaEvent_t done = nullptr; // after the last copy of the previous user
+  int *host = nullptr;        // pinned, kPollSlots
+  int *hostDev = nullptr;     // the device's address of host
+  int *counter = nullptr;     // device: the next slot to write
+  cudaEvent_t done = nullptr; // after the last write of the previous user
 };
 // A pool of pinned slot arrays and event rings, per device: a PCG run takes
 // one out and returns it when it ends. The pool outlives short-lived host
@@ -514,13 +516,17 @@ ExitPoll *exitPollTake() {
   auto *p = new ExitPoll;
   p->device = dev;
   if (cudaHostAlloc(reinterpret_cast<void **>(&p->host),
-                    sizeof(int) * kPollSlots, cudaHostAllocDefault) !=
-      cudaSuccess) {
+                    sizeof(int) * kPollSlots, cudaHostAllocMapped) !=
+          cudaSuccess ||
+      cudaHostGetDevicePointer(reinterpret_cast<void **>(&p->hostDev),
+                               p->host, 0) != cudaSuccess ||
+      cudaMalloc(reinterpret_cast<void **>(&p->counter), sizeof(int)) !=
+          cudaSuccess) {
     cudaGetLastError();
+    if (p->host) cudaFreeHost(p->host);
     delete p;
     return nullptr;
   }
-  for (auto &e : p->ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
   cudaEventCreateWithFlags(&p->done, cudaEventDisableTiming);
   return p;
 }
@@ -534,6 +540,18 @@ void exitPollGive(ExitPoll *p, cudaStream_t s) {
 }
 
 namespace {
+// the count of finished columns into the next host slot (one thread, after
+// a step's kernels): the host reads it without a copy or an event
+__global__ void pcgMarkKernel(const int *ndone, int *hostSlots,
+                              int *counter) {
+  const int k = *counter;
+  *counter = k + 1;
+  if (k < kPollSlots) {
+    *(volatile int *)(hostSlots + k) = *(volatile const int *)ndone;
+    __threadfence_system();
+  }
+}
+
 __global__ void invDiag32Kernel(const double *c0, double shift, size_t ns,
                                 float *inv) {
   const size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -592,19 +610,37 @@ void pcgRun(const PcgPlan<T> &pl, cudaStream_t s) {
   cudaMemsetAsync(pl.arrive, 0, 2 * sizeof(unsigned) * pl.ncols, s);
   pcgInitFinish<<<pl.ncols, 32, 0, s>>>(pl.st, pl.partials, nblk, pl.tol,
                                         pl.ndone);
-  // Early exit: after the init and after every step the count of finished
-  // columns is copied to pinned host memory behind an event; before step
-  // `it` the host reads the count of step it - kLag (already complete, so
-  // the device queue never drains) and stops issuing steps once every
+  // Early exit: after the init and after every step a one-thread kernel
+  // writes the count of finished columns into the next slot of mapped
+  // pinned host memory (slot 0 after the init, it + 1 after step it); the
+  // host marks a slot unwritten (-1) before it launches the step that
+  // writes it. Before step `it` the host reads the slot of step it - kLag
+  // (so the device queue never drains) and stops issuing steps once every
   // column has finished. Later steps would only launch no-op kernels.
   ExitPoll *poll = pl.ndone ? exitPollTake() : nullptr;
-  auto mark = [&](int slot) {
-    if (!poll) return;
-    cudaMemcpyAsync(poll->host + slot, pl.ndone, sizeof(int),
-                    cudaMemcpyDeviceToHost, s);
-    cudaEventRecord(poll->ev[slot % kPollEvents], s);
+  auto mark = [&]() {
+    if (poll) pcgMarkKernel<<<1, 1, 0, s>>>(pl.ndone, poll->hostDev,
+                                           poll->counter);
   };
-  mark(0);
+  if (poll) {
+    cudaMemsetAsync(poll->counter, 0, sizeof(int), s);
+    poll->host[0] = -1;
+    poll->host[1] = -1;
+  }
+  mark();
+  // waits (bounded, ~10 s, then for the stream) until the slot is written
+  auto readSlot = [&](int slot) -> int {
+    volatile int *h = poll->host + slot;
+    const auto t0 = std::chrono::steady_clock::now();
+    for (unsigned spin = 0; *h == -1; ++spin) {
+      if ((spin & 1023u) == 0 &&
+          std::chrono::steady_clock::now() - t0 > std::chrono::seconds(10)) {
+        cudaStreamSynchronize(s);
+        break;
+      }
+    }
+    return *h;
+  };
   auto step = [&]() {
     pl.apply(pl.P, pl.N, pl.AP, pl.ncols, pl.shift, s);
     pcgDotKernel<T><<<grid, kThreads, 0, s>>>(
@@ -619,8 +655,9 @@ void pcgRun(const PcgPlan<T> &pl, cudaStream_t s) {
     pcgPKernel<T><<<grid, kThreads, 0, s>>>(
         reinterpret_cast<V *>(pl.P), reinterpret_cast<const V *>(pl.Z), pl.N,
         pl.st);
+    mark();
   };
-  // One step is the same four launches with the same arguments every time:
+  // One step is the same five launches with the same arguments every time:
   // after a first direct step (which also settles the stencil's tuned
   // shape), it is captured once into a CUDA graph and replayed, one graph
   // launch per step. NCGM_PCG_GRAPH=0 keeps direct launches.
@@ -630,12 +667,10 @@ void pcgRun(const PcgPlan<T> &pl, cudaStream_t s) {
   cudaGraphExec_t exec = nullptr;
   bool graphFailed = false;
   for (int it = 0; it < pl.maxSteps; ++it) {
-    if (poll && it + 1 - kLag >= 0 && it + 1 - kLag < kPollSlots) {
-      const int slot = it + 1 - kLag;
-      if (cudaEventSynchronize(poll->ev[slot % kPollEvents]) == cudaSuccess &&
-          poll->host[slot] >= pl.ncols)
-        break;
-    }
+    if (poll && it + 1 - kLag >= 0 && it + 1 - kLag < kPollSlots &&
+        readSlot(it + 1 - kLag) >= pl.ncols)
+      break;
+    if (poll && it + 2 < kPollSlots) poll->host[it + 2] = -1;
     if (useGraph && it > 0 && !exec && !graphFailed) {
       if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) ==
           cudaSuccess) {
@@ -654,7 +689,6 @@ void pcgRun(const PcgPlan<T> &pl, cudaStream_t s) {
       cudaGraphLaunch(exec, s);
     else
       step();
-    if (it + 1 < kPollSlots) mark(it + 1);
   }
   exitPollGive(poll, s);
   if (exec) cudaGraphExecDestroy(exec);
