@@ -382,8 +382,10 @@ int ncgm_shell_observables(ncgm_ctx *ctx, const double *Psi, int ncols,
  * NCGM_FP32: tensor cores (tcgen05 kind::tf32 with split TF32 operands,
  * FP32 accumulation over row chunks, FP64 chunk sums; ~2e-6 relative);
  * NCGM_FP32_TC: tensor cores (tcgen05 kind::f16, values split into six
- * 7-bit integer digits held exactly in BF16, exact FP32 sums per digit
- * level, FP64 combination; ~1e-13 relative). */
+ * 7-bit integer digits held exactly in BF16 and written once per operand,
+ * exact FP32 sums per digit level, exact 64-bit combination, FP64 chunk
+ * sums; ~1e-13 relative). With A == B (the same buffer) and p == q the
+ * block is staged and split once. */
 int ncgm_gram(ncgm_ctx *ctx, const double *A, int p, const double *B, int q,
               double *C, int precision);
 
